@@ -1,0 +1,198 @@
+/*
+ * csim.h — C ABI of libcsimgpu.so, the GB300 backend for CircuitSimulator's
+ * stabilizer-rank norm-estimation path.
+ *
+ * Everything here is plain C: pointers, sizes and int status codes.  All
+ * pointer arguments are HOST memory unless the name ends in _dev; the library
+ * copies to and from the GPU itself.  Nothing returned is allocated by the
+ * library (the reference allocates states in the callee and frees them in the
+ * caller, libcirc/stabilizer/stabilizer.c:9-51; here the caller owns every
+ * buffer).  Each csim_ctx owns its own CUDA stream, device buffers and random
+ * generators, so distinct contexts may be used from distinct threads; one
+ * context must not be used by two threads at once.
+ *
+ * Qubit counts are limited to 1..CSIM_MAX_QUBITS (64): one uint64 per row.
+ */
+#ifndef CSIM_H
+#define CSIM_H
+
+#include <stdint.h>
+#include <stdio.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CSIM_MAX_QUBITS 64
+
+/* ------------------------------------------------------------------ status */
+#define CSIM_OK 0
+#define CSIM_ERR_ARG (-1)         /* bad argument (size, range, null)          */
+#define CSIM_ERR_CUDA (-2)        /* a CUDA runtime call failed                */
+#define CSIM_ERR_DEVICE (-3)      /* a kernel flagged an impossible value      */
+#define CSIM_ERR_NOMEM (-4)       /* device or host allocation failed          */
+#define CSIM_ERR_NODEVICE (-5)    /* no CUDA device / no sm_103 device         */
+#define CSIM_ERR_PROTOCOL (-6)    /* malformed backend stdin input             */
+
+/* ------------------------------------------------------------------ types */
+
+/*
+ * One stabilizer state, packed.  Replaces struct StabilizerState
+ * (libcirc/stabilizer/stabilizer.h:5-16), whose matrices are byte-packed
+ * MSB-first bit arrays (libcirc/utils/matrix.c:330-339).
+ *
+ * Row r of G, Gbar and J is one uint64 whose bit c is column c.
+ * D[a] = 2*(2*bit_a(D2) + bit_a(D1)) in {0,2,4,6} (stabilizer.c:55-62).
+ * J[a] bit b set means J_ab = 4.  Only rows/columns < n are meaningful;
+ * everything above n must be zero.
+ */
+typedef struct csim_state {
+    int32_t n;         /* number of qubits, 1..64                     */
+    int32_t k;         /* dimension of the affine space, 0..n         */
+    int32_t Q;         /* constant term of q, in Z8                   */
+    int32_t reserved0; /* must be 0                                   */
+    uint64_t h;        /* shift vector                                */
+    uint64_t D1;       /* low bit of D/2                              */
+    uint64_t D2;       /* high bit of D/2                             */
+    uint64_t reserved1;
+    uint64_t G[CSIM_MAX_QUBITS];
+    uint64_t Gbar[CSIM_MAX_QUBITS];
+    uint64_t J[CSIM_MAX_QUBITS];
+} csim_state;
+
+/*
+ * A Pauli projector Π = Π_r (1 + i^{phase_r} Z(zeta_r) X(xi_r))/2, in the
+ * stdin-protocol encoding (libcirc/utils/comms.c:9-36): phase_r = v in Z4,
+ * xs[r] bit c = x-part on qubit c, zs[r] bit c = z-part.  Replaces struct
+ * Projector (libcirc/utils/comms.h:4-11).
+ */
+typedef struct csim_projector {
+    int32_t nstabs;
+    int32_t nqubits;
+    const int32_t *phase;
+    const uint64_t *xs;
+    const uint64_t *zs;
+} csim_projector;
+
+/* Random-state generators for the samplers. */
+#define CSIM_RNG_PHILOX 0 /* counter-based, one independent stream per state (GPU)   */
+#define CSIM_RNG_LIBC 1   /* the sequence of srand(seed); rand() of the C library:
+                             reproduces the reference's draws sample for sample       */
+
+typedef struct csim_ctx csim_ctx;
+
+/* ------------------------------------------------------------- context */
+
+/* Opens a context on CUDA device `device`.  Fails with CSIM_ERR_NODEVICE if the
+ * device is not an sm_103 part (the kernels are built for sm_103a only). */
+int csim_ctx_create(int device, csim_ctx **out);
+void csim_ctx_destroy(csim_ctx *ctx);
+/* Message of the last failing call on this context ("" if none). */
+const char *csim_last_error(const csim_ctx *ctx);
+/* Number of kernels this context has launched so far. */
+int64_t csim_launch_count(const csim_ctx *ctx);
+
+/* ----------------------------------------------- stabilizer primitives (batched) */
+
+/* eps/p/m of <a[i]|b[i]> for i < count; value = eps * 2^{p/2} * e^{i pi m/4}.
+ * Replaces innerProductExact, libcirc/stabilizer/stabilizer.c:589-659. */
+int csim_inner_product_exact(csim_ctx *ctx, int64_t count, const csim_state *a, const csim_state *b,
+                             int32_t *eps, int32_t *p, int32_t *m);
+
+/* Exponential sum of each state's quadratic form; states are updated in place
+ * exactly as the reference updates them.
+ * Replaces exponentialSumExact, libcirc/stabilizer/stabilizer.c:300-481. */
+int csim_exponential_sum_exact(csim_ctx *ctx, int64_t count, csim_state *s, int32_t *eps, int32_t *p,
+                               int32_t *m);
+
+/* Intersects state i with {x : xi[i].x = alpha[i]}; status 0 EMPTY, 1 SAME, 2 SUCCESS.
+ * Replaces shrink, libcirc/stabilizer/stabilizer.c:500-585. */
+int csim_shrink(csim_ctx *ctx, int64_t count, csim_state *s, const uint64_t *xi, const int32_t *alpha,
+                int32_t lazy, int32_t *status);
+
+/* Projects state i onto (1 + i^{m[i]} Z(zeta[i]) X(xi[i]))/2; norm[i] in {0, 1, 2^-1/2}.
+ * Replaces measurePauli, libcirc/stabilizer/stabilizer.c:827-959. */
+int csim_measure_pauli(csim_ctx *ctx, int64_t count, csim_state *s, const int32_t *m, const uint64_t *zeta,
+                       const uint64_t *xi, double *norm);
+
+/* Replaces extend, libcirc/stabilizer/stabilizer.c:759-825. */
+int csim_extend(csim_ctx *ctx, int64_t count, csim_state *s, const uint64_t *xi);
+
+/* count random n-qubit states from the counter-based generator: state i uses
+ * stream (seed, first + i).  Same law as randomStabilizerState,
+ * libcirc/stabilizer/stabilizer.c:689-756. */
+int csim_random_states(csim_ctx *ctx, int32_t n, int64_t count, uint64_t seed, uint64_t first,
+                       csim_state *out);
+
+/* count random n-qubit states built from recorded rand() values: state i
+ * consumes words[offsets[i] .. offsets[i+1]) in the order the reference's
+ * randomStabilizerState calls rand().  Fails with CSIM_ERR_DEVICE if a state
+ * needs more words than its segment holds. */
+int csim_random_states_replay(csim_ctx *ctx, int32_t n, int64_t count, const uint32_t *words,
+                              const int64_t *offsets, csim_state *out);
+
+/* Term idx[i] of the exact decomposition of |H^{(x)t}>.
+ * Replaces prepH, libcirc/stateprep.c:36-81. */
+int csim_prep_h(csim_ctx *ctx, int32_t t, int64_t count, const int64_t *idx, csim_state *out);
+
+/* Term idx[i] of |L> for the k x t code L (L[r] = row r).
+ * Replaces prepL, libcirc/stateprep.c:85-120. */
+int csim_prep_l(csim_ctx *ctx, int32_t t, const uint64_t *L, int32_t k, int64_t count, const int64_t *idx,
+                csim_state *out);
+
+/* ------------------------------------------------------------- hot path */
+
+/* All pairs <theta[a] | phi_j> for a < ntheta, j0 <= j < j0 + nj, where phi_j is
+ * term j of |L> (exact == 0) or of the exact |H^t> decomposition (exact != 0).
+ * Outputs are indexed [a * nj + (j - j0)].  This is the inner loop of
+ * singleProjectorSample, libcirc/innerprod.c:122-138. */
+int csim_term_products(csim_ctx *ctx, int32_t t, int32_t exact, const uint64_t *L, int32_t k,
+                       int64_t ntheta, const csim_state *theta, int64_t j0, int64_t nj, int32_t *eps,
+                       int32_t *p, int32_t *m);
+
+/* 2^t |projfactor * sum_j <theta|phi_j>|^2 for `count` random states drawn with
+ * generator `rng` (seed `seed`), one value per state in draw order.
+ * Replaces singleProjectorSample, libcirc/innerprod.c:88-144. */
+int csim_single_projector_samples(csim_ctx *ctx, const csim_projector *P, const uint64_t *L, int32_t k,
+                                  int32_t exact, int64_t count, int32_t rng, uint64_t seed, double *values);
+
+/* Median of `bins` means of `samples` samples.  Replaces multiSampledProjector
+ * and sampledProjector, libcirc/innerprod.c:23-84; with rng == CSIM_RNG_LIBC
+ * the states drawn are the reference's for srand(seed). */
+int csim_multi_sampled_projector(csim_ctx *ctx, const csim_projector *P, const uint64_t *L, int32_t k,
+                                 int32_t exact, double norm, int32_t samples, int32_t bins, int32_t rng,
+                                 uint64_t seed, double *out);
+
+/* |sum_{i<=j} (2 - delta_ij) <Pi phi_i | phi_j>| over all chi(chi+1)/2 pairs.
+ * Replaces exactProjector, libcirc/innerprod.c:148-261. */
+int csim_exact_projector(csim_ctx *ctx, const csim_projector *P, const uint64_t *L, int32_t k,
+                         int32_t exact, double norm, double *out);
+
+/* ------------------------------------------------------------- host side */
+
+/* Chooses the decomposition: exact |H^t> terms, or a random k x t code L
+ * (rows returned in L_out, capacity 64).  *exact and *k are in/out exactly as
+ * in decompose, libcirc/probability.c:307-415.  Random bits come from the
+ * libc-compatible generator state `*rng_state` (see csim_libc_rand_*), which
+ * the reference leaves at its unseeded default (seed 1). */
+int csim_decompose(int32_t t, double fidbound, int32_t rank, int32_t fidelity, int32_t force_l,
+                   int32_t verbose, int32_t quiet, int32_t *exact, int32_t *k, double *norm, uint64_t *L_out,
+                   void *rng_state, FILE *log);
+
+/* The C library's srand()/rand() sequence, reproduced as a value type so that
+ * each context owns one.  Use csim_libc_rand_size() bytes of storage. */
+int64_t csim_libc_rand_size(void);
+void csim_libc_rand_seed(void *state, uint32_t seed);
+int32_t csim_libc_rand_next(void *state);
+
+/* The whole backend: reads the stdin protocol of libcirc/probability.py:249-272
+ * from `in` and writes the reference's output lines (libcirc/probability.c:44-221)
+ * to `out`, the last two being numerator and denominator in %.17e.
+ * Returns 0 on success. */
+int csim_backend_run(FILE *in, FILE *out, int device);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CSIM_H */
