@@ -1,0 +1,384 @@
+"""Benchmark: stabilizer inner products/s on the c2 workload (t = 40, chi = 2^16, L = 4096).
+
+One step = the backend work of one probability query: numerator and
+denominator estimates (multiSampledProjector of libcirc/innerprod.c:23 on G'
+and H') over L = 4096 random stabilizer states each, every state paired with
+all 2^16 terms of the k = 16 code.  The inputs (projectors G', H' of a seeded
+random Clifford+T circuit, n = 24, t = 40, 8 measured qubits) are the committed
+protocol file tests/golden/workload_c2.txt.
+
+  value  pairs per second of device time (CUDA events on the library's stream,
+         states drawn on the GPU, inputs resident)
+  e2e    pairs per second of wall time through the C ABI with host buffers and
+         the reference's own rand() draws (host word generation, uploads and
+         result reads inside the timed region)
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun each rank draws its own states (weak scaling); rank 0 prints.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = os.path.join(ROOT, "tests", "golden", "workload_c2.txt")
+METRIC = "stabilizer inner products/s (t=40)"
+UNIT = "inner products/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+# ------------------------------------------------------------------ workload
+def parse_protocol(text):
+    """13 scalars + two projectors (libcirc/probability.py:249-272, comms.c:9-36)."""
+    tok = text.split()
+    names = ["quiet", "verbose", "noapprox", "samples", "bins", "t", "k", "exact", "fidbound", "fidelity", "rank",
+             "forceL", "forceSample"]
+    cfg = {}
+    for i, nme in enumerate(names):
+        cfg[nme] = float(tok[i]) if nme == "fidbound" else int(tok[i])
+    pos = len(names)
+    projs = []
+    for _ in range(2):
+        ns, nq = int(tok[pos]), int(tok[pos + 1])
+        pos += 2
+        ph, xs, zs = [], [], []
+        for _ in range(ns):
+            ph.append(int(tok[pos]))
+            pos += 1
+            x = z = 0
+            for j in range(nq):
+                if int(tok[pos]) & 1:
+                    x |= 1 << j
+                if int(tok[pos + 1]) & 1:
+                    z |= 1 << j
+                pos += 2
+            xs.append(x)
+            zs.append(z)
+        projs.append((ph, xs, zs, nq))
+    return cfg, projs
+
+
+def load_workload():
+    cfg, projs = parse_protocol(open(WORKLOAD).read())
+    from circuitsimulator_gb300 import backend
+
+    exact, k, norm, L = backend.decompose(cfg["t"], cfg["fidbound"], cfg["rank"], cfg["fidelity"], cfg["forceL"],
+                                          cfg["exact"], cfg["k"])
+    return cfg, projs, exact, k, norm, L
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for nme, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nme)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+# ------------------------------------------------------------------ roofline
+# Mean packed 64-bit row operations per (theta, term) pair of the
+# elementary-update algorithm on this workload (the roofline's work unit),
+# measured by `python oracle/rowops.py 24 400` over 9600 pairs (each checked
+# against the dense restatement): 2576 row-ops/pair, 33% orthogonal pairs.
+ROWOPS_PER_PAIR_T40 = 2576.0
+
+
+def alu_peak_gops(num_sms, mhz):
+    """Integer lane-op issue peak: SMs x 4 schedulers x 32 lanes x clock."""
+    return num_sms * 4 * 32 * mhz * 1e6 / 1e9
+
+
+# ------------------------------------------------------------------ CPU baseline (oracle leg)
+def cpu_baseline(cfg, projs, k, L, budget_s=15.0):
+    """The oracle restatement of the reference algorithm (oracle/csim_oracle.c)
+    on all host cores, on a bounded sample of the same workload: a few states
+    drawn and projected onto G' exactly as the reference does, paired with a
+    block of consecutive terms of the same code."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_ffi import ORACLE_SO, Oracle, make_projector
+
+    if not os.path.exists(ORACLE_SO):
+        subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
+    O = Oracle()
+    t = cfg["t"]
+    ph, xs, zs, nq = projs[0]
+    P = make_projector(ph, xs, zs, nq)
+    r = O.rng(12345)
+    thetas = []
+    while len(thetas) < 4:
+        s = O.random_state(t, r)
+        if O.project(s, P) != 0:
+            thetas.append(s[0])
+    th = np.array(thetas)
+    Lw = np.asarray(L, dtype=np.uint64)
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    O.term_products(t, 0, Lw, k, th, 0, 64, threads=cores)
+    cal = (time.perf_counter() - t0) / (4 * 64)
+    nj = int(max(64, min(2 ** k, budget_s / max(cal, 1e-9) / 4)))
+    t0 = time.perf_counter()
+    O.term_products(t, 0, Lw, k, th, 0, nj, threads=cores)
+    dt = time.perf_counter() - t0
+    return {"value": 4 * nj / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "4 projected thetas x %d terms of the c2 code (t=40), oracle/csim_oracle.c on %d threads, %.1f s"
+                      % (nj, cores, dt)}
+
+
+# ------------------------------------------------------------------ arms
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    from circuitsimulator_gb300 import backend
+
+    torch.cuda.set_device(local_rank)
+    cfg, projs, exact, k, norm, L = load_workload()
+    gpu = backend.Backend(local_rank)
+    P = [backend.projector(ph, xs, zs, nq) for (ph, xs, zs, nq) in projs]
+    samples, bins = cfg["samples"], cfg["bins"]
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    seed0 = 1000003 * (rank + 1)
+
+    def step(i, rng):
+        st = []
+        for q in range(2):
+            seed = (seed0 + 2 * i + q) & 0xFFFFFFFF
+            gpu.multiSampledProjector(P[q], L, exact, norm, samples, bins, rng, seed)
+            st.append(gpu.last_stats().as_dict())
+        return st
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- device-resident arm (value)
+    for i in range(args.warmup):
+        step(i, backend.RNG_PHILOX)
+        flush.zero_()
+    barrier()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    launches0 = gpu.launches
+    dev_ms, pair_ms, pairs, states, live = 0.0, 0.0, 0, 0, 0
+    for i in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        for s in step(args.warmup + i, backend.RNG_PHILOX):
+            dev_ms += s["device_ms"]
+            pair_ms += s["pair_kernel_ms"]
+            pairs += s["pairs"]
+            states += s["states"]
+            live += s["states_live"]
+    barrier()
+    launches = gpu.launches - launches0
+    clk = clocks.stop()
+
+    # ---- end-to-end arm (e2e): C ABI with host buffers, the reference's rand() draws
+    for i in range(min(args.warmup, 1)):
+        step(10_000 + i, backend.RNG_LIBC)
+    barrier()
+    e2e_pairs, h2d, d2h = 0, 0, 0
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        for s in step(20_000 + i, backend.RNG_LIBC):
+            e2e_pairs += s["pairs"]
+            h2d += s["h2d_bytes"]
+            d2h += s["d2h_bytes"]
+    barrier()
+    e2e_s = time.perf_counter() - t0
+
+    # max over ranks of the times, sum of the work
+    totals = np.array([dev_ms, e2e_s, pairs, e2e_pairs, pair_ms], dtype=np.float64)
+    if world > 1:
+        tt = torch.tensor(totals, device="cuda")
+        mx = tt.clone()
+        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+        sm = tt.clone()
+        torch.distributed.all_reduce(sm, op=torch.distributed.ReduceOp.SUM)
+        dev_ms, e2e_s, pair_ms = float(mx[0]), float(mx[1]), float(mx[4])
+        pairs, e2e_pairs = int(sm[2]), int(sm[3])
+    if rank != 0:
+        return None
+
+    value = pairs / (dev_ms / 1e3)
+    props = torch.cuda.get_device_properties(local_rank)
+    mhz = clk.get("sm_mhz") or 2070.0
+    per_pair = ROWOPS_PER_PAIR_T40
+    kernel_rate = (pairs / world) / (pair_ms / 1e3)  # pairs/s of the pair kernel alone (rank 0 share)
+    achieved = kernel_rate * per_pair / 1e9 if per_pair else None
+    peak = alu_peak_gops(props.multi_processor_count, clk.get("sm_max_mhz") or 2070.0)
+    roofline = {"bound": "alu", "kernel": "k_terms<2,0> (theta x prepL term pairs)",
+                "achieved": achieved, "peak": peak, "unit": "G packed row-ops/s",
+                "frac": (achieved / peak) if achieved else None,
+                "traffic": None,
+                "work_unit": "packed row-op (one 64-bit row test/XOR/update of the elementary-update algorithm)",
+                "rowops_per_pair": per_pair,
+                "peak_source": "SMs x 4 x 32 lanes x sm_max_mhz (MEASURED_PEAKS.json holds no integer peak)",
+                "pair_kernel_share": pair_ms / dev_ms}
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64 GF(2) rows; Z8 / exact int128 Z[w] sums; f64 final |.|^2",
+        "data": "synthetic: seeded random Clifford+T circuit (n=24, t=40, 8 measured qubits) -> G', H' "
+                "(tests/golden/workload_c2.txt); random stabilizer states drawn per step",
+        "config": {"workload": "c2: t=40, chi=2^16 (k=16 code), L=%d states x 2 projectors per step" % samples,
+                   "t": cfg["t"], "k": k, "samples": samples, "bins": bins, "states_per_step": states // args.steps,
+                   "live_states_per_step": live // args.steps, "pairs_per_step": pairs // args.steps // world,
+                   "l2": "flushed between steps (256 MiB write); hot data (codewords 512 KiB) is L2-resident",
+                   "rng": "Philox on device (value); the C library's rand() sequence (e2e)"},
+        "e2e": {"value": e2e_pairs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
+                "d2h_bytes_per_step": d2h // args.steps, "ms_per_step": 1e3 * e2e_s / args.steps},
+        "roofline": roofline,
+        "clocks": clk,
+        "gpu_launches": launches,
+    }
+    if world == 1:
+        try:
+            out["cpu_baseline"] = cpu_baseline(cfg, projs, k, L)
+        except Exception as e:  # the baseline never decides the run
+            out["cpu_baseline"] = {"value": None, "unit": UNIT, "error": str(e)}
+    return out
+
+
+def run_reference(args, rank, world):
+    """The reference's algorithm on the host cores (the oracle port of
+    libcirc/stabilizer.c + stateprep.c + innerprod.c: the reference's own C
+    code is not available on the GPU machine), one bounded sample per step."""
+    if rank != 0:
+        return None
+    cfg, projs = parse_protocol(open(WORKLOAD).read())
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_ffi import ORACLE_SO, Oracle, make_projector
+
+    if not os.path.exists(ORACLE_SO):
+        subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
+    O = Oracle()
+    kind = "port"
+    t = cfg["t"]
+    r1 = O.rng(1)
+    exact, k, norm, L = O.decompose(t, cfg["fidbound"], cfg["rank"], cfg["fidelity"], cfg["forceL"], cfg["exact"],
+                                    cfg["k"], r1)
+    ph, xs, zs, nq = projs[0]
+    P = make_projector(ph, xs, zs, nq)
+    r = O.rng(777)
+    cores = os.cpu_count() or 1
+    per_step_s = 6.0
+    rates = []
+    nj = None
+    for i in range(args.warmup + args.steps):
+        thetas = []
+        while len(thetas) < 2:
+            s = O.random_state(t, r)
+            if O.project(s, P) != 0:
+                thetas.append(s[0])
+        th = np.array(thetas)
+        if nj is None:
+            t0 = time.perf_counter()
+            O.term_products(t, 0, L, k, th, 0, 32, threads=cores)
+            cal = (time.perf_counter() - t0) / 64
+            nj = int(max(32, min(2 ** k, per_step_s / max(cal, 1e-9) / 2)))
+        j0 = (i * nj) % (2 ** k - nj + 1)
+        t0 = time.perf_counter()
+        O.term_products(t, 0, L, k, th, j0, nj, threads=cores)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            rates.append((2 * nj, dt))
+    pairs = sum(a for a, _ in rates)
+    secs = sum(b for _, b in rates)
+    value = pairs / secs
+    sample = "per step: 2 projected states x %d terms of the c2 code (t=40) on %d threads" % (nj, cores)
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (host C)",
+            "data": "synthetic: tests/golden/workload_c2.txt",
+            "config": {"workload": "c2: t=40, chi=2^16 (k=16 code) -- bounded sample per step", "t": t, "k": k},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+    else:
+        if world > 1:
+            import torch
+
+            torch.cuda.set_device(local_rank)
+            torch.distributed.init_process_group("nccl")
+        out = run_ours(args, rank, world, local_rank)
+        if world > 1:
+            import torch
+
+            torch.distributed.barrier()
+            torch.distributed.destroy_process_group()
+    if out is not None:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,299 @@
+"""Python view of libcsimgpu.so (include/csim.h) with the reference's names.
+
+Each method calls one C-ABI entry point; all stabilizer work runs in the
+sm_103a kernels.  There is no CPU fallback: if the library is missing or no
+GB300 is visible, construction fails with an exception.
+
+    innerProductExact      libcirc/stabilizer/stabilizer.c:589
+    exponentialSumExact    libcirc/stabilizer/stabilizer.c:300
+    shrink                 libcirc/stabilizer/stabilizer.c:500
+    measurePauli / extend  libcirc/stabilizer/stabilizer.c:827 / :759
+    randomStabilizerState  libcirc/stabilizer/stabilizer.c:689
+    prepH / prepL          libcirc/stateprep.c:36 / :85
+    singleProjectorSample  libcirc/innerprod.c:88
+    multiSampledProjector  libcirc/innerprod.c:23
+    exactProjector         libcirc/innerprod.c:148
+    decompose              libcirc/probability.c:307
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from .state import STATE_DTYPE
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libcsimgpu.so")
+EXE_PATH = os.path.join(PKG, "gpubackend")
+
+RNG_PHILOX = 0
+RNG_LIBC = 1
+SEED_CONTINUE = (1 << 64) - 1
+
+_ERRORS = {-1: "bad argument", -2: "CUDA error", -3: "device check failed", -4: "out of memory",
+           -5: "no sm_103 device", -6: "protocol error"}
+
+
+class CsimError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("csim error %d (%s): %s" % (code, _ERRORS.get(code, "?"), msg))
+        self.code = code
+
+
+class Stats(C.Structure):
+    """csim_stats of include/csim.h."""
+    _fields_ = [("device_ms", C.c_double), ("pair_kernel_ms", C.c_double), ("states", C.c_int64),
+                ("states_live", C.c_int64), ("pairs", C.c_int64), ("h2d_bytes", C.c_int64),
+                ("d2h_bytes", C.c_int64), ("kernels", C.c_int64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class _Projector(C.Structure):
+    _fields_ = [("nstabs", C.c_int32), ("nqubits", C.c_int32), ("phase", C.c_void_p), ("xs", C.c_void_p),
+                ("zs", C.c_void_p)]
+
+
+_lib = None
+
+
+def load_library(path=LIB_PATH):
+    """Loads libcsimgpu.so once; raises if it is missing (run circuitsimulator_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError("%s not built: run python -m circuitsimulator_gb300.build" % path)
+    lib = C.CDLL(path)
+    vp, i32, i64, u64 = C.c_void_p, C.c_int32, C.c_int64, C.c_uint64
+    sig = {
+        "csim_ctx_create": ([C.c_int, C.POINTER(C.c_void_p)], C.c_int),
+        "csim_ctx_destroy": ([vp], None),
+        "csim_last_error": ([vp], C.c_char_p),
+        "csim_launch_count": ([vp], i64),
+        "csim_last_stats": ([vp, vp], C.c_int),
+        "csim_inner_product_exact": ([vp, i64, vp, vp, vp, vp, vp], C.c_int),
+        "csim_exponential_sum_exact": ([vp, i64, vp, vp, vp, vp], C.c_int),
+        "csim_shrink": ([vp, i64, vp, vp, vp, i32, vp], C.c_int),
+        "csim_measure_pauli": ([vp, i64, vp, vp, vp, vp, vp], C.c_int),
+        "csim_extend": ([vp, i64, vp, vp], C.c_int),
+        "csim_random_states": ([vp, i32, i64, u64, u64, vp], C.c_int),
+        "csim_random_states_replay": ([vp, i32, i64, vp, vp, vp], C.c_int),
+        "csim_prep_h": ([vp, i32, i64, vp, vp], C.c_int),
+        "csim_prep_l": ([vp, i32, vp, i32, i64, vp, vp], C.c_int),
+        "csim_term_products": ([vp, i32, i32, vp, i32, i64, vp, i64, i64, vp, vp, vp], C.c_int),
+        "csim_single_projector_samples": ([vp, vp, vp, i32, i32, i64, i32, u64, vp], C.c_int),
+        "csim_multi_sampled_projector": ([vp, vp, vp, i32, i32, C.c_double, i32, i32, i32, u64, vp], C.c_int),
+        "csim_exact_projector": ([vp, vp, vp, i32, i32, C.c_double, vp], C.c_int),
+        "csim_decompose": ([i32, C.c_double, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp], C.c_int),
+        "csim_libc_rand_size": ([], i64),
+        "csim_libc_rand_seed": ([vp, C.c_uint32], None),
+        "csim_libc_rand_next": ([vp], i32),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = lib
+    return lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _states(a):
+    a = np.ascontiguousarray(a)
+    if a.dtype != STATE_DTYPE:
+        raise TypeError("expected csim_state records")
+    return a.reshape(-1)
+
+
+def projector(phases, xs, zs, nqubits):
+    """Protocol-encoded projector -> ctypes struct (keeps its arrays alive)."""
+    ph = np.ascontiguousarray(np.asarray(phases, dtype=np.int32).reshape(-1))
+    xa = np.ascontiguousarray(np.asarray([int(x) for x in xs], dtype=np.uint64).reshape(-1))
+    za = np.ascontiguousarray(np.asarray([int(z) for z in zs], dtype=np.uint64).reshape(-1))
+    P = _Projector(len(ph), int(nqubits), _p(ph) if len(ph) else None, _p(xa) if len(ph) else None,
+                   _p(za) if len(ph) else None)
+    P._keep = (ph, xa, za)
+    return P
+
+
+class LibcRand:
+    """The C library's srand()/rand() sequence as a value (csim_libc_rand_*)."""
+
+    def __init__(self, seed=1):
+        lib = load_library()
+        self._buf = C.create_string_buffer(int(lib.csim_libc_rand_size()))
+        lib.csim_libc_rand_seed(self._buf, int(seed) & 0xFFFFFFFF)
+
+    def rand(self):
+        return load_library().csim_libc_rand_next(self._buf)
+
+
+def decompose(t, fidbound=1e-5, rank=False, fidelity=False, forceL=False, exact=False, k=0, rng=None):
+    """decompose() of libcirc/probability.c:307 -> (exact, k, norm, L or None)."""
+    lib = load_library()
+    rng = rng or LibcRand(1)
+    e, kk, norm = C.c_int32(int(bool(exact))), C.c_int32(int(k or 0)), C.c_double(0)
+    L = np.zeros(64, dtype=np.uint64)
+    rc = lib.csim_decompose(int(t), float(fidbound), int(bool(rank)), int(bool(fidelity)), int(bool(forceL)), 0, 1,
+                            C.byref(e), C.byref(kk), C.byref(norm), _p(L), rng._buf, None)
+    if rc:
+        raise CsimError(rc, "decompose")
+    return bool(e.value), kk.value, norm.value, (None if e.value else L[: kk.value].copy())
+
+
+class Backend:
+    """One csim_ctx: a CUDA stream, device buffers and random streams on one GB300."""
+
+    def __init__(self, device=0):
+        self.lib = load_library()
+        h = C.c_void_p()
+        rc = self.lib.csim_ctx_create(int(device), C.byref(h))
+        if rc:
+            raise CsimError(rc, "cannot open device %d" % device)
+        self.ctx = h
+
+    def close(self):
+        if self.ctx:
+            self.lib.csim_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc:
+            raise CsimError(rc, self.lib.csim_last_error(self.ctx).decode())
+
+    @property
+    def launches(self):
+        return int(self.lib.csim_launch_count(self.ctx))
+
+    def last_stats(self):
+        st = Stats()
+        self._check(self.lib.csim_last_stats(self.ctx, C.byref(st)))
+        return st
+
+    # ---------------------------------------------------------------- primitives
+    def innerProductExact(self, a, b):
+        a, b = _states(a), _states(b)
+        n = len(a)
+        eps, p, m = (np.zeros(n, dtype=np.int32) for _ in range(3))
+        self._check(self.lib.csim_inner_product_exact(self.ctx, n, _p(a), _p(b), _p(eps), _p(p), _p(m)))
+        return eps, p, m
+
+    def exponentialSumExact(self, s):
+        """Returns (eps, p, m) and updates the states in place."""
+        s = _states(s)
+        n = len(s)
+        eps, p, m = (np.zeros(n, dtype=np.int32) for _ in range(3))
+        self._check(self.lib.csim_exponential_sum_exact(self.ctx, n, _p(s), _p(eps), _p(p), _p(m)))
+        return eps, p, m
+
+    def shrink(self, s, xi, alpha, lazy=False):
+        s = _states(s)
+        n = len(s)
+        xi = np.ascontiguousarray(np.broadcast_to(np.asarray(xi, dtype=np.uint64), (n,)))
+        al = np.ascontiguousarray(np.broadcast_to(np.asarray(alpha, dtype=np.int32), (n,)))
+        st = np.zeros(n, dtype=np.int32)
+        self._check(self.lib.csim_shrink(self.ctx, n, _p(s), _p(xi), _p(al), int(bool(lazy)), _p(st)))
+        return st
+
+    def measurePauli(self, s, m, zeta, xi):
+        s = _states(s)
+        n = len(s)
+        m = np.ascontiguousarray(np.broadcast_to(np.asarray(m, dtype=np.int32), (n,)))
+        z = np.ascontiguousarray(np.broadcast_to(np.asarray(zeta, dtype=np.uint64), (n,)))
+        x = np.ascontiguousarray(np.broadcast_to(np.asarray(xi, dtype=np.uint64), (n,)))
+        norm = np.zeros(n, dtype=np.float64)
+        self._check(self.lib.csim_measure_pauli(self.ctx, n, _p(s), _p(m), _p(z), _p(x), _p(norm)))
+        return norm
+
+    def extend(self, s, xi):
+        s = _states(s)
+        n = len(s)
+        x = np.ascontiguousarray(np.broadcast_to(np.asarray(xi, dtype=np.uint64), (n,)))
+        self._check(self.lib.csim_extend(self.ctx, n, _p(s), _p(x)))
+
+    def randomStabilizerState(self, n, count=1, seed=0, first=0):
+        out = np.zeros(int(count), dtype=STATE_DTYPE)
+        self._check(self.lib.csim_random_states(self.ctx, int(n), int(count), int(seed), int(first), _p(out)))
+        return out
+
+    def randomStabilizerStateReplay(self, n, words, offsets):
+        words = np.ascontiguousarray(words, dtype=np.uint32)
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        out = np.zeros(len(offsets) - 1, dtype=STATE_DTYPE)
+        self._check(self.lib.csim_random_states_replay(self.ctx, int(n), len(out), _p(words), _p(offsets), _p(out)))
+        return out
+
+    def prepH(self, idx, t):
+        idx = np.ascontiguousarray(np.atleast_1d(np.asarray(idx, dtype=np.int64)))
+        out = np.zeros(len(idx), dtype=STATE_DTYPE)
+        self._check(self.lib.csim_prep_h(self.ctx, int(t), len(idx), _p(idx), _p(out)))
+        return out
+
+    def prepL(self, idx, t, L):
+        idx = np.ascontiguousarray(np.atleast_1d(np.asarray(idx, dtype=np.int64)))
+        L = np.ascontiguousarray(np.asarray([int(x) for x in L], dtype=np.uint64))
+        out = np.zeros(len(idx), dtype=STATE_DTYPE)
+        self._check(self.lib.csim_prep_l(self.ctx, int(t), _p(L), len(L), len(idx), _p(idx), _p(out)))
+        return out
+
+    # ---------------------------------------------------------------- hot path
+    def term_products(self, t, exact, L, theta, j0, nj):
+        """(eps, p, m) of <theta_a|phi_j>, shape (len(theta), nj)."""
+        theta = _states(theta)
+        Lp = np.ascontiguousarray(np.asarray([int(x) for x in (L if L is not None else [])] or [0], dtype=np.uint64))
+        k = 0 if L is None else len(L)
+        na = len(theta)
+        eps, p, m = (np.zeros(na * nj, dtype=np.int32) for _ in range(3))
+        self._check(self.lib.csim_term_products(self.ctx, int(t), int(bool(exact)), _p(Lp), int(k), na, _p(theta),
+                                                int(j0), int(nj), _p(eps), _p(p), _p(m)))
+        return eps.reshape(na, nj), p.reshape(na, nj), m.reshape(na, nj)
+
+    def singleProjectorSample(self, P, L, exact, count, rng=RNG_LIBC, seed=SEED_CONTINUE):
+        Lp = np.ascontiguousarray(np.asarray([int(x) for x in (L if L is not None else [])] or [0], dtype=np.uint64))
+        k = 0 if L is None else len(L)
+        vals = np.zeros(int(count), dtype=np.float64)
+        self._check(self.lib.csim_single_projector_samples(self.ctx, C.byref(P), _p(Lp), int(k), int(bool(exact)),
+                                                           int(count), int(rng), int(seed), _p(vals)))
+        return vals
+
+    def multiSampledProjector(self, P, L, exact, norm, samples, bins=1, rng=RNG_LIBC, seed=SEED_CONTINUE):
+        Lp = np.ascontiguousarray(np.asarray([int(x) for x in (L if L is not None else [])] or [0], dtype=np.uint64))
+        k = 0 if L is None else len(L)
+        out = C.c_double(0)
+        self._check(self.lib.csim_multi_sampled_projector(self.ctx, C.byref(P), _p(Lp), int(k), int(bool(exact)),
+                                                          float(norm), int(samples), int(bins), int(rng), int(seed),
+                                                          C.byref(out)))
+        return out.value
+
+    def exactProjector(self, P, L, exact, norm):
+        Lp = np.ascontiguousarray(np.asarray([int(x) for x in (L if L is not None else [])] or [0], dtype=np.uint64))
+        k = 0 if L is None else len(L)
+        out = C.c_double(0)
+        self._check(self.lib.csim_exact_projector(self.ctx, C.byref(P), _p(Lp), int(k), int(bool(exact)),
+                                                  float(norm), C.byref(out)))
+        return out.value
+
+
+def run_backend(protocol_text, seed=None, rng=None, timeout=None, exe=EXE_PATH):
+    """Runs the gpubackend executable on one stdin-protocol input; returns its
+    stdout lines (the last two are numerator and denominator)."""
+    env = dict(os.environ)
+    if seed is not None:
+        env["CSIM_SEED"] = str(int(seed))
+    if rng is not None:
+        env["CSIM_RNG"] = rng
+    r = subprocess.run([exe, "stdin"], input=protocol_text.encode(), stdout=subprocess.PIPE, stderr=subprocess.PIPE,
+                       env=env, timeout=timeout)
+    return r.returncode, r.stdout.decode().splitlines()

@@ -1,0 +1,42 @@
+// csim_internal.h — launch interface between the C ABI host code
+// (csim_host.cpp) and the kernels (csim_kernels.cu).  Not installed.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace csim {
+
+struct GState;  // device image of csim_state (csim_warp.cuh)
+
+struct Launch {
+    cudaStream_t stream;
+    int* d_err;         // device error word, OR of csim::kErr* flags
+    int64_t* launches;  // host counter of kernel launches
+    int num_sms;
+};
+
+int launch_inner_product(const Launch& L, int nr, const GState* a, const GState* b, int64_t count, int* eps, int* p,
+                         int* m);
+int launch_exp_sum(const Launch& L, int nr, GState* s, int64_t count, int* eps, int* p, int* m);
+int launch_shrink(const Launch& L, int nr, GState* s, const uint64_t* xi, const int* alpha, int lazy, int64_t count,
+                  int* status);
+int launch_measure(const Launch& L, int nr, GState* s, const int* m, const uint64_t* zeta, const uint64_t* xi,
+                   int64_t count, int* code);
+int launch_extend(const Launch& L, int nr, GState* s, const uint64_t* xi, int64_t count);
+int launch_random_states(const Launch& L, int n, int64_t count, int mode, uint64_t seed, uint64_t first,
+                         const uint32_t* words, const int64_t* offsets, const double* cum, GState* out,
+                         int64_t* consumed);
+int launch_project(const Launch& L, int nr, GState* s, int64_t count, int nstabs, const int* m, const uint64_t* zeta,
+                   const uint64_t* xi, int* code);
+int launch_codewords(const Launch& L, const uint64_t* Ld, int k, int64_t j0, int64_t count, uint64_t* out);
+int launch_prep(const Launch& L, int t, int exact, const uint64_t* codewords, const int64_t* idx, int64_t count,
+                GState* out);
+// part / part_diag: 4 int128 per work item (ntheta * ceil(nj/chunk) items), zeroed by the caller
+int launch_terms(const Launch& L, int nr, int mode, const uint64_t* codewords, const GState* phis,
+                 const GState* theta, const int* code, int64_t ntheta, int64_t j0, int64_t nj, int chunk, int P,
+                 __int128* part, __int128* part_diag, int* eps_o, int* p_o, int* m_o);
+int launch_reduce_parts(const Launch& L, const __int128* part, int64_t ntheta, int64_t nchunks, __int128* acc);
+
+}  // namespace csim

@@ -78,6 +78,10 @@ typedef struct csim_projector {
 #define CSIM_RNG_PHILOX 0 /* counter-based, one independent stream per state (GPU)   */
 #define CSIM_RNG_LIBC 1   /* the sequence of srand(seed); rand() of the C library:
                              reproduces the reference's draws sample for sample       */
+/* Pass as `seed` to continue the context's current stream instead of reseeding
+ * (the reference draws the numerator's and the denominator's samples from one
+ * stream, libcirc/probability.c:182-198). */
+#define CSIM_SEED_CONTINUE UINT64_MAX
 
 typedef struct csim_ctx csim_ctx;
 
@@ -91,6 +95,21 @@ void csim_ctx_destroy(csim_ctx *ctx);
 const char *csim_last_error(const csim_ctx *ctx);
 /* Number of kernels this context has launched so far. */
 int64_t csim_launch_count(const csim_ctx *ctx);
+
+/* Measurements of the last estimator call (csim_single_projector_samples,
+ * csim_multi_sampled_projector, csim_exact_projector) on this context.  Device
+ * times come from CUDA events recorded on the context's stream. */
+typedef struct csim_stats {
+    double device_ms;        /* first kernel start .. last kernel end, summed over batches */
+    double pair_kernel_ms;   /* the (theta, term) pair kernel alone                        */
+    int64_t states;          /* random states drawn                                        */
+    int64_t states_live;     /* states not annihilated by the projector                    */
+    int64_t pairs;           /* inner products computed (live states x terms)              */
+    int64_t h2d_bytes;       /* host -> device bytes copied by the call                    */
+    int64_t d2h_bytes;       /* device -> host bytes copied by the call                    */
+    int64_t kernels;         /* kernels launched by the call                               */
+} csim_stats;
+int csim_last_stats(const csim_ctx *ctx, csim_stats *out);
 
 /* ----------------------------------------------- stabilizer primitives (batched) */
 

@@ -872,3 +872,245 @@ void orc_term_products(int t, int exact, const uint64_t *L, int k, int64_t nthet
     for (int i = 0; i < threads; i++) pthread_create(&th[i], NULL, grid_worker, &g);
     for (int i = 0; i < threads; i++) pthread_join(th[i], NULL);
 }
+
+/* ======================================================================
+ * Elementary-update restatement of one (theta, prepL term) pair, with a
+ * count of packed row operations (the roofline's work unit).
+ *
+ * Same results as orc_inner_product_exact(theta, prepL term) — the tests
+ * check this — but each basis change R = I + u e_c^T is applied as rank-one
+ * row/column updates instead of updateDJ's dense R J R^T.  One "row-op" is one
+ * 64-bit operation on one matrix row or one bit-sliced vector: a bit test or
+ * parity of a row, a row XOR, a column-bit update of a row, a row swap, or a
+ * bit-sliced D/h/Q update.
+ * ==================================================================== */
+typedef struct {
+    int n, k, Q;
+    uint64_t h, D1, D2;
+    uint64_t G[CSIM_MAX_QUBITS], J[CSIM_MAX_QUBITS];
+} el_state;
+
+static inline int el_getD(const el_state *s, int i) { return 2 * (2 * BIT(s->D2, i) + BIT(s->D1, i)); }
+
+static void el_addD(el_state *s, uint64_t u, int d1, int d2) {
+    const uint64_t a1 = d1 ? u : 0, a2 = d2 ? u : 0, c = s->D1 & a1;
+    s->D1 ^= a1;
+    s->D2 ^= a2 ^ c;
+}
+
+/* updateDJ for R = I + u1 e_c1^T + u2 e_c2^T (c2 < 0: absent) */
+static void el_applyR(el_state *s, int c1, uint64_t u1, int c2, uint64_t u2, int64_t *ops) {
+    const int k = s->k;
+    const uint64_t km = k >= 64 ? ~0ULL : (ONE(k) - 1);
+    uint64_t row1 = s->J[c1], col1 = 0, row2 = c2 >= 0 ? s->J[c2] : 0, col2 = 0;
+    for (int x = 0; x < s->n; x++) {
+        col1 |= (uint64_t)BIT(s->J[x], c1) << x;
+        if (c2 >= 0) col2 |= (uint64_t)BIT(s->J[x], c2) << x;
+    }
+    const int d11 = BIT(s->D1, c1), d21 = BIT(s->D2, c1);
+    const int d12 = c2 >= 0 ? BIT(s->D1, c2) : 0, d22 = c2 >= 0 ? BIT(s->D2, c2) : 0;
+    el_addD(s, u1, d11, d21);
+    if (c2 >= 0) el_addD(s, u2, d12, d22);
+    s->D1 &= km;
+    s->D2 &= km;
+    uint64_t flip = u1 & ((col1 & ~((c1 + 1 >= 64) ? ~0ULL : (ONE(c1 + 1) - 1))) | (row1 & (ONE(c1) - 1)));
+    if (c2 >= 0) {
+        flip ^= u2 & ((col2 & ~((c2 + 1 >= 64) ? ~0ULL : (ONE(c2 + 1) - 1))) | (row2 & (ONE(c2) - 1)));
+        const int jc = c1 > c2 ? BIT(row1, c2) : BIT(row2, c1);
+        if (jc) flip ^= u1 & u2;
+    }
+    s->D2 ^= flip;
+    for (int x = 0; x < s->n; x++) {
+        uint64_t r = s->J[x];
+        if (BIT(u1, x)) r ^= row1;
+        if (c2 >= 0 && BIT(u2, x)) r ^= row2;
+        uint64_t r2 = r;
+        if (BIT(r, c1)) r2 ^= u1;
+        if (c2 >= 0 && BIT(r, c2)) r2 ^= u2;
+        s->J[x] = r2;
+    }
+    *ops += 2 /* pivot rows */ + popc(u1) + popc(u2) /* row XORs */ + k /* column updates */ + 3 /* D */;
+}
+
+static void el_swap(el_state *s, int i, int j, int64_t *ops) {
+    const int k = s->k;
+    const uint64_t km = k >= 64 ? ~0ULL : (ONE(k) - 1);
+    if (i != j) {
+        uint64_t t = ((s->D1 >> i) ^ (s->D1 >> j)) & 1;
+        s->D1 ^= (t << i) | (t << j);
+        t = ((s->D2 >> i) ^ (s->D2 >> j)) & 1;
+        s->D2 ^= (t << i) | (t << j);
+        uint64_t r = s->J[i];
+        s->J[i] = s->J[j];
+        s->J[j] = r;
+        for (int x = 0; x < s->n; x++) {
+            t = ((s->J[x] >> i) ^ (s->J[x] >> j)) & 1;
+            s->J[x] ^= (t << i) | (t << j);
+        }
+        *ops += 2 + k + 2;
+    }
+    s->D1 &= km;
+    s->D2 &= km;
+}
+
+static int el_shrink_unit(el_state *s, int q, int64_t *ops) {
+    const int k = s->k;
+    uint64_t S = 0;
+    for (int a = 0; a < k; a++)
+        if (BIT(s->G[a], q)) S |= ONE(a);
+    *ops += k;
+    const int beta = BIT(s->h, q);
+    if (!S) return 1 - beta;
+    const int i = 63 - __builtin_clzll(S);
+    const uint64_t U = S & ~ONE(i);
+    for (int a = 0; a < k; a++)
+        if (BIT(U, a)) s->G[a] ^= s->G[i];
+    *ops += popc(U);
+    if (U) el_applyR(s, i, U, -1, 0, ops);
+    const int kk = k - 1;
+    uint64_t t = s->G[i];
+    s->G[i] = s->G[kk];
+    s->G[kk] = t;
+    *ops += 2;
+    el_swap(s, i, kk, ops);
+    if (beta) {
+        s->h ^= s->G[kk];
+        s->Q = (s->Q + el_getD(s, kk)) % 8;
+        for (int x = 0; x < s->n; x++)
+            if (BIT(s->J[x], kk)) s->D2 ^= ONE(x);
+        *ops += 2 + k;
+    } else {
+        s->Q = s->Q % 8;
+    }
+    s->k = kk;
+    return 2;
+}
+
+static void el_partial_gamma(int A, int *e, int *p, int *m) {
+    while (A < 0) A += 8;
+    *e = (A % 8 == 4) ? 0 : 1;
+    switch (A % 8) {
+    case 0: *p = 2; *m = 0; break;
+    case 2: *p = 1; *m = 1; break;
+    case 4: *p = 0; *m = 0; break;
+    case 6: *p = 1; *m = 7; break;
+    default: orc_assert_failures++; break;
+    }
+}
+
+static void el_wsigma(const el_state *s, int sigma, int sidx, uint64_t Mm, uint64_t DA, const int *partner, int *e,
+                      int *p, int *m, int64_t *ops) {
+    if (s->k == 0) {
+        *e = 1; *p = 0; *m = s->Q;
+        return;
+    }
+    const int tM0 = s->Q + sigma * el_getD(s, sidx >= 0 ? sidx : 0);
+    int P = 0, Ms = 0;
+    for (int x = 0; x < s->n; x++) {
+        int ee = 1, pp = 0, mm = 0;
+        if (BIT(Mm, x)) {
+            el_partial_gamma(el_getD(s, x) + sigma * 4 * (sidx >= 0 ? BIT(s->J[x], sidx) : 0), &ee, &pp, &mm);
+            (*ops)++;
+        } else if (BIT(DA, x)) {
+            const int b = partner[x];
+            const int js_a = sidx >= 0 ? BIT(s->J[x], sidx) : 0, js_b = sidx >= 0 ? BIT(s->J[b], sidx) : 0;
+            gamma_ab(&ee, &pp, &mm, el_getD(s, x) + sigma * 4 * js_a, el_getD(s, b) + sigma * 4 * js_b);
+            (*ops)++;
+        } else {
+            continue;
+        }
+        if (!ee) {
+            *e = 0; *p = 0; *m = 0;
+            return;
+        }
+        P += pp;
+        Ms += mm;
+    }
+    *e = 1;
+    *p = P;
+    *m = (Mm | DA) ? (tM0 + Ms) % 8 : tM0;
+}
+
+static void el_exp_sum(el_state *s, int *eps, int *p, int *m, int64_t *ops) {
+    const int k = s->k;
+    const uint64_t km = k >= 64 ? ~0ULL : (ONE(k) - 1);
+    const uint64_t Sm = s->D1 & km;
+    int sidx = -1;
+    if (Sm) {
+        const int a = __builtin_ctzll(Sm);
+        const uint64_t U = Sm & ~ONE(a);
+        if (U) el_applyR(s, a, U, -1, 0, ops);
+        else {
+            s->D1 &= km;
+            s->D2 &= km;
+        }
+        el_swap(s, a, k - 1, ops);
+        sidx = k - 1;
+    }
+    uint64_t E = km & ~(sidx >= 0 ? ONE(sidx) : 0);
+    uint64_t Mm = 0, DA = 0;
+    int partner[CSIM_MAX_QUBITS] = {0};
+    while (E) {
+        const int a = __builtin_ctzll(E);
+        const uint64_t ra = s->J[a], K = ra & E & ~ONE(a);
+        (*ops)++;
+        if (!K) {
+            Mm |= ONE(a);
+            E &= ~ONE(a);
+        } else {
+            const int b = __builtin_ctzll(K);
+            const uint64_t Ep = E & ~ONE(a) & ~ONE(b);
+            const uint64_t vb = ra & Ep, va = s->J[b] & Ep;
+            if (vb | va) el_applyR(s, b, vb, a, va, ops);
+            else {
+                s->D1 &= km;
+                s->D2 &= km;
+            }
+            DA |= ONE(a);
+            partner[a] = b;
+            E = Ep;
+        }
+    }
+    if (sidx < 0) {
+        el_wsigma(s, 0, -1, Mm, DA, partner, eps, p, m, ops);
+        return;
+    }
+    int e0, p0, m0, e1, p1, m1;
+    el_wsigma(s, 0, sidx, Mm, DA, partner, &e0, &p0, &m0, ops);
+    el_wsigma(s, 1, sidx, Mm, DA, partner, &e1, &p1, &m1, ops);
+    if (e0 == 0) { *eps = e1; *p = p1; *m = m1; return; }
+    if (e1 == 0) { *eps = e0; *p = p0; *m = m0; return; }
+    if (p0 != p1 || ((m1 - m0) % 2) != 0) { orc_assert_failures++; return; }
+    int ee, pp = 0, mm = 0;
+    el_partial_gamma(m1 - m0, &ee, &pp, &mm);
+    *eps = ee;
+    if (!ee) { *p = 0; *m = 0; }
+    else { *p = pp + p0; *m = mm + m0 % 8; }
+}
+
+void orc_pair_rowops(const csim_state *theta, uint64_t x, int *eps, int *p, int *m, int64_t *ops) {
+    el_state s;
+    s.n = theta->n;
+    s.k = theta->k;
+    s.Q = theta->Q;
+    s.h = theta->h;
+    s.D1 = theta->D1;
+    s.D2 = theta->D2;
+    memcpy(s.G, theta->G, sizeof(s.G));
+    memcpy(s.J, theta->J, sizeof(s.J));
+    const int k1 = s.k, k2 = popc(x);
+    uint64_t zeros = ~x & (s.n >= 64 ? ~0ULL : (ONE(s.n) - 1));
+    *ops = 0;
+    while (zeros) {
+        const int q = 63 - __builtin_clzll(zeros);
+        zeros &= ~ONE(q);
+        *eps = el_shrink_unit(&s, q, ops);
+        if (*eps == 0) {
+            *p = 0;
+            *m = 0;
+            return;
+        }
+    }
+    el_exp_sum(&s, eps, p, m, ops);
+    *p -= k1 + k2;
+}

@@ -70,6 +70,11 @@ double orc_project(csim_state *s, const csim_projector *P);
 void orc_term_products(int t, int exact, const uint64_t *L, int k, int64_t ntheta, const csim_state *theta,
                        int64_t j0, int64_t nj, int32_t *eps, int32_t *p, int32_t *m, int threads);
 
+/* One (theta, term-of-|L>) pair by elementary rank-one updates, with the number
+ * of packed 64-bit row operations it takes (the roofline's work unit).  Same
+ * (eps, p, m) as orc_inner_product_exact with the prepL term of codeword x. */
+void orc_pair_rowops(const csim_state *theta, uint64_t x, int *eps, int *p, int *m, int64_t *ops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -99,6 +99,7 @@ class Oracle:
                                       C.POINTER(C.c_double), C.c_void_p, C.POINTER(RngState)]
         lib.orc_term_products.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int64, _st_p, C.c_int64,
                                           C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        lib.orc_pair_rowops.argtypes = [_st_p, C.c_uint64, _ip, _ip, _ip, C.POINTER(C.c_int64)]
         self.assert_failures = C.c_int.in_dll(lib, "orc_assert_failures")
 
     # -- rng
@@ -161,6 +162,11 @@ class Oracle:
     def codeword(self, i, L):
         L = np.ascontiguousarray(L, dtype=np.uint64)
         return int(self.lib.orc_codeword(int(i), _ptr(L), len(L)))
+
+    def pair_rowops(self, theta, x):
+        e, p, m, ops = C.c_int(0), C.c_int(0), C.c_int(0), C.c_int64(0)
+        self.lib.orc_pair_rowops(_ptr(theta), int(x), C.byref(e), C.byref(p), C.byref(m), C.byref(ops))
+        return (e.value, p.value, m.value), ops.value
 
     def project(self, s, P):
         return self.lib.orc_project(_ptr(s), C.byref(P))

@@ -1,0 +1,318 @@
+"""Parity of the CUDA path (through the C ABI of libcsimgpu.so) with the
+reference: its unit-test fixtures, vectors produced by the reference's own C
+code, and the oracle restatement on seeded inputs up to the c2 workload's shape
+(t = 40, chi = 2^16).  Integer results must be bit-exact, (eps, p, m) with m
+unreduced; probabilities within 1e-12 relative (+1e-12 absolute floor, for
+sums that cancel) of the reference's double accumulation on the same draws."""
+import os
+
+import numpy as np
+import pytest
+
+from circuitsimulator_gb300 import backend
+from circuitsimulator_gb300.state import STATE_DTYPE
+from golden.golden_io import state_from_json, states_from_json
+from helpers import close, full_view, phase_m, rand_word, random_projector_rows
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-12
+FLOOR = 1e-12
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    b = backend.Backend(0)
+    yield b
+    b.close()
+
+
+def _words(xs):
+    return np.array([int(x, 16) for x in xs], dtype=np.uint64)
+
+
+# ---------------------------------------------------------------- reference unit-test fixtures
+def test_fixture_exponential_sum(gpu, golden_fixtures):
+    cases = golden_fixtures["exponential_sum"]
+    s = states_from_json([c["in"] for c in cases])
+    eps, p, m = gpu.exponentialSumExact(s)
+    for i, c in enumerate(cases):
+        assert [eps[i], p[i], m[i]] == list(c["ref"]), i
+        f = c["fixture"]
+        assert eps[i] == f[0] and p[i] == f[1] and m[i] % 8 == f[2] % 8
+        assert full_view(s[i]) == full_view(state_from_json(c["ref_state"])), i
+
+
+def test_fixture_shrink(gpu, golden_fixtures):
+    cases = golden_fixtures["shrink"]
+    s = states_from_json([c["in"] for c in cases])
+    st = gpu.shrink(s, _words([c["xi"] for c in cases]), [c["alpha"] for c in cases], lazy=False)
+    for i, c in enumerate(cases):
+        assert st[i] == c["ref_status"] == c["fixture"]["status"]
+        assert full_view(s[i]) == full_view(state_from_json(c["ref_state"])), i
+
+
+def test_fixture_measure_pauli(gpu, golden_fixtures):
+    cases = golden_fixtures["measure_pauli"]
+    s = states_from_json([c["in"] for c in cases])
+    res = gpu.measurePauli(s, [c["m"] for c in cases], _words([c["zeta"] for c in cases]),
+                           _words([c["xi"] for c in cases]))
+    for i, c in enumerate(cases):
+        assert res[i] == c["ref_result"]
+        assert full_view(s[i]) == full_view(state_from_json(c["ref_state"])), i
+
+
+def test_fixture_extend(gpu, golden_fixtures):
+    cases = golden_fixtures["extend"]
+    s = states_from_json([c["in"] for c in cases])
+    gpu.extend(s, _words([c["xi"] for c in cases]))
+    for i, c in enumerate(cases):
+        assert full_view(s[i]) == full_view(state_from_json(c["ref_state"])), i
+
+
+def test_fixture_inner_product(gpu, golden_fixtures):
+    cases = golden_fixtures["inner_product"]
+    a = states_from_json([c["a"] for c in cases])
+    b = states_from_json([c["b"] for c in cases])
+    eps, p, m = gpu.innerProductExact(a, b)
+    for i, c in enumerate(cases):
+        assert [eps[i], p[i], m[i]] == list(c["ref"])
+
+
+# ---------------------------------------------------------------- vectors from the reference's C code
+def test_random_states_replay(gpu, golden_seeded):
+    by_n = {}
+    for rec in golden_seeded["random_states"]:
+        by_n.setdefault(rec["n"], []).append(rec)
+    for n, recs in by_n.items():
+        words = np.concatenate([np.array(r["words"], dtype=np.uint32) for r in recs])
+        offs = np.cumsum([0] + [len(r["words"]) for r in recs]).astype(np.int64)
+        out = gpu.randomStabilizerStateReplay(n, words, offs)
+        for i, r in enumerate(recs):
+            assert full_view(out[i]) == full_view(state_from_json(r["state"])), (n, i)
+
+
+def test_random_states_replay_short_segment_is_an_error(gpu, golden_seeded):
+    rec = [r for r in golden_seeded["random_states"] if r["n"] == 12][0]
+    words = np.array(rec["words"][:-3], dtype=np.uint32)
+    with pytest.raises(backend.CsimError):
+        gpu.randomStabilizerStateReplay(12, words, np.array([0, len(words)], dtype=np.int64))
+
+
+def test_term_pairs(gpu, golden_seeded):
+    for e in golden_seeded["term_pairs"]:
+        t = e["t"]
+        L = _words(e["L"])
+        thetas = states_from_json(e["theta"])
+        js = e["j"]
+        j0, nj = min(js), max(js) - min(js) + 1
+        eps, p, m = gpu.term_products(t, False, L, thetas, j0, nj)
+        for a in range(len(thetas)):
+            for jj, j in enumerate(js):
+                assert [eps[a, j - j0], p[a, j - j0], m[a, j - j0]] == list(e["prod_l"][a][jj]), (t, a, j)
+        if "jh" in e:
+            jh = e["jh"]
+            j0, nj = min(jh), max(jh) - min(jh) + 1
+            eps, p, m = gpu.term_products(t, True, None, thetas, j0, nj)
+            for a in range(len(thetas)):
+                for jj, j in enumerate(jh):
+                    assert [eps[a, j - j0], p[a, j - j0], m[a, j - j0]] == list(e["prod_h"][a][jj]), (t, a, j)
+        phis = gpu.prepL(e["j"][: len(e["phi_l"])], t, L)
+        for i, d in enumerate(e["phi_l"]):
+            assert full_view(phis[i]) == full_view(state_from_json(d))
+        if "phi_h" in e:
+            phis = gpu.prepH(e["jh"][: len(e["phi_h"])], t)
+            for i, d in enumerate(e["phi_h"]):
+                assert full_view(phis[i]) == full_view(state_from_json(d))
+
+
+def test_state_pairs(gpu, golden_seeded):
+    cases = golden_seeded["state_pairs"]
+    a = states_from_json([c["a"] for c in cases])
+    b = states_from_json([c["b"] for c in cases])
+    eps, p, m = gpu.innerProductExact(a, b)
+    for i, c in enumerate(cases):
+        assert [eps[i], p[i], m[i]] == list(c["ref"]), i
+
+
+def test_estimators_same_draws(gpu, golden_seeded):
+    for e in golden_seeded["estimators"]:
+        t, exact = e["t"], e["exact"]
+        pr = e["projector"]
+        P = backend.projector(pr["phase"], _words(pr["xs"]), _words(pr["zs"]), t)
+        L = None if exact else _words(e["L"])
+        singles = gpu.singleProjectorSample(P, L, exact, len(e["singles"]), backend.RNG_LIBC, e["seed"])
+        for a, b in zip(singles, e["singles"]):
+            assert close(a, b, REL, FLOOR), (a, b)
+        v = gpu.multiSampledProjector(P, L, exact, e["norm"], e["samples"], e["bins"], backend.RNG_LIBC, e["seed"])
+        assert close(v, e["multi"], REL, FLOOR), (v, e["multi"])
+        if e["exact_projector"] is not None:
+            x = gpu.exactProjector(P, L, exact, e["norm"])
+            assert close(x, e["exact_projector"], REL, FLOOR), (x, e["exact_projector"])
+
+
+# ---------------------------------------------------------------- seeded inputs vs the oracle
+def _project_all(gpu, states, rows):
+    """measurePauli row by row on every state; drops annihilated ones (innerprod.c:104-116)."""
+    ph, xs, zs = rows
+    keep = np.ones(len(states), dtype=bool)
+    pf = np.ones(len(states))
+    for r in range(len(ph)):
+        idx = np.nonzero(keep)[0]
+        sub = states[idx].copy()
+        res = gpu.measurePauli(sub, phase_m(ph[r]), zs[r], xs[r])
+        states[idx] = sub
+        pf[idx] *= res
+        keep[idx[res == 0]] = False
+    return states[keep], pf[keep]
+
+
+@pytest.mark.parametrize("t,k,ntheta,nj", [(3, 3, 8, 8), (7, 5, 16, 32), (24, 10, 12, 96), (33, 9, 12, 64),
+                                           (40, 16, 12, 96), (64, 14, 6, 48)])
+def test_term_products_vs_oracle(gpu, oracle, t, k, ntheta, nj):
+    rs = np.random.RandomState(1000 + t)
+    L = np.array([rand_word(rs, t) for _ in range(k)], dtype=np.uint64)
+    th = gpu.randomStabilizerState(t, 3 * ntheta, seed=77 + t)
+    th, _ = _project_all(gpu, th, random_projector_rows(rs, t, max(1, t // 4)))
+    th = th[:ntheta]
+    assert len(th) > 0
+    j0 = int(rs.randint(0, max(1, 2 ** k - nj)))
+    nj = min(nj, 2 ** k - j0)
+    eg, pg, mg = gpu.term_products(t, False, L, th, j0, nj)
+    eo, po, mo = oracle.term_products(t, 0, L, k, th, j0, nj, threads=os.cpu_count() or 1)
+    assert (eg.reshape(-1) == eo).all() and (pg.reshape(-1) == po).all() and (mg.reshape(-1) == mo).all()
+    if t <= 24:
+        nh = min(nj, 2 ** ((t + 1) // 2))
+        eg, pg, mg = gpu.term_products(t, True, None, th, 0, nh)
+        eo, po, mo = oracle.term_products(t, 1, None, 0, th, 0, nh, threads=os.cpu_count() or 1)
+        assert (eg.reshape(-1) == eo).all() and (pg.reshape(-1) == po).all() and (mg.reshape(-1) == mo).all()
+
+
+def test_random_states_philox_are_valid(gpu):
+    """Counter-based draws keep the invariants of randomStabilizerState's output."""
+    for n in (1, 5, 31, 32, 33, 40, 64):
+        s = gpu.randomStabilizerState(n, 64, seed=9)
+        for x in s:
+            k = int(x["k"])
+            G = [int(v) for v in x["G"][:n]]
+            B = [int(v) for v in x["Gbar"][:n]]
+            for a in range(n):
+                for b in range(n):
+                    assert bin(G[a] & B[b]).count("1") % 2 == (a == b)
+            J = [int(v) for v in x["J"][:n]]
+            for a in range(k):
+                assert ((J[a] >> a) & 1) == ((int(x["D1"]) >> a) & 1)
+                for b in range(k):
+                    assert ((J[a] >> b) & 1) == ((J[b] >> a) & 1)
+            assert int(x["Q"]) == 0
+
+
+def test_philox_sampler_matches_its_own_states(gpu):
+    """singleProjectorSample with the counter-based generator equals the
+    explicit pipeline (same draws -> project -> all pairs -> exact sum)."""
+    rs = np.random.RandomState(5)
+    t, k, count = 12, 6, 24
+    L = [rand_word(rs, t) for _ in range(k)]
+    rows = random_projector_rows(rs, t, 3)
+    P = backend.projector(rows[0], rows[1], rows[2], t)
+    vals = gpu.singleProjectorSample(P, L, False, count, backend.RNG_PHILOX, 4242)
+    th = gpu.randomStabilizerState(t, count, seed=4242, first=0)
+    for i in range(count):
+        s = th[i:i + 1].copy()
+        pf = 1.0
+        for r in range(len(rows[0])):
+            res = gpu.measurePauli(s, phase_m(rows[0][r]), rows[2][r], rows[1][r])[0]
+            pf *= res
+            if res == 0:
+                break
+        if pf == 0:
+            assert vals[i] == 0
+            continue
+        eps, p, m = gpu.term_products(t, False, L, s, 0, 2 ** k)
+        tot = sum(complex((2.0 ** (pp / 2.0)) * np.exp(1j * np.pi * (mm % 8) / 4.0)) * e
+                  for e, pp, mm in zip(eps[0], p[0], m[0]))
+        want = 2.0 ** t * abs(tot * pf) ** 2
+        assert close(vals[i], want, 1e-10, 1e-12), (i, vals[i], want)
+
+
+@pytest.mark.slow
+def test_c2_shape_subsample_bit_exact(gpu, oracle):
+    """t = 40, chi = 2^16 (the c2 workload's code size): 10^5 (theta, term) pairs
+    drawn at random from 8 projected thetas x all 2^16 terms, bit-exact against
+    the oracle; plus a checksum of every pair's value against the fused
+    per-theta accumulation of the sampler."""
+    rs = np.random.RandomState(40)
+    t, k = 40, 16
+    L = np.array([rand_word(rs, t) for _ in range(k)], dtype=np.uint64)
+    rows = random_projector_rows(rs, t, 10)
+    th = gpu.randomStabilizerState(t, 32, seed=2024)
+    th, pf = _project_all(gpu, th, rows)
+    th, pf = th[:8], pf[:8]
+    eps, p, m = gpu.term_products(t, False, L, th, 0, 2 ** k)
+    # 10^5-pair subsample: 12 random blocks of 1024 consecutive terms per theta
+    nthreads = os.cpu_count() or 1
+    checked = 0
+    for a in range(len(th)):
+        for j0 in rs.choice(2 ** k // 1024, size=12, replace=False) * 1024:
+            j0 = int(j0)
+            eo, po, mo = oracle.term_products(t, 0, L, k, th[a:a + 1], j0, 1024, threads=nthreads)
+            assert (eps[a, j0:j0 + 1024] == eo).all() and (p[a, j0:j0 + 1024] == po).all() \
+                and (m[a, j0:j0 + 1024] == mo).all(), (a, j0)
+            checked += 1024
+    assert checked >= 98000
+    # the reference's p lies in [-2t, t] (p_expsum - k1 - k2), m in [0, 14]
+    assert (m >= 0).all() and (m <= 14).all() and (p <= t).all() and (p >= -2 * t).all()
+
+
+def _exact_sum(eps, p, m, P):
+    """sum of eps 2^{p/2} w^m as exact Z[w] coordinates scaled by 2^{P/2} (Python ints)."""
+    z = [0, 0, 0, 0]
+    for e, pp, mm in zip(eps.tolist(), p.tolist(), m.tolist()):
+        if not e:
+            continue
+        q, mm = pp + P, mm % 8
+        if q % 2 == 0:
+            z[mm & 3] += -(1 << (q // 2)) if mm >= 4 else (1 << (q // 2))
+        else:
+            c = 1 << ((q - 1) // 2)
+            a, b = (mm + 1) % 8, (mm + 3) % 8
+            z[a & 3] += -c if a >= 4 else c
+            z[b & 3] -= -c if b >= 4 else c
+    return z
+
+
+@pytest.mark.slow
+def test_c2_shape_sampler_checksum(gpu):
+    """t = 40, chi = 2^16: the fused sampler (draw -> project -> all 2^16 terms ->
+    per-theta exact sum) equals the exact sum of the 2^16 per-pair results of
+    the same draws, theta by theta (a checksum over 65536 pairs per theta)."""
+    rs = np.random.RandomState(41)
+    t, k, count, seed = 40, 16, 24, 99
+    L = [rand_word(rs, t) for _ in range(k)]
+    rows = random_projector_rows(rs, t, 6)
+    P = backend.projector(rows[0], rows[1], rows[2], t)
+    vals = gpu.singleProjectorSample(P, L, False, count, backend.RNG_PHILOX, seed)
+    th = gpu.randomStabilizerState(t, count, seed=seed, first=0)
+    s2 = 0.70710678118654752440
+    checked = 0
+    for i in range(count):
+        s = th[i:i + 1].copy()
+        pf = 1.0
+        for r in range(len(rows[0])):
+            res = gpu.measurePauli(s, phase_m(rows[0][r]), rows[2][r], rows[1][r])[0]
+            pf *= res
+            if res == 0:
+                break
+        if pf == 0:
+            assert vals[i] == 0
+            continue
+        eps, p, m = gpu.term_products(t, False, L, s, 0, 2 ** k)
+        z = _exact_sum(eps[0], p[0], m[0], 2 * t)
+        re = (z[0] + (z[1] - z[3]) * s2) * 2.0 ** -t
+        im = (z[2] + (z[1] + z[3]) * s2) * 2.0 ** -t
+        want = 2.0 ** t * ((re * pf) ** 2 + (im * pf) ** 2)
+        assert close(vals[i], want, 1e-13, 1e-300), (i, vals[i], want)
+        checked += 1
+        if checked == 4:
+            break
+    assert checked >= 2
