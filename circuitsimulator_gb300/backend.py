@@ -27,6 +27,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libcsimgpu.so")
 EXE_PATH = os.path.join(PKG, "gpubackend")
 
+OPT_PAIR_KERNEL = 1
+OPT_PER_THREAD = 2
 RNG_PHILOX = 0
 RNG_LIBC = 1
 SEED_CONTINUE = (1 << 64) - 1
@@ -74,6 +76,7 @@ def load_library(path=LIB_PATH):
         "csim_last_error": ([vp], C.c_char_p),
         "csim_launch_count": ([vp], i64),
         "csim_last_stats": ([vp, vp], C.c_int),
+        "csim_set_option": ([vp, i32, i64], C.c_int),
         "csim_inner_product_exact": ([vp, i64, vp, vp, vp, vp, vp], C.c_int),
         "csim_exponential_sum_exact": ([vp, i64, vp, vp, vp, vp], C.c_int),
         "csim_shrink": ([vp, i64, vp, vp, vp, i32, vp], C.c_int),
@@ -176,6 +179,10 @@ class Backend:
     @property
     def launches(self):
         return int(self.lib.csim_launch_count(self.ctx))
+
+    def set_option(self, option, value):
+        """CSIM_OPT_PAIR_KERNEL = 1 (0 thread-per-pair, 1 warp-per-pair), CSIM_OPT_PER_THREAD = 2."""
+        self._check(self.lib.csim_set_option(self.ctx, int(option), int(value)))
 
     def last_stats(self):
         st = Stats()

@@ -182,6 +182,8 @@ struct csim_ctx {
     uint64_t philox_next = 0;
     csim_stats stats = {};
     int64_t stats_launch0 = 0;
+    int pair_kernel = 0;  // CSIM_OPT_PAIR_KERNEL
+    int per_thread = 16;  // CSIM_OPT_PER_THREAD
     cudaEvent_t ev[4] = {};
 };
 
@@ -343,6 +345,22 @@ extern "C" void csim_ctx_destroy(csim_ctx* ctx) {
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
+}
+
+extern "C" int csim_set_option(csim_ctx* ctx, int32_t option, int64_t value) {
+    if (!ctx) return CSIM_ERR_ARG;
+    switch (option) {
+    case CSIM_OPT_PAIR_KERNEL:
+        if (value != 0 && value != 1) return fail(ctx, CSIM_ERR_ARG, "pair kernel must be 0 or 1");
+        ctx->pair_kernel = (int)value;
+        return CSIM_OK;
+    case CSIM_OPT_PER_THREAD:
+        if (value < 1 || value > 64) return fail(ctx, CSIM_ERR_ARG, "per-thread pairs must be 1..64");
+        ctx->per_thread = (int)value;
+        return CSIM_OK;
+    default:
+        return fail(ctx, CSIM_ERR_ARG, "unknown option %d", option);
+    }
 }
 
 extern "C" int csim_last_stats(const csim_ctx* ctx, csim_stats* out) {
@@ -671,9 +689,13 @@ extern "C" int csim_term_products(csim_ctx* ctx, int32_t t, int32_t exact, const
         int* dp = (int*)v;
         CKR(dbuf(ctx, kBufM, c * nj * 4, &v));
         int* dm = (int*)v;
-        if (csim::launch_terms(launch_of(ctx), nr, exact ? 1 : 0, dcw, (const csim::GState*)dphis,
-                               (const csim::GState*)dth, nullptr, c, j0, nj, 64, 2 * t, nullptr, nullptr, de, dp, dm))
-            return fail(ctx, CSIM_ERR_CUDA, "term launch failed");
+        const int rc = (!exact && ctx->pair_kernel == 0)
+                           ? csim::launch_terms_tp(launch_of(ctx), t, dcw, (const csim::GState*)dth, nullptr, c, j0, nj,
+                                                   ctx->per_thread, 2 * t, nullptr, de, dp, dm)
+                           : csim::launch_terms(launch_of(ctx), nr, exact ? 1 : 0, dcw, (const csim::GState*)dphis,
+                                                (const csim::GState*)dth, nullptr, c, j0, nj, 64, 2 * t, nullptr,
+                                                nullptr, de, dp, dm);
+        if (rc) return fail(ctx, CSIM_ERR_CUDA, "term launch failed");
         CKR(dget(ctx, eps + o * nj, de, c * nj));
         CKR(dget(ctx, p + o * nj, dp, c * nj));
         CKR(dget(ctx, m + o * nj, dm, c * nj));
@@ -707,7 +729,9 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
     const int nr = t > 32 ? 2 : 1;
     const int64_t chi = exact ? ((int64_t)1 << ((t + 1) / 2)) : ((int64_t)1 << k);
     const int P2 = 2 * t;
-    const int64_t chunk = chunk_for(chi), nchunks = (chi + chunk - 1) / chunk;
+    const bool tp = !exact && ctx->pair_kernel == 0;
+    const int64_t chunk = chunk_for(chi);
+    const int64_t nchunks = tp ? csim::terms_tp_blocks(chi, ctx->per_thread) : (chi + chunk - 1) / chunk;
 
     std::vector<int> hm(P->nstabs);
     for (int r = 0; r < P->nstabs; r++) hm[r] = phase_m(P->phase[r]);
@@ -764,9 +788,12 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
         __int128* dpart = (__int128*)v;
         CK(cudaMemsetAsync(dpart, 0, nparts * sizeof(__int128), ctx->stream));
         CK(cudaEventRecord(ctx->ev[1], ctx->stream));
-        if (csim::launch_terms(launch_of(ctx), nr, exact ? 1 : 0, dcw, (const csim::GState*)dphis, dth, dcode, c, 0,
-                               chi, (int)chunk, P2, dpart, nullptr, nullptr, nullptr, nullptr))
-            return fail(ctx, CSIM_ERR_CUDA, "term launch failed");
+        const int rc = tp ? csim::launch_terms_tp(launch_of(ctx), t, dcw, dth, dcode, c, 0, chi, ctx->per_thread, P2,
+                                                  dpart, nullptr, nullptr, nullptr)
+                          : csim::launch_terms(launch_of(ctx), nr, exact ? 1 : 0, dcw, (const csim::GState*)dphis, dth,
+                                               dcode, c, 0, chi, (int)chunk, P2, dpart, nullptr, nullptr, nullptr,
+                                               nullptr);
+        if (rc) return fail(ctx, CSIM_ERR_CUDA, "term launch failed");
         CK(cudaEventRecord(ctx->ev[2], ctx->stream));
         CKR(dbuf(ctx, kBufAcc, (size_t)c * 4 * sizeof(__int128), &v));
         __int128* dacc = (__int128*)v;

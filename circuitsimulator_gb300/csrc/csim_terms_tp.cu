@@ -1,0 +1,144 @@
+// csim_terms_tp.cu — the (theta, prepL term) pair kernel, one thread per pair.
+//
+// For a term phi_x of |L> (a product of |0> and |+>, libcirc/stateprep.c:85-120)
+// innerProductExact(theta, phi_x) (libcirc/stabilizer/stabilizer.c:589-659)
+// reduces to shrinks of theta by e_q, alpha = 0, for the zero bits q of the
+// codeword x in descending order, then exponentialSumExact: phi_x has
+// Q = D = J = h = 0, so the R stage (stabilizer.c:611-652) changes nothing.
+//
+// Each thread keeps its pair's working state in shared memory with a
+// [index][thread] layout (one 64-bit word per thread per index, so every
+// access is conflict-free whatever the index):
+//   sJ[r]  row r of J                       (r < k)
+//   sGT[c] column c of G as a row mask       (only the zero columns of x,
+//          the only ones a later shrink or h-update of this pair reads)
+// and D1, D2, h, Q, k in registers.  Every basis change is the elementary
+// rank-one update of csim_warp.cuh applied row by row, with each row's
+// column bits gathered in the same pass; the exponential sum folds each
+// monomer/dimer factor into W0/W1 as soon as that row is final
+// (stabilizer.c:372-418 never touches a finished row again).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "csim_internal.h"
+#include "csim_pair_core.cuh"
+#include "csim_warp.cuh"
+
+namespace csim {
+
+constexpr int kTP = 64;  // threads per block
+
+struct TPShared {
+    // pristine theta
+    uint64_t pJ[64];
+    uint64_t pGT[64];
+    uint64_t h, D1, D2;
+    int n, k, Q, live;
+    __int128 red[kTP][4];
+};
+
+// Work item = (theta a, block of kTP * per_thread consecutive terms).  Thread t
+// takes terms jb + t + kTP * r, r < per_thread.  Partial sums: 4 int128 per item.
+__global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, const GState* theta, const int* code,
+                                                  int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P,
+                                                  int nmax, __int128* part, int* eps_o, int* p_o, int* m_o,
+                                                  int* err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TPShared& sh = *reinterpret_cast<TPShared*>(smem_raw);
+    const int tid = threadIdx.x;
+    int e = 0;
+    const int64_t span = (int64_t)kTP * per_thread;
+    const int64_t nblk = (nj + span - 1) / span;
+    const int64_t items = ntheta * nblk;
+    for (int64_t item = blockIdx.x; item < items; item += gridDim.x) {
+        const int64_t a = item / nblk, cb = item % nblk;
+        __syncthreads();  // previous item's use of sh is over
+        if (tid == 0) {
+            sh.live = code ? (code[a] >= 0) : 1;
+            sh.n = theta[a].n;
+            sh.k = theta[a].k;
+            sh.Q = theta[a].Q;
+            sh.h = theta[a].h;
+            sh.D1 = theta[a].D1;
+            sh.D2 = theta[a].D2;
+        }
+        {
+            const GState* g = theta + a;
+            sh.pJ[tid] = g->J[tid];
+            // transpose G: column c as a mask over rows < k
+            const int n = g->n, k = g->k;
+            uint64_t col = 0ull;
+            if (tid < n)
+                for (int r = 0; r < k; r++) col |= ((g->G[r] >> tid) & 1ull) << r;
+            sh.pGT[tid] = col;
+        }
+        __syncthreads();
+        __int128 z[4] = {0, 0, 0, 0};
+        const int n = sh.n;
+        if (n > nmax) e |= kErrArg;
+        if (sh.live && n >= 1 && n <= nmax) {
+            uint64_t* sJ = reinterpret_cast<uint64_t*>(smem_raw + sizeof(TPShared));
+            uint64_t* sGT = sJ + (size_t)nmax * kTP;
+            const int64_t jb = j0 + cb * span;
+            for (int r = 0; r < per_thread; r++) {
+                const int64_t j = jb + tid + (int64_t)kTP * r;
+                if (j >= j0 + nj) break;
+                const uint64_t x = codewords[j - j0];
+                int eps, pp, mm;
+                pc::pair_l(n, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ, sh.pGT, x, sJ + tid, sGT + tid, kTP, eps, pp,
+                           mm, e);
+                pc::zacc(z, eps, pp, mm, P, e);
+                if (eps_o) {
+                    const int64_t w = a * nj + (j - j0);
+                    eps_o[w] = eps;
+                    p_o[w] = pp;
+                    m_o[w] = mm;
+                }
+            }
+        }
+        if (part) {
+            for (int q = 0; q < 4; q++) sh.red[tid][q] = z[q];
+            __syncthreads();
+            if (tid < 4) {
+                __int128 acc = 0;
+                for (int t = 0; t < kTP; t++) acc += sh.red[t][tid];
+                part[4 * item + tid] = acc;
+            }
+        }
+    }
+    e = (int)__reduce_or_sync(kFull, (unsigned)e);
+    if (e && (tid & 31) == 0) atomicOr(err, e);
+}
+
+size_t terms_tp_smem(int nmax) { return sizeof(TPShared) + (size_t)2 * nmax * kTP * sizeof(uint64_t); }
+
+int launch_terms_tp(const Launch& L, int nmax, const uint64_t* codewords, const GState* theta, const int* code,
+                    int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P, __int128* part, int* eps_o,
+                    int* p_o, int* m_o) {
+    if (ntheta <= 0 || nj <= 0) return 0;
+    if (nmax < 1 || nmax > 64) return -1;
+    const int64_t span = (int64_t)kTP * per_thread;
+    const int64_t nblk = (nj + span - 1) / span;
+    const size_t smem = terms_tp_smem(nmax);
+    if (cudaFuncSetAttribute(k_terms_tp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)terms_tp_smem(64)) !=
+        cudaSuccess)
+        return -1;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_terms_tp, kTP, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    const int64_t items = ntheta * nblk;
+    int64_t grid = (int64_t)L.num_sms * per_sm;
+    if (grid > items) grid = items;
+    k_terms_tp<<<(int)grid, kTP, smem, L.stream>>>(codewords, theta, code, ntheta, j0, nj, per_thread, P, nmax, part,
+                                                    eps_o, p_o, m_o, L.d_err);
+    (*L.launches)++;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int64_t terms_tp_blocks(int64_t nj, int per_thread) {
+    const int64_t span = (int64_t)kTP * per_thread;
+    return (nj + span - 1) / span;
+}
+
+}  // namespace csim

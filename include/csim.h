@@ -111,6 +111,11 @@ typedef struct csim_stats {
 } csim_stats;
 int csim_last_stats(const csim_ctx *ctx, csim_stats *out);
 
+/* Tuning options (no counterpart in the reference). */
+#define CSIM_OPT_PAIR_KERNEL 1 /* |L>-term pairs: 0 = one thread per pair (default), 1 = one warp per pair */
+#define CSIM_OPT_PER_THREAD 2  /* |L>-term pairs per thread per work item of the thread-per-pair kernel (1..64) */
+int csim_set_option(csim_ctx *ctx, int32_t option, int64_t value);
+
 /* ----------------------------------------------- stabilizer primitives (batched) */
 
 /* eps/p/m of <a[i]|b[i]> for i < count; value = eps * 2^{p/2} * e^{i pi m/4}.

@@ -316,3 +316,28 @@ def test_c2_shape_sampler_checksum(gpu):
         if checked == 4:
             break
     assert checked >= 2
+
+
+@pytest.mark.parametrize("t,k", [(12, 6), (40, 16), (64, 12)])
+def test_pair_kernels_agree(gpu, t, k):
+    """Thread-per-pair and warp-per-pair kernels: identical per-pair results and
+    identical sampler values (exact sums)."""
+    rs = np.random.RandomState(7000 + t)
+    L = [rand_word(rs, t) for _ in range(k)]
+    rows = random_projector_rows(rs, t, max(1, t // 5))
+    th = gpu.randomStabilizerState(t, 12, seed=31 + t)
+    th, _ = _project_all(gpu, th, rows)
+    nj = min(2 ** k, 8192)
+    try:
+        gpu.set_option(backend.OPT_PAIR_KERNEL, 0)
+        a = gpu.term_products(t, False, L, th, 0, nj)
+        P = backend.projector(rows[0], rows[1], rows[2], t)
+        va = gpu.singleProjectorSample(P, L, False, 16, backend.RNG_PHILOX, 5)
+        gpu.set_option(backend.OPT_PAIR_KERNEL, 1)
+        b = gpu.term_products(t, False, L, th, 0, nj)
+        vb = gpu.singleProjectorSample(P, L, False, 16, backend.RNG_PHILOX, 5)
+    finally:
+        gpu.set_option(backend.OPT_PAIR_KERNEL, 0)
+    for x, y in zip(a, b):
+        assert (x == y).all()
+    assert (va == vb).all()

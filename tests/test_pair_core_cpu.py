@@ -1,0 +1,89 @@
+"""The thread-per-pair kernel's pair routine (csim_pair_core.cuh), compiled
+for the host, against the oracle: (eps, p, m) bit-exact, m unreduced, on
+seeded projected states at t = 1..64 and on the reference's golden pairs."""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from golden.golden_io import states_from_json
+from helpers import phase_m, rand_word, random_projector_rows
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "native", "tp_host_check.cpp")
+SO = os.path.join(HERE, "native", "_build", "libtphost.so")
+CORE = os.path.join(os.path.dirname(HERE), "circuitsimulator_gb300", "csrc", "csim_pair_core.cuh")
+
+
+@pytest.fixture(scope="module")
+def tp():
+    os.makedirs(os.path.dirname(SO), exist_ok=True)
+    if not os.path.exists(SO) or os.path.getmtime(SO) < max(os.path.getmtime(SRC), os.path.getmtime(CORE)):
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", SRC, "-o", SO])
+    lib = C.CDLL(SO)
+    lib.tp_host_pairs.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.tp_host_pairs.restype = C.c_int
+
+    def run(thetas, xs):
+        thetas = np.ascontiguousarray(thetas)
+        xs = np.ascontiguousarray(np.asarray(xs, dtype=np.uint64))
+        n = len(thetas) * len(xs)
+        e, p, m = (np.zeros(n, dtype=np.int32) for _ in range(3))
+        err = lib.tp_host_pairs(thetas.ctypes.data, len(thetas), xs.ctypes.data, len(xs), e.ctypes.data,
+                                p.ctypes.data, m.ctypes.data)
+        return err, e, p, m
+
+    return run
+
+
+@pytest.mark.parametrize("t,k", [(1, 1), (2, 2), (3, 3), (6, 4), (12, 6), (24, 8), (31, 8), (33, 8), (40, 10),
+                                 (57, 8), (63, 7), (64, 8)])
+def test_pair_core_vs_oracle(tp, oracle, t, k):
+    rs = np.random.RandomState(500 + t)
+    L = np.array([rand_word(rs, t) for _ in range(k)], dtype=np.uint64)
+    rows = random_projector_rows(rs, t, max(1, t // 3))
+    r = oracle.rng(t)
+    thetas = []
+    for _ in range(40):
+        s = oracle.random_state(t, r)
+        pf = 1.0
+        for q in range(len(rows[0])):
+            res = oracle.measure_pauli(s, phase_m(rows[0][q]), rows[2][q], rows[1][q])
+            pf *= res
+            if res == 0:
+                break
+        if pf:
+            thetas.append(s[0])
+        if len(thetas) == 8:
+            break
+    thetas = np.array(thetas)
+    js = np.unique(rs.randint(0, 2 ** k, size=48))
+    xs = [oracle.codeword(int(j), L) for j in js]
+    err, e, p, m = tp(thetas, xs)
+    assert err == 0
+    w = 0
+    for a in range(len(thetas)):
+        for jj, j in enumerate(js):
+            want = oracle.inner_product(thetas[a:a + 1], oracle.prep_l(int(j), t, L))
+            assert (e[w], p[w], m[w]) == want, (t, a, int(j))
+            w += 1
+
+
+def test_pair_core_golden(tp, golden_seeded):
+    for ent in golden_seeded["term_pairs"]:
+        t = ent["t"]
+        L = [int(x, 16) for x in ent["L"]]
+        thetas = states_from_json(ent["theta"])
+        xs = []
+        for j in ent["j"]:
+            x = 0
+            for rr in range(len(L)):
+                if (j >> (len(L) - 1 - rr)) & 1:
+                    x ^= L[rr]
+            xs.append(x)
+        err, e, p, m = tp(thetas, xs)
+        assert err == 0
+        got = np.stack([e, p, m], axis=1).reshape(len(thetas), len(xs), 3)
+        assert got.tolist() == ent["prod_l"]
