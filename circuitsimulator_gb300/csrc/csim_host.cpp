@@ -674,6 +674,15 @@ extern "C" int csim_term_products(csim_ctx* ctx, int32_t t, int32_t exact, const
     if (ntheta == 0 || nj == 0) return CSIM_OK;
     int nr;
     CKR(check_states(ctx, theta, ntheta, &nr, t));
+    // the thread-per-pair kernel needs a symmetric J block (always true of drawn states)
+    bool sym = true;
+    for (int64_t a = 0; a < ntheta && sym; a++)
+        for (int x = 0; x < theta[a].k && sym; x++)
+            for (int y = 0; y < theta[a].k; y++)
+                if (((theta[a].J[x] >> y) & 1) != ((theta[a].J[y] >> x) & 1)) {
+                    sym = false;
+                    break;
+                }
     uint64_t* dcw;
     csim_state* dphis;
     CKR(stage_terms(ctx, t, exact, L, k, j0, nj, &dcw, &dphis));
@@ -689,7 +698,7 @@ extern "C" int csim_term_products(csim_ctx* ctx, int32_t t, int32_t exact, const
         int* dp = (int*)v;
         CKR(dbuf(ctx, kBufM, c * nj * 4, &v));
         int* dm = (int*)v;
-        const int rc = (!exact && ctx->pair_kernel == 0)
+        const int rc = (!exact && ctx->pair_kernel == 0 && sym)
                            ? csim::launch_terms_tp(launch_of(ctx), t, dcw, (const csim::GState*)dth, nullptr, c, j0, nj,
                                                    ctx->per_thread, 2 * t, nullptr, de, dp, dm)
                            : csim::launch_terms(launch_of(ctx), nr, exact ? 1 : 0, dcw, (const csim::GState*)dphis,

@@ -97,6 +97,17 @@ struct PairRegs {
     uint64_t h, D1, D2;
 };
 
+// Warp-uniform loop bounds: on the device every lane of the warp runs the
+// same number of iterations (the warp maximum) with its own work predicated,
+// so the 32 pairs of a warp stay converged; on the host the bound is the
+// pair's own.
+CSIM_HD inline int uniform_max(int v) {
+#if defined(__CUDA_ARCH__)
+    return (int)__reduce_max_sync(0xffffffffu, (unsigned)v);
+#else
+    return v;
+#endif
+}
 
 CSIM_HD inline void tp_add_D(PairRegs& s, uint64_t u, int d1, int d2) {
     const uint64_t a1 = d1 ? u : 0ull, a2 = d2 ? u : 0ull;
@@ -105,69 +116,92 @@ CSIM_HD inline void tp_add_D(PairRegs& s, uint64_t u, int d1, int d2) {
     s.D2 ^= a2 ^ carry;
 }
 
-// shrink by e_q (alpha = 0) on the thread's pair; returns 0 EMPTY, 1 SAME, 2 SUCCESS.
-// `zrem` = zero columns still to be used (only those columns of G are kept).
-CSIM_HD inline int tp_shrink(PairRegs& s, uint64_t* sJ, uint64_t* sGT, int st, int q, uint64_t zrem) {
+CSIM_HD inline int tp_getD(const PairRegs& s, int i) { return 2 * (2 * getbit(s.D2, i) + getbit(s.D1, i)); }
+
+// Shrink by e_q (alpha = 0), stabilizer.c:500-585, for a symmetric J.
+// `act`: this lane has a shrink to do.  Returns 0 EMPTY, 1 SAME, 2 SUCCESS
+// (1 when inactive).  All lanes must call it together.
+//
+// With R = I + U e_i^T (U = S \ {i}, i = max S) and J symmetric,
+//   R J R^T = J + U Ji^T + Ji U^T + J_ii U U^T,
+// i.e. row x gets Ji if x in U and U if x in C = Ji ^ (J_ii ? U : 0); then
+// basis vectors i and kk = k-1 swap and kk is dropped: row kk moves to slot
+// i and every row's bit i becomes its old bit kk = bit x of row kk.  The +4
+// corrections of updateDJ are U & Ji, and updateQD's J.y is column kk of the
+// result, i.e. C with bit i taken from bit kk of C.
+CSIM_HD inline int tp_shrink(PairRegs& s, uint64_t* sJ, uint64_t* sGT, int st, int q, uint64_t zrem, bool act) {
     const int k = s.k;
     const uint64_t km = lowmask(k);
-    const uint64_t S = RG(q) & km;
-    const int beta = getbit(s.h, q);
-    if (!S) return 1 - beta;
-    const int i = 63 - hd_clz64(S);
+    const uint64_t S = act ? (RG(q) & km) : 0ull;
+    const int beta = act ? getbit(s.h, q) : 0;
+    const bool upd = S != 0ull;
+    const int i = upd ? 63 - hd_clz64(S) : 0;
     const uint64_t U = S & ~bit1(i);
     const int kk = k - 1;
 
-    // G (column form): rows in U get the pivot row, then row kk moves into slot i;
+    // G, column form: rows in U get the pivot row, row kk moves to slot i;
     // h gets the pivot row when beta = 1 (stabilizer.c:530-533, 557, 569-573)
-    uint64_t z = zrem;
-    while (z) {
-        const int c = hd_ffs64(z) - 1;
-        z &= z - 1;
-        uint64_t g = RG(c);
-        const uint64_t gi = (g >> i) & 1ull;
-        g ^= U & (0ull - gi);
-        const uint64_t gk = (g >> kk) & 1ull;
-        g = (g & ~bit1(i)) | (gk << i);
-        RG(c) = g;
-        if (beta) s.h ^= gi << c;
+    const uint64_t mi = bit1(i), mk = bit1(kk & 63);
+    const int nz = upd ? hd_popc64(zrem) : 0;
+    const int NZ = uniform_max(nz);
+    uint64_t z = zrem, hflip = 0ull;
+    for (int t = 0; t < NZ; t++) {
+        if (t < nz) {
+            const int c = hd_ffs64(z) - 1;
+            const uint64_t mc = z & (0ull - z);  // lowest remaining zero column, as a mask
+            z ^= mc;
+            uint64_t g = RG(c);
+            const uint64_t gi = 0ull - (uint64_t)((g & mi) != 0ull);
+            g ^= U & gi;
+            g = (g & ~mi) | (mi & (0ull - (uint64_t)((g & mk) != 0ull)));
+            RG(c) = g;
+            hflip |= mc & gi;
+        }
     }
+    if (beta) s.h ^= hflip;
 
-    // J: R = I + U e_i^T (rows, then columns), then the swap i <-> kk; gather the
-    // pivot's original column (D2 corrections) and the final column kk (beta term)
-    const uint64_t Ji = RJ(i);
-    uint64_t colI = 0ull, colK = 0ull;
-    for (int x = 0; x < k; x++) {
-        uint64_t r = RJ(x);
-        colI |= ((r >> i) & 1ull) << x;
-        r ^= Ji & (0ull - ((U >> x) & 1ull));
-        r ^= U & (0ull - ((r >> i) & 1ull));
-        // column swap i <-> kk, row x goes to slot dst; the pivot row lands in
-        // slot kk, which the shrink drops, so slot kk is never written (and is
-        // still unread when x = i comes first, i < kk)
-        const uint64_t tb = ((r >> i) ^ (r >> kk)) & 1ull;
-        r ^= (tb << i) | (tb << kk);
-        const int dst = (x == kk) ? i : ((x == i) ? kk : x);
-        colK |= ((r >> kk) & 1ull) << dst;
-        if (dst != kk) RJ(dst) = r;
+    // J: rank-two update, then the i <-> kk swap and drop of kk
+    const uint64_t Ji = upd ? RJ(i) : 0ull;
+    const uint64_t C = Ji ^ (getbit(Ji, i) ? U : 0ull);  // new row (and column) i
+    const uint64_t Jk = upd ? (RJ(kk) ^ (getbit(C, kk) ? U : 0ull)) : 0ull;  // new row kk (kk not in U)
+    // every row of the lane's block is rewritten (rows i and kk get values that are
+    // replaced or dropped just below), so the pass is branch-free; rows at or
+    // beyond k are outside the block and never read again
+    const int KX = uniform_max(upd ? k : 0);
+    if (upd) {
+        uint64_t cu = U, cc = C, cj = Jk;
+        for (int x = 0; x < KX; x++) {
+            uint64_t r = RJ(x);
+            r ^= Ji & (0ull - (cu & 1ull));
+            r ^= U & (0ull - (cc & 1ull));
+            r = (r & ~mi) | (mi & (0ull - (cj & 1ull)));
+            RJ(x) = r;
+            cu >>= 1;
+            cc >>= 1;
+            cj >>= 1;
+        }
     }
-    // D (eq. 49 + lower-triangle corrections), swap, beta term (updateQD)
-    const uint64_t Li = (colI & ~lowmask(i + 1)) | (Ji & lowmask(i));
-    tp_add_D(s, U, getbit(s.D1, i), getbit(s.D2, i));
-    s.D2 ^= U & Li;
-    if (i != kk) {
-        s.D1 = swapbits(s.D1, i, kk);
-        s.D2 = swapbits(s.D2, i, kk);
+    if (upd && i != kk) RJ(i) = (Jk & ~mi) | (mi & (0ull - ((Jk >> kk) & 1ull)));
+    if (upd) {
+        // D: eq. 49 and the lower-triangle parities (J[max][min] = Ji by symmetry)
+        tp_add_D(s, U, getbit(s.D1, i), getbit(s.D2, i));
+        s.D2 ^= U & Ji;
+        if (i != kk) {
+            s.D1 = swapbits(s.D1, i, kk);
+            s.D2 = swapbits(s.D2, i, kk);
+        }
+        s.D1 &= km;
+        s.D2 &= km;
+        if (beta) {
+            s.Q = (s.Q + tp_getD(s, kk)) % 8;
+            s.D2 ^= ((C & ~bit1(i)) | (((C >> kk) & 1ull) << i)) & lowmask(kk);
+        } else {
+            s.Q = s.Q % 8;
+        }
+        s.k = kk;
+        return 2;
     }
-    s.D1 &= km;
-    s.D2 &= km;
-    if (beta) {
-        s.Q = (s.Q + 2 * (2 * getbit(s.D2, kk) + getbit(s.D1, kk))) % 8;
-        s.D2 ^= colK;
-    } else {
-        s.Q = s.Q % 8;
-    }
-    s.k = kk;
-    return 2;
+    return act ? 1 - beta : 1;
 }
 
 // W0/W1 accumulators of Wsigma (stabilizer.c:258-297)
@@ -191,99 +225,112 @@ CSIM_HD inline void tp_factor_dimer(WAcc& w, int A, int B, int& err) {
     w.m += m;
 }
 
-CSIM_HD inline int tp_getD(const PairRegs& s, int i) {
-    return 2 * (2 * getbit(s.D2, i) + getbit(s.D1, i));
-}
-
-// exponentialSumExact (stabilizer.c:300-481) on the thread's pair
-CSIM_HD inline void tp_exp_sum(PairRegs& s, uint64_t* sJ, int st, int& eps, int& p, int& m, int& err) {
-    const int k = s.k;
+// exponentialSumExact (stabilizer.c:300-481), symmetric J; `act` as for tp_shrink.
+CSIM_HD inline void tp_exp_sum(PairRegs& s, uint64_t* sJ, int st, bool act, int& eps, int& p, int& m, int& err) {
+    const int k = act ? s.k : 0;
     const uint64_t km = lowmask(k);
-    if (k == 0) {  // Wsigma's k == 0 case
-        eps = 1; p = 0; m = s.Q;
-        return;
-    }
     const uint64_t Sm = s.D1 & km;
     int sidx = -1;
-    if (Sm) {
-        // R = I + U e_a^T, then swap a <-> k-1 (stabilizer.c:317-336)
-        const int a = hd_ffs64(Sm) - 1;
+    {
+        // R = I + U e_a^T, then swap a <-> kk (stabilizer.c:317-336); kk may lie in U
+        const bool upd = Sm != 0ull;
+        const int a = upd ? hd_ffs64(Sm) - 1 : 0;
         const uint64_t U = Sm & ~bit1(a);
         const int kk = k - 1;
-        const uint64_t Ja = RJ(a), Jk = RJ(kk);  // row a is stored into slot kk before x = kk is read
-        uint64_t colA = 0ull;
-        for (int x = 0; x < k; x++) {
-            uint64_t r = (x == kk) ? Jk : RJ(x);
-            colA |= ((r >> a) & 1ull) << x;
-            r ^= Ja & (0ull - ((U >> x) & 1ull));
-            r ^= U & (0ull - ((r >> a) & 1ull));
-            const uint64_t tb = ((r >> a) ^ (r >> kk)) & 1ull;
-            r ^= (tb << a) | (tb << kk);
-            const int dst = (x == kk) ? a : ((x == a) ? kk : x);
-            RJ(dst) = r;
+        const uint64_t Ja = upd ? RJ(a) : 0ull;
+        const uint64_t C = Ja ^ (getbit(Ja, a) ? U : 0ull);  // new row/column a
+        const uint64_t Jk = upd ? (RJ(kk) ^ (getbit(U, kk) ? Ja : 0ull) ^ (getbit(C, kk) ? U : 0ull)) : 0ull;
+        const int KX = uniform_max(upd ? k : 0);
+        if (upd) {
+            // rows a and kk are rewritten below; the pass itself is branch-free
+            const uint64_t ma = bit1(a), mk = bit1(kk & 63);
+            uint64_t cu = U, cc = C, cj = Jk;
+            for (int x = 0; x < KX; x++) {
+                uint64_t r = RJ(x);
+                r ^= Ja & (0ull - (cu & 1ull));
+                r ^= U & (0ull - (cc & 1ull));
+                // swap bits a and kk: bit a <- J'[x][kk] = bit x of Jk, bit kk <- J'[x][a] = bit x of C
+                r = (r & ~(ma | mk)) | (ma & (0ull - (cj & 1ull))) | (mk & (0ull - (cc & 1ull)));
+                RJ(x) = r;
+                cu >>= 1;
+                cc >>= 1;
+                cj >>= 1;
+            }
         }
-        const uint64_t La = (colA & ~lowmask(a + 1)) | (Ja & lowmask(a));
-        tp_add_D(s, U, getbit(s.D1, a), getbit(s.D2, a));
-        s.D2 ^= U & La;
-        s.D1 = swapbits(s.D1, a, kk) & km;
-        s.D2 = swapbits(s.D2, a, kk) & km;
-        sidx = kk;
+        if (upd && a != kk) {
+            RJ(a) = swapbits(Jk, a, kk);
+            RJ(kk) = swapbits(C, a, kk);
+        } else if (upd) {
+            RJ(a) = C;
+        }
+        if (upd) {
+            tp_add_D(s, U, getbit(s.D1, a), getbit(s.D2, a));
+            s.D2 ^= U & Ja;
+            s.D1 = swapbits(s.D1, a, kk) & km;
+            s.D2 = swapbits(s.D2, a, kk) & km;
+            sidx = kk;
+        }
     }
     uint64_t E = km & ~(sidx >= 0 ? bit1(sidx) : 0ull);
     WAcc w0 = {0, 0, 0}, w1 = {0, 0, 0};
-    bool any = false;
-    while (E) {
-        const int a = hd_ffs64(E) - 1;
-        const uint64_t ra = RJ(a);
+    const bool any = E != 0ull;
+    const int NE = uniform_max(hd_popc64(E));
+    for (int it = 0; it < NE; it++) {
+        const bool live = E != 0ull;
+        const int a = live ? hd_ffs64(E) - 1 : 0;
+        const uint64_t ra = live ? RJ(a) : 0ull;
         const uint64_t K = ra & E & ~bit1(a);
-        any = true;
-        if (!K) {  // monomer {a}: row a is final
-            E &= ~bit1(a);
+        const bool dimer = K != 0ull;
+        const int b = dimer ? hd_ffs64(K) - 1 : 0;
+        const uint64_t rb = dimer ? RJ(b) : 0ull;
+        if (live && !dimer) {  // monomer {a}: row a is final
             const int Da = tp_getD(s, a);
             tp_factor_mono(w0, Da, err);
             if (sidx >= 0) tp_factor_mono(w1, Da + 4 * getbit(ra, sidx), err);
-            continue;
         }
-        const int b = hd_ffs64(K) - 1;
-        const uint64_t rb = RJ(b);
-        const uint64_t Ep = E & ~bit1(a) & ~bit1(b);
-        const uint64_t vb = ra & Ep, va = rb & Ep;
-        // dimer {a, b}: rows a and b are final now (D, and their bit sidx)
-        {
+        if (dimer) {  // dimer {a, b}: rows a and b are final
             const int Da = tp_getD(s, a), Db = tp_getD(s, b);
             tp_factor_dimer(w0, Da, Db, err);
             if (sidx >= 0) tp_factor_dimer(w1, Da + 4 * getbit(ra, sidx), Db + 4 * getbit(rb, sidx), err);
         }
-        if (vb | va) {
-            // R = I + vb e_b^T + va e_a^T on the rows still in play (Ep); the other
-            // rows of R are the identity, so their J rows and D entries stay put
-            // except for columns a, b, which nothing reads again.
-            uint64_t colA = 0ull, colB = 0ull;
-            uint64_t z = Ep;
-            while (z) {
-                const int x = hd_ffs64(z) - 1;
-                z &= z - 1;
+        const uint64_t Ep = dimer ? (E & ~bit1(a) & ~bit1(b)) : (E & ~bit1(a));
+        const uint64_t vb = dimer ? (ra & Ep) : 0ull, va = dimer ? (rb & Ep) : 0ull;
+        const bool upd = (vb | va) != 0ull;
+        // R = I + vb e_b^T + va e_a^T on the rows still in play (Ep):
+        //   row x += vb_x Jb + va_x Ja + Cb_x vb + Ca_x va, with the coefficient
+        //   columns Cb = (RJ)[.][b], Ca = (RJ)[.][a] (symmetric J)
+        const int jaa = getbit(ra, a), jbb = getbit(rb, b), jab = getbit(ra, b);
+        const uint64_t Cb = rb ^ (jbb ? vb : 0ull) ^ (jab ? va : 0ull);
+        const uint64_t Ca = ra ^ (jab ? vb : 0ull) ^ (jaa ? va : 0ull);
+        const int np = upd ? hd_popc64(Ep) : 0;
+        const int NP = uniform_max(np);
+        uint64_t zz = Ep;
+        for (int t = 0; t < NP; t++) {
+            if (t < np) {
+                const int x = hd_ffs64(zz) - 1;
+                zz &= zz - 1;
                 uint64_t r = RJ(x);
-                colA |= ((r >> a) & 1ull) << x;
-                colB |= ((r >> b) & 1ull) << x;
                 r ^= rb & (0ull - ((vb >> x) & 1ull));
                 r ^= ra & (0ull - ((va >> x) & 1ull));
-                const uint64_t bb = (r >> b) & 1ull, ba = (r >> a) & 1ull;
-                r ^= vb & (0ull - bb);
-                r ^= va & (0ull - ba);
+                r ^= vb & (0ull - ((Cb >> x) & 1ull));
+                r ^= va & (0ull - ((Ca >> x) & 1ull));
                 RJ(x) = r;
             }
+        }
+        if (upd) {
             const int db1 = getbit(s.D1, b), db2 = getbit(s.D2, b), da1 = getbit(s.D1, a), da2 = getbit(s.D2, a);
             tp_add_D(s, vb, db1, db2);
             tp_add_D(s, va, da1, da2);
-            const uint64_t Lb = (colB & ~lowmask(b + 1)) | (rb & lowmask(b));
-            const uint64_t La = (colA & ~lowmask(a + 1)) | (ra & lowmask(a));
-            uint64_t flip = (vb & Lb) ^ (va & La);
-            const int jab = (b > a) ? getbit(rb, a) : getbit(ra, b);
+            uint64_t flip = (vb & rb) ^ (va & ra);
             if (jab) flip ^= vb & va;
             s.D2 ^= flip;
         }
-        E = Ep;
+        if (live) E = Ep;
+    }
+    if (!act) return;
+    if (k == 0) {  // Wsigma's k == 0 case
+        eps = 1; p = 0; m = s.Q;
+        return;
     }
     // W0 = Wsigma(sigma = 0), W1 = Wsigma(sigma = 1) (stabilizer.c:425-479)
     const int tM0 = s.Q, tM1 = s.Q + (sidx >= 0 ? tp_getD(s, sidx) : 0);
@@ -316,8 +363,6 @@ CSIM_HD inline void tp_exp_sum(PairRegs& s, uint64_t* sJ, int st, int& eps, int&
     }
 }
 
-
-
 // Adds eps 2^{p/2} w^m, scaled by 2^{P/2}, to z = z0 + z1 w + z2 w^2 + z3 w^3
 // (w = e^{i pi/4}, sqrt 2 = w - w^3).  With P = 2n every term of a pair's
 // p in [-2n, n] is an integer below 2^96, exact in 128 bits.
@@ -340,9 +385,10 @@ CSIM_HD inline void zacc(__int128 (&z)[4], int eps, int p, int m, int P, int& er
     }
 }
 
-// One pair: theta's pristine rows in (J, GT-columns-as-row-masks), codeword x.
-// The caller provides working memory sJ/sGT (stride st) of n indices each.
-CSIM_HD inline void pair_l(int n, int k1, int Q, uint64_t h, uint64_t D1, uint64_t D2, const uint64_t* pJ,
+// One pair: theta's pristine J rows and G columns (as row masks), codeword x;
+// working memory sJ/sGT (stride st), n indices each.  J must be symmetric.
+// `valid` = this lane has a pair (all lanes of a warp call together).
+CSIM_HD inline void pair_l(bool valid, int n, int k1, int Q, uint64_t h, uint64_t D1, uint64_t D2, const uint64_t* pJ,
                            const uint64_t* pGT, uint64_t x, uint64_t* sJ, uint64_t* sGT, int st, int& eps, int& p,
                            int& m, int& err) {
     PairRegs s;
@@ -351,8 +397,9 @@ CSIM_HD inline void pair_l(int n, int k1, int Q, uint64_t h, uint64_t D1, uint64
     s.h = h;
     s.D1 = D1;
     s.D2 = D2;
-    for (int r = 0; r < k1; r++) RJ(r) = pJ[r];
-    uint64_t zeros = ~x & lowmask(n);
+    if (valid)
+        for (int r = 0; r < k1; r++) RJ(r) = pJ[r];
+    uint64_t zeros = valid ? (~x & lowmask(n)) : 0ull;
     for (uint64_t zz = zeros; zz; zz &= zz - 1) {
         const int c = hd_ffs64(zz) - 1;
         RG(c) = pGT[c];
@@ -360,18 +407,22 @@ CSIM_HD inline void pair_l(int n, int k1, int Q, uint64_t h, uint64_t D1, uint64
     eps = 0;
     p = 0;
     m = 0;
-    while (zeros) {
-        const int q = 63 - hd_clz64(zeros);
-        zeros &= ~bit1(q);
-        eps = tp_shrink(s, sJ, sGT, st, q, zeros);
-        if (eps == 0) {
-            p = 0;
-            m = 0;
-            return;
-        }
+    bool alive = valid;
+    const int NZ = uniform_max(hd_popc64(zeros));
+    for (int it = 0; it < NZ; it++) {
+        const bool act = alive && zeros != 0ull;
+        const int q = act ? 63 - hd_clz64(zeros) : 0;
+        if (act) zeros &= ~bit1(q);
+        const int r = tp_shrink(s, sJ, sGT, st, q, zeros, act);
+        if (act && r == 0) alive = false;
     }
-    tp_exp_sum(s, sJ, st, eps, p, m, err);
-    p -= k1 + hd_popc64(x);
+    tp_exp_sum(s, sJ, st, alive, eps, p, m, err);
+    if (alive) p -= k1 + hd_popc64(x);
+    else {
+        eps = 0;
+        p = 0;
+        m = 0;
+    }
 }
 
 #undef RJ

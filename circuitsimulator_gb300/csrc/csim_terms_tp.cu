@@ -35,8 +35,15 @@ struct TPShared {
     uint64_t pGT[64];
     uint64_t h, D1, D2;
     int n, k, Q, live;
-    __int128 red[kTP][4];
+    __int128 red[kTP / 32][4];
 };
+
+__device__ __forceinline__ __int128 shfl_xor_i128(__int128 v, int m) {
+    uint64_t lo = (uint64_t)v, hi = (uint64_t)((unsigned __int128)v >> 64);
+    lo = ((uint64_t)__shfl_xor_sync(kFull, (uint32_t)(lo >> 32), m) << 32) | __shfl_xor_sync(kFull, (uint32_t)lo, m);
+    hi = ((uint64_t)__shfl_xor_sync(kFull, (uint32_t)(hi >> 32), m) << 32) | __shfl_xor_sync(kFull, (uint32_t)hi, m);
+    return (__int128)(((unsigned __int128)hi << 64) | lo);
+}
 
 // Work item = (theta a, block of kTP * per_thread consecutive terms).  Thread t
 // takes terms jb + t + kTP * r, r < per_thread.  Partial sums: 4 int128 per item.
@@ -74,20 +81,28 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
             sh.pGT[tid] = col;
         }
         __syncthreads();
+        // the pair routine relies on a symmetric J (true of every state drawn
+        // and projected by this library); anything else is refused
+        bool asym = false;
+        if (tid < sh.k)
+            for (int r = 0; r < sh.k; r++) asym |= ((sh.pJ[tid] >> r) & 1ull) != ((sh.pJ[r] >> tid) & 1ull);
+        asym = __syncthreads_or(asym) != 0;
         __int128 z[4] = {0, 0, 0, 0};
         const int n = sh.n;
-        if (n > nmax) e |= kErrArg;
-        if (sh.live && n >= 1 && n <= nmax) {
+        if (n > nmax || asym) e |= kErrArg;
+        if (sh.live && !asym && n >= 1 && n <= nmax) {
             uint64_t* sJ = reinterpret_cast<uint64_t*>(smem_raw + sizeof(TPShared));
             uint64_t* sGT = sJ + (size_t)nmax * kTP;
             const int64_t jb = j0 + cb * span;
             for (int r = 0; r < per_thread; r++) {
                 const int64_t j = jb + tid + (int64_t)kTP * r;
-                if (j >= j0 + nj) break;
-                const uint64_t x = codewords[j - j0];
+                const bool valid = j < j0 + nj;
+                if (__all_sync(kFull, !valid)) break;  // warp-uniform exit
+                const uint64_t x = valid ? codewords[j - j0] : 0ull;
                 int eps, pp, mm;
-                pc::pair_l(n, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ, sh.pGT, x, sJ + tid, sGT + tid, kTP, eps, pp,
-                           mm, e);
+                pc::pair_l(valid, n, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ, sh.pGT, x, sJ + tid, sGT + tid, kTP,
+                           eps, pp, mm, e);
+                if (!valid) continue;
                 pc::zacc(z, eps, pp, mm, P, e);
                 if (eps_o) {
                     const int64_t w = a * nj + (j - j0);
@@ -97,12 +112,15 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
                 }
             }
         }
-        if (part) {
-            for (int q = 0; q < 4; q++) sh.red[tid][q] = z[q];
+        if (part) {  // warp sums by shuffles, then the block's warps
+            for (int q = 0; q < 4; q++)
+                for (int o = 16; o > 0; o >>= 1) z[q] += shfl_xor_i128(z[q], o);
+            if ((tid & 31) == 0)
+                for (int q = 0; q < 4; q++) sh.red[tid >> 5][q] = z[q];
             __syncthreads();
             if (tid < 4) {
                 __int128 acc = 0;
-                for (int t = 0; t < kTP; t++) acc += sh.red[t][tid];
+                for (int w = 0; w < kTP / 32; w++) acc += sh.red[w][tid];
                 part[4 * item + tid] = acc;
             }
         }

@@ -20,7 +20,7 @@ extern "C" int tp_host_pairs(const csim_state* theta, int ntheta, const uint64_t
         }
         for (int j = 0; j < nx; j++) {
             const int w = a * nx + j;
-            csim::pc::pair_l(th.n, th.k, th.Q, th.h, th.D1, th.D2, th.J, pGT, xs[j], wJ, wG, 1, eps[w], p[w], m[w],
+            csim::pc::pair_l(true, th.n, th.k, th.Q, th.h, th.D1, th.D2, th.J, pGT, xs[j], wJ, wG, 1, eps[w], p[w], m[w],
                              err);
         }
     }
