@@ -77,6 +77,7 @@ def load_library(path=LIB_PATH):
         "csim_launch_count": ([vp], i64),
         "csim_last_stats": ([vp, vp], C.c_int),
         "csim_set_option": ([vp, i32, i64], C.c_int),
+        "csim_rng_position": ([vp, u64, u64], C.c_int),
         "csim_inner_product_exact": ([vp, i64, vp, vp, vp, vp, vp], C.c_int),
         "csim_exponential_sum_exact": ([vp, i64, vp, vp, vp, vp], C.c_int),
         "csim_shrink": ([vp, i64, vp, vp, vp, i32, vp], C.c_int),
@@ -183,6 +184,10 @@ class Backend:
     def set_option(self, option, value):
         """CSIM_OPT_PAIR_KERNEL = 1 (0 thread-per-pair, 1 warp-per-pair), CSIM_OPT_PER_THREAD = 2."""
         self._check(self.lib.csim_set_option(self.ctx, int(option), int(value)))
+
+    def rng_position(self, seed, first):
+        """Next CSIM_RNG_PHILOX draw (with SEED_CONTINUE) is state `first` of stream `seed`."""
+        self._check(self.lib.csim_rng_position(self.ctx, int(seed), int(first)))
 
     def last_stats(self):
         st = Stats()

@@ -363,6 +363,13 @@ extern "C" int csim_set_option(csim_ctx* ctx, int32_t option, int64_t value) {
     }
 }
 
+extern "C" int csim_rng_position(csim_ctx* ctx, uint64_t seed, uint64_t first) {
+    if (!ctx) return CSIM_ERR_ARG;
+    ctx->philox_seed = seed;
+    ctx->philox_next = first;
+    return CSIM_OK;
+}
+
 extern "C" int csim_last_stats(const csim_ctx* ctx, csim_stats* out) {
     if (!ctx || !out) return CSIM_ERR_ARG;
     *out = ctx->stats;

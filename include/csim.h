@@ -111,6 +111,12 @@ typedef struct csim_stats {
 } csim_stats;
 int csim_last_stats(const csim_ctx *ctx, csim_stats *out);
 
+/* Positions the context's counter-based generator: the next state drawn with
+ * CSIM_RNG_PHILOX and seed CSIM_SEED_CONTINUE is state `first` of stream
+ * `seed`.  Lets ranks draw disjoint blocks of one stream (the reference's
+ * MPI split of samples, libcirc/innerprod.c:64-83, without changing the draws). */
+int csim_rng_position(csim_ctx *ctx, uint64_t seed, uint64_t first);
+
 /* Tuning options (no counterpart in the reference). */
 #define CSIM_OPT_PAIR_KERNEL 1 /* |L>-term pairs: 0 = one thread per pair (default), 1 = one warp per pair */
 #define CSIM_OPT_PER_THREAD 2  /* |L>-term pairs per thread per work item of the thread-per-pair kernel (1..64) */

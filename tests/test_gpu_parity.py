@@ -341,3 +341,19 @@ def test_pair_kernels_agree(gpu, t, k):
     for x, y in zip(a, b):
         assert (x == y).all()
     assert (va == vb).all()
+
+
+def test_philox_blocks_compose(gpu):
+    """State i of a counter-based stream is the same whoever draws it: two
+    blocks drawn separately (as two ranks would) equal one draw of both."""
+    rs = np.random.RandomState(9)
+    t, k = 24, 8
+    L = [rand_word(rs, t) for _ in range(k)]
+    rows = random_projector_rows(rs, t, 5)
+    P = backend.projector(rows[0], rows[1], rows[2], t)
+    whole = gpu.singleProjectorSample(P, L, False, 50, backend.RNG_PHILOX, 123)
+    parts = []
+    for lo, hi in ((0, 21), (21, 50)):
+        gpu.rng_position(123, lo)
+        parts.append(gpu.singleProjectorSample(P, L, False, hi - lo, backend.RNG_PHILOX, backend.SEED_CONTINUE))
+    assert (np.concatenate(parts) == whole).all()
