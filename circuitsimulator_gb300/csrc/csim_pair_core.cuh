@@ -89,12 +89,75 @@ CSIM_HD inline void gamma_ab(int A, int B, int& e, int& p, int& m, int& err) {
     else err |= kErrGamma;
 }
 
-#define RJ(r) sJ[(size_t)(r) * st]
+// J rows are stored in pairs: rows 2p and 2p+1 are adjacent 64-bit slots, so
+// one 16-byte access moves both; pair p of a lane is 2*st slots after pair
+// p-1.  G columns are single slots st apart.  While every row-space index
+// of a pair is below 32 (k <= 32) the arithmetic runs on 32-bit words W
+// and only the low halves of the slots are read (the high halves are left
+// as they are and never read again).
+#define RJ(r) sJ[(size_t)((r) >> 1) * 2 * st + ((r) & 1)]
 #define RG(c) sGT[(size_t)(c) * st]
+
+struct alignas(16) U64x2 {
+    uint64_t a, b;
+};
+
+template <class W>
+struct WordTraits;
+template <>
+struct WordTraits<uint64_t> {
+    static constexpr int bits = 64;
+    CSIM_HD static int popc(uint64_t x) { return hd_popc64(x); }
+    CSIM_HD static int ffs(uint64_t x) { return hd_ffs64(x); }
+    CSIM_HD static int clz(uint64_t x) { return hd_clz64(x); }
+};
+template <>
+struct WordTraits<uint32_t> {
+    static constexpr int bits = 32;
+    CSIM_HD static int popc(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+        return __popc(x);
+#else
+        return __builtin_popcount(x);
+#endif
+    }
+    CSIM_HD static int ffs(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+        return __ffs((int)x);
+#else
+        return __builtin_ffs((int)x);
+#endif
+    }
+    CSIM_HD static int clz(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+        return __clz((int)x);
+#else
+        return x ? __builtin_clz(x) : 32;
+#endif
+    }
+};
+
+template <class W>
+CSIM_HD inline W wbit(int i) {
+    return (W)1 << i;
+}
+template <class W>
+CSIM_HD inline W wlow(int k) {
+    return k >= WordTraits<W>::bits ? (W)~(W)0 : (W)(((W)1 << k) - (W)1);
+}
+template <class W>
+CSIM_HD inline int wget(W w, int i) {
+    return (int)((w >> i) & (W)1);
+}
+template <class W>
+CSIM_HD inline W wmask(bool b) {  // all ones if b
+    return (W)0 - (W)(b ? 1 : 0);
+}
 
 struct PairRegs {
     int k, Q;
-    uint64_t h, D1, D2;
+    uint64_t h;       // position space (n bits)
+    uint64_t D1, D2;  // row space (k bits)
 };
 
 // Warp-uniform loop bounds: on the device every lane of the warp runs the
@@ -118,6 +181,14 @@ CSIM_HD inline void tp_add_D(PairRegs& s, uint64_t u, int d1, int d2) {
 
 CSIM_HD inline int tp_getD(const PairRegs& s, int i) { return 2 * (2 * getbit(s.D2, i) + getbit(s.D1, i)); }
 
+// one row of the shrink's rank-two update + bit move (see tp_shrink)
+template <class W>
+CSIM_HD inline W shrink_row(W r, W Ji, W U, W mi, W bu, W bc, W bj) {
+    r ^= Ji & bu;
+    r ^= U & bc;
+    return (r & ~mi) | (mi & bj);
+}
+
 // Shrink by e_q (alpha = 0), stabilizer.c:500-585, for a symmetric J.
 // `act`: this lane has a shrink to do.  Returns 0 EMPTY, 1 SAME, 2 SUCCESS
 // (1 when inactive).  All lanes must call it together.
@@ -129,19 +200,21 @@ CSIM_HD inline int tp_getD(const PairRegs& s, int i) { return 2 * (2 * getbit(s.
 // i and every row's bit i becomes its old bit kk = bit x of row kk.  The +4
 // corrections of updateDJ are U & Ji, and updateQD's J.y is column kk of the
 // result, i.e. C with bit i taken from bit kk of C.
+template <class W>
 CSIM_HD inline int tp_shrink(PairRegs& s, uint64_t* sJ, uint64_t* sGT, int st, int q, uint64_t zrem, bool act) {
+    using T = WordTraits<W>;
     const int k = s.k;
-    const uint64_t km = lowmask(k);
-    const uint64_t S = act ? (RG(q) & km) : 0ull;
+    const W km = wlow<W>(k);
+    const W S = act ? ((W)RG(q) & km) : (W)0;
     const int beta = act ? getbit(s.h, q) : 0;
-    const bool upd = S != 0ull;
-    const int i = upd ? 63 - hd_clz64(S) : 0;
-    const uint64_t U = S & ~bit1(i);
+    const bool upd = S != (W)0;
+    const int i = upd ? T::bits - 1 - T::clz(S) : 0;
+    const W U = S & ~wbit<W>(i);
     const int kk = k - 1;
+    const W mi = wbit<W>(i), mk = wbit<W>(kk & (T::bits - 1));
 
     // G, column form: rows in U get the pivot row, row kk moves to slot i;
     // h gets the pivot row when beta = 1 (stabilizer.c:530-533, 557, 569-573)
-    const uint64_t mi = bit1(i), mk = bit1(kk & 63);
     const int nz = upd ? hd_popc64(zrem) : 0;
     const int NZ = uniform_max(nz);
     uint64_t z = zrem, hflip = 0ull;
@@ -150,51 +223,56 @@ CSIM_HD inline int tp_shrink(PairRegs& s, uint64_t* sJ, uint64_t* sGT, int st, i
             const int c = hd_ffs64(z) - 1;
             const uint64_t mc = z & (0ull - z);  // lowest remaining zero column, as a mask
             z ^= mc;
-            uint64_t g = RG(c);
-            const uint64_t gi = 0ull - (uint64_t)((g & mi) != 0ull);
-            g ^= U & gi;
-            g = (g & ~mi) | (mi & (0ull - (uint64_t)((g & mk) != 0ull)));
-            RG(c) = g;
-            hflip |= mc & gi;
+            W g = (W)RG(c);
+            const bool gi = (g & mi) != (W)0;
+            g ^= U & wmask<W>(gi);
+            g = (g & ~mi) | (mi & wmask<W>((g & mk) != (W)0));
+            RG(c) = (uint64_t)g;
+            if (gi) hflip |= mc;
         }
     }
     if (beta) s.h ^= hflip;
 
     // J: rank-two update, then the i <-> kk swap and drop of kk
-    const uint64_t Ji = upd ? RJ(i) : 0ull;
-    const uint64_t C = Ji ^ (getbit(Ji, i) ? U : 0ull);  // new row (and column) i
-    const uint64_t Jk = upd ? (RJ(kk) ^ (getbit(C, kk) ? U : 0ull)) : 0ull;  // new row kk (kk not in U)
+    const W Ji = upd ? (W)RJ(i) : (W)0;
+    const W C = Ji ^ (wget<W>(Ji, i) ? U : (W)0);  // new row (and column) i
+    const W Jk = upd ? (W)((W)RJ(kk) ^ (wget<W>(C, kk) ? U : (W)0)) : (W)0;  // new row kk (kk not in U)
     // every row of the lane's block is rewritten (rows i and kk get values that are
     // replaced or dropped just below), so the pass is branch-free; rows at or
     // beyond k are outside the block and never read again
     const int KX = uniform_max(upd ? k : 0);
     if (upd) {
-        uint64_t cu = U, cc = C, cj = Jk;
-        for (int x = 0; x < KX; x++) {
-            uint64_t r = RJ(x);
-            r ^= Ji & (0ull - (cu & 1ull));
-            r ^= U & (0ull - (cc & 1ull));
-            r = (r & ~mi) | (mi & (0ull - (cj & 1ull)));
-            RJ(x) = r;
-            cu >>= 1;
-            cc >>= 1;
-            cj >>= 1;
+        // two rows per 16-byte access (the pair buffer holds an even number of rows)
+        W cu = U, cc = C, cj = Jk;
+#if defined(__CUDA_ARCH__)
+#pragma unroll 2
+#endif
+        for (int x = 0; x < KX; x += 2) {
+            U64x2* pr = reinterpret_cast<U64x2*>(&RJ(x));
+            U64x2 v = *pr;
+            v.a = (uint64_t)shrink_row<W>((W)v.a, Ji, U, mi, wmask<W>(cu & 1), wmask<W>(cc & 1), wmask<W>(cj & 1));
+            v.b = (uint64_t)shrink_row<W>((W)v.b, Ji, U, mi, wmask<W>((cu >> 1) & 1), wmask<W>((cc >> 1) & 1),
+                                          wmask<W>((cj >> 1) & 1));
+            *pr = v;
+            cu >>= 2;
+            cc >>= 2;
+            cj >>= 2;
         }
     }
-    if (upd && i != kk) RJ(i) = (Jk & ~mi) | (mi & (0ull - ((Jk >> kk) & 1ull)));
+    if (upd && i != kk) RJ(i) = (uint64_t)((Jk & ~mi) | (mi & wmask<W>(wget<W>(Jk, kk))));
     if (upd) {
         // D: eq. 49 and the lower-triangle parities (J[max][min] = Ji by symmetry)
-        tp_add_D(s, U, getbit(s.D1, i), getbit(s.D2, i));
-        s.D2 ^= U & Ji;
+        tp_add_D(s, (uint64_t)U, getbit(s.D1, i), getbit(s.D2, i));
+        s.D2 ^= (uint64_t)(U & Ji);
         if (i != kk) {
             s.D1 = swapbits(s.D1, i, kk);
             s.D2 = swapbits(s.D2, i, kk);
         }
-        s.D1 &= km;
-        s.D2 &= km;
+        s.D1 &= lowmask(k);
+        s.D2 &= lowmask(k);
         if (beta) {
             s.Q = (s.Q + tp_getD(s, kk)) % 8;
-            s.D2 ^= ((C & ~bit1(i)) | (((C >> kk) & 1ull) << i)) & lowmask(kk);
+            s.D2 ^= (uint64_t)(((C & ~mi) | (mi & wmask<W>(wget<W>(C, kk)))) & wlow<W>(kk));
         } else {
             s.Q = s.Q % 8;
         }
@@ -226,104 +304,106 @@ CSIM_HD inline void tp_factor_dimer(WAcc& w, int A, int B, int& err) {
 }
 
 // exponentialSumExact (stabilizer.c:300-481), symmetric J; `act` as for tp_shrink.
+template <class W>
 CSIM_HD inline void tp_exp_sum(PairRegs& s, uint64_t* sJ, int st, bool act, int& eps, int& p, int& m, int& err) {
+    using T = WordTraits<W>;
     const int k = act ? s.k : 0;
-    const uint64_t km = lowmask(k);
-    const uint64_t Sm = s.D1 & km;
+    const W km = wlow<W>(k);
+    const W Sm = (W)s.D1 & km;
     int sidx = -1;
     {
         // R = I + U e_a^T, then swap a <-> kk (stabilizer.c:317-336); kk may lie in U
-        const bool upd = Sm != 0ull;
-        const int a = upd ? hd_ffs64(Sm) - 1 : 0;
-        const uint64_t U = Sm & ~bit1(a);
+        const bool upd = Sm != (W)0;
+        const int a = upd ? T::ffs(Sm) - 1 : 0;
+        const W U = Sm & ~wbit<W>(a);
         const int kk = k - 1;
-        const uint64_t Ja = upd ? RJ(a) : 0ull;
-        const uint64_t C = Ja ^ (getbit(Ja, a) ? U : 0ull);  // new row/column a
-        const uint64_t Jk = upd ? (RJ(kk) ^ (getbit(U, kk) ? Ja : 0ull) ^ (getbit(C, kk) ? U : 0ull)) : 0ull;
+        const W Ja = upd ? (W)RJ(a) : (W)0;
+        const W C = Ja ^ (wget<W>(Ja, a) ? U : (W)0);  // new row/column a
+        const W Jk = upd ? (W)((W)RJ(kk) ^ (wget<W>(U, kk) ? Ja : (W)0) ^ (wget<W>(C, kk) ? U : (W)0)) : (W)0;
         const int KX = uniform_max(upd ? k : 0);
         if (upd) {
             // rows a and kk are rewritten below; the pass itself is branch-free
-            const uint64_t ma = bit1(a), mk = bit1(kk & 63);
-            uint64_t cu = U, cc = C, cj = Jk;
+            const W ma = wbit<W>(a), mk = wbit<W>(kk & (T::bits - 1));
+            W cu = U, cc = C, cj = Jk;
             for (int x = 0; x < KX; x++) {
-                uint64_t r = RJ(x);
-                r ^= Ja & (0ull - (cu & 1ull));
-                r ^= U & (0ull - (cc & 1ull));
+                W r = (W)RJ(x);
+                r ^= Ja & wmask<W>(cu & 1);
+                r ^= U & wmask<W>(cc & 1);
                 // swap bits a and kk: bit a <- J'[x][kk] = bit x of Jk, bit kk <- J'[x][a] = bit x of C
-                r = (r & ~(ma | mk)) | (ma & (0ull - (cj & 1ull))) | (mk & (0ull - (cc & 1ull)));
-                RJ(x) = r;
+                r = (r & ~(ma | mk)) | (ma & wmask<W>(cj & 1)) | (mk & wmask<W>(cc & 1));
+                RJ(x) = (uint64_t)r;
                 cu >>= 1;
                 cc >>= 1;
                 cj >>= 1;
             }
         }
         if (upd && a != kk) {
-            RJ(a) = swapbits(Jk, a, kk);
-            RJ(kk) = swapbits(C, a, kk);
+            RJ(a) = (uint64_t)(W)swapbits((uint64_t)Jk, a, kk);
+            RJ(kk) = (uint64_t)(W)swapbits((uint64_t)C, a, kk);
         } else if (upd) {
-            RJ(a) = C;
+            RJ(a) = (uint64_t)C;
         }
         if (upd) {
-            tp_add_D(s, U, getbit(s.D1, a), getbit(s.D2, a));
-            s.D2 ^= U & Ja;
-            s.D1 = swapbits(s.D1, a, kk) & km;
-            s.D2 = swapbits(s.D2, a, kk) & km;
+            tp_add_D(s, (uint64_t)U, getbit(s.D1, a), getbit(s.D2, a));
+            s.D2 ^= (uint64_t)(U & Ja);
+            s.D1 = swapbits(s.D1, a, kk) & lowmask(k);
+            s.D2 = swapbits(s.D2, a, kk) & lowmask(k);
             sidx = kk;
         }
     }
-    uint64_t E = km & ~(sidx >= 0 ? bit1(sidx) : 0ull);
+    W E = km & ~(sidx >= 0 ? wbit<W>(sidx) : (W)0);
     WAcc w0 = {0, 0, 0}, w1 = {0, 0, 0};
-    const bool any = E != 0ull;
-    const int NE = uniform_max(hd_popc64(E));
+    const bool any = E != (W)0;
+    const int NE = uniform_max(T::popc(E));
     for (int it = 0; it < NE; it++) {
-        const bool live = E != 0ull;
-        const int a = live ? hd_ffs64(E) - 1 : 0;
-        const uint64_t ra = live ? RJ(a) : 0ull;
-        const uint64_t K = ra & E & ~bit1(a);
-        const bool dimer = K != 0ull;
-        const int b = dimer ? hd_ffs64(K) - 1 : 0;
-        const uint64_t rb = dimer ? RJ(b) : 0ull;
+        const bool live = E != (W)0;
+        const int a = live ? T::ffs(E) - 1 : 0;
+        const W ra = live ? (W)RJ(a) : (W)0;
+        const W K = ra & E & ~wbit<W>(a);
+        const bool dimer = K != (W)0;
+        const int b = dimer ? T::ffs(K) - 1 : 0;
+        const W rb = dimer ? (W)RJ(b) : (W)0;
         if (live && !dimer) {  // monomer {a}: row a is final
             const int Da = tp_getD(s, a);
             tp_factor_mono(w0, Da, err);
-            if (sidx >= 0) tp_factor_mono(w1, Da + 4 * getbit(ra, sidx), err);
+            if (sidx >= 0) tp_factor_mono(w1, Da + 4 * wget<W>(ra, sidx), err);
         }
         if (dimer) {  // dimer {a, b}: rows a and b are final
             const int Da = tp_getD(s, a), Db = tp_getD(s, b);
             tp_factor_dimer(w0, Da, Db, err);
-            if (sidx >= 0) tp_factor_dimer(w1, Da + 4 * getbit(ra, sidx), Db + 4 * getbit(rb, sidx), err);
+            if (sidx >= 0) tp_factor_dimer(w1, Da + 4 * wget<W>(ra, sidx), Db + 4 * wget<W>(rb, sidx), err);
         }
-        const uint64_t Ep = dimer ? (E & ~bit1(a) & ~bit1(b)) : (E & ~bit1(a));
-        const uint64_t vb = dimer ? (ra & Ep) : 0ull, va = dimer ? (rb & Ep) : 0ull;
-        const bool upd = (vb | va) != 0ull;
+        const W Ep = dimer ? (E & ~wbit<W>(a) & ~wbit<W>(b)) : (E & ~wbit<W>(a));
+        const W vb = dimer ? (ra & Ep) : (W)0, va = dimer ? (rb & Ep) : (W)0;
+        const bool upd = (vb | va) != (W)0;
         // R = I + vb e_b^T + va e_a^T on the rows still in play (Ep):
         //   row x += vb_x Jb + va_x Ja + Cb_x vb + Ca_x va, with the coefficient
         //   columns Cb = (RJ)[.][b], Ca = (RJ)[.][a] (symmetric J)
-        const int jaa = getbit(ra, a), jbb = getbit(rb, b), jab = getbit(ra, b);
-        const uint64_t Cb = rb ^ (jbb ? vb : 0ull) ^ (jab ? va : 0ull);
-        const uint64_t Ca = ra ^ (jab ? vb : 0ull) ^ (jaa ? va : 0ull);
-        const int np = upd ? hd_popc64(Ep) : 0;
+        const int jaa = wget<W>(ra, a), jbb = wget<W>(rb, b), jab = wget<W>(ra, b);
+        const W Cb = rb ^ (jbb ? vb : (W)0) ^ (jab ? va : (W)0);
+        const W Ca = ra ^ (jab ? vb : (W)0) ^ (jaa ? va : (W)0);
+        const int np = upd ? T::popc(Ep) : 0;
         const int NP = uniform_max(np);
-        uint64_t zz = Ep;
+        W zz = Ep;
         for (int t = 0; t < NP; t++) {
             if (t < np) {
-                const int x = hd_ffs64(zz) - 1;
+                const int x = T::ffs(zz) - 1;
                 zz &= zz - 1;
-                uint64_t r = RJ(x);
-                r ^= rb & (0ull - ((vb >> x) & 1ull));
-                r ^= ra & (0ull - ((va >> x) & 1ull));
-                r ^= vb & (0ull - ((Cb >> x) & 1ull));
-                r ^= va & (0ull - ((Ca >> x) & 1ull));
-                RJ(x) = r;
+                W r = (W)RJ(x);
+                r ^= rb & wmask<W>(wget<W>(vb, x));
+                r ^= ra & wmask<W>(wget<W>(va, x));
+                r ^= vb & wmask<W>(wget<W>(Cb, x));
+                r ^= va & wmask<W>(wget<W>(Ca, x));
+                RJ(x) = (uint64_t)r;
             }
         }
         if (upd) {
             const int db1 = getbit(s.D1, b), db2 = getbit(s.D2, b), da1 = getbit(s.D1, a), da2 = getbit(s.D2, a);
-            tp_add_D(s, vb, db1, db2);
-            tp_add_D(s, va, da1, da2);
-            uint64_t flip = (vb & rb) ^ (va & ra);
+            tp_add_D(s, (uint64_t)vb, db1, db2);
+            tp_add_D(s, (uint64_t)va, da1, da2);
+            W flip = (vb & rb) ^ (va & ra);
             if (jab) flip ^= vb & va;
-            s.D2 ^= flip;
+            s.D2 ^= (uint64_t)flip;
         }
         if (live) E = Ep;
     }
@@ -386,8 +466,10 @@ CSIM_HD inline void zacc(__int128 (&z)[4], int eps, int p, int m, int P, int& er
 }
 
 // One pair: theta's pristine J rows and G columns (as row masks), codeword x;
-// working memory sJ/sGT (stride st), n indices each.  J must be symmetric.
-// `valid` = this lane has a pair (all lanes of a warp call together).
+// working memory sJ/sGT (stride st), n indices each (sJ an even number).
+// J must be symmetric.  `valid` = this lane has a pair (all lanes of a warp
+// call together).  The row arithmetic is 64-bit while the warp's largest k
+// exceeds 32 and 32-bit after that.
 CSIM_HD inline void pair_l(bool valid, int n, int k1, int Q, uint64_t h, uint64_t D1, uint64_t D2, const uint64_t* pJ,
                            const uint64_t* pGT, uint64_t x, uint64_t* sJ, uint64_t* sGT, int st, int& eps, int& p,
                            int& m, int& err) {
@@ -398,7 +480,12 @@ CSIM_HD inline void pair_l(bool valid, int n, int k1, int Q, uint64_t h, uint64_
     s.D1 = D1;
     s.D2 = D2;
     if (valid)
-        for (int r = 0; r < k1; r++) RJ(r) = pJ[r];
+        for (int r = 0; r < k1; r += 2) {
+            U64x2 v;
+            v.a = pJ[r];
+            v.b = pJ[r + 1];
+            *reinterpret_cast<U64x2*>(&RJ(r)) = v;
+        }
     uint64_t zeros = valid ? (~x & lowmask(n)) : 0ull;
     for (uint64_t zz = zeros; zz; zz &= zz - 1) {
         const int c = hd_ffs64(zz) - 1;
@@ -413,10 +500,13 @@ CSIM_HD inline void pair_l(bool valid, int n, int k1, int Q, uint64_t h, uint64_
         const bool act = alive && zeros != 0ull;
         const int q = act ? 63 - hd_clz64(zeros) : 0;
         if (act) zeros &= ~bit1(q);
-        const int r = tp_shrink(s, sJ, sGT, st, q, zeros, act);
+        const bool wide = uniform_max(alive ? s.k : 0) > 32;
+        const int r = wide ? tp_shrink<uint64_t>(s, sJ, sGT, st, q, zeros, act)
+                           : tp_shrink<uint32_t>(s, sJ, sGT, st, q, zeros, act);
         if (act && r == 0) alive = false;
     }
-    tp_exp_sum(s, sJ, st, alive, eps, p, m, err);
+    if (uniform_max(alive ? s.k : 0) > 32) tp_exp_sum<uint64_t>(s, sJ, st, alive, eps, p, m, err);
+    else tp_exp_sum<uint32_t>(s, sJ, st, alive, eps, p, m, err);
     if (alive) p -= k1 + hd_popc64(x);
     else {
         eps = 0;

@@ -91,8 +91,9 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
         const int n = sh.n;
         if (n > nmax || asym) e |= kErrArg;
         if (sh.live && !asym && n >= 1 && n <= nmax) {
+            const int nrow2 = (nmax + 1) & ~1;  // J rows, an even count (pairs)
             uint64_t* sJ = reinterpret_cast<uint64_t*>(smem_raw + sizeof(TPShared));
-            uint64_t* sGT = sJ + (size_t)nmax * kTP;
+            uint64_t* sGT = sJ + (size_t)nrow2 * kTP;
             const int64_t jb = j0 + cb * span;
             for (int r = 0; r < per_thread; r++) {
                 const int64_t j = jb + tid + (int64_t)kTP * r;
@@ -100,7 +101,7 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
                 if (__all_sync(kFull, !valid)) break;  // warp-uniform exit
                 const uint64_t x = valid ? codewords[j - j0] : 0ull;
                 int eps, pp, mm;
-                pc::pair_l(valid, n, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ, sh.pGT, x, sJ + tid, sGT + tid, kTP,
+                pc::pair_l(valid, n, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ, sh.pGT, x, sJ + 2 * tid, sGT + tid, kTP,
                            eps, pp, mm, e);
                 if (!valid) continue;
                 pc::zacc(z, eps, pp, mm, P, e);
@@ -129,7 +130,9 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
     if (e && (tid & 31) == 0) atomicOr(err, e);
 }
 
-size_t terms_tp_smem(int nmax) { return sizeof(TPShared) + (size_t)2 * nmax * kTP * sizeof(uint64_t); }
+size_t terms_tp_smem(int nmax) {
+    return sizeof(TPShared) + (size_t)(((nmax + 1) & ~1) + nmax) * kTP * sizeof(uint64_t);
+}
 
 int launch_terms_tp(const Launch& L, int nmax, const uint64_t* codewords, const GState* theta, const int* code,
                     int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P, __int128* part, int* eps_o,

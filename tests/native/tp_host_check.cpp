@@ -9,7 +9,9 @@
 extern "C" int tp_host_pairs(const csim_state* theta, int ntheta, const uint64_t* xs, int nx, int* eps, int* p,
                              int* m) {
     int err = 0;
-    uint64_t pGT[64], wJ[64], wG[64];
+    uint64_t pGT[64];
+    alignas(16) uint64_t wJ[66];
+    uint64_t wG[64];
     for (int a = 0; a < ntheta; a++) {
         const csim_state& th = theta[a];
         for (int c = 0; c < 64; c++) {
