@@ -198,6 +198,26 @@ int csim_multi_sampled_projector(csim_ctx *ctx, const csim_projector *P, const u
 int csim_exact_projector(csim_ctx *ctx, const csim_projector *P, const uint64_t *L, int32_t k,
                          int32_t exact, double norm, double *out);
 
+/* The sampler above for terms of |L> (exact == 0) with CSIM_RNG_PHILOX and an
+ * explicit seed, for callers that must not allocate device memory: a program
+ * whose GPU memory is owned by its own pool allocator or pre-planned to the
+ * byte, or a component that has been handed no spare device memory.  It
+ * calls no cudaMalloc/cudaFree and needs no csim_ctx; its device scratch is
+ * one fixed 2.5 MiB array in the library, held by every GPU that loads it.
+ * Same values as csim_single_projector_samples(ctx, P, L, k, 0, count,
+ * CSIM_RNG_PHILOX, seed, values).  Limits: 1 <= count <= CSIM_STATIC_MAX_STATES,
+ * 0 <= k <= CSIM_STATIC_MAX_K, 1 <= P->nstabs <= 64; larger inputs fail with
+ * CSIM_ERR_ARG.  The first call on a device looks the array's device address
+ * up (cudaGetSymbolAddress), so make that first call before any stream
+ * capture.  Calls share the array: calls that overlap on the GPU (from two
+ * threads, or two processes' streams on one device) race and must be
+ * serialized by the caller.  Runs on the legacy default stream of `device`.
+ * No counterpart in the reference. */
+#define CSIM_STATIC_MAX_STATES 256
+#define CSIM_STATIC_MAX_K 16
+int csim_single_projector_samples_static(int32_t device, const csim_projector *P, const uint64_t *L, int32_t k,
+                                         int64_t count, uint64_t seed, double *values);
+
 /* ------------------------------------------------------------- host side */
 
 /* Chooses the decomposition: exact |H^t> terms, or a random k x t code L
