@@ -189,7 +189,7 @@ def run_ours(args, rank, world, local_rank):
     cfg, projs, exact, k, norm, L = load_workload()
     gpu = backend.Backend(local_rank)
     P = [backend.projector(ph, xs, zs, nq) for (ph, xs, zs, nq) in projs]
-    samples, bins = cfg["samples"], cfg["bins"]
+    samples, bins = (args.samples or cfg["samples"]), cfg["bins"]
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     seed0 = 1000003 * (rank + 1)
 
@@ -287,7 +287,7 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clk,
         "gpu_launches": launches,
     }
-    if world == 1:
+    if world == 1 and not args.no_cpu_baseline:
         try:
             out["cpu_baseline"] = cpu_baseline(cfg, projs, k, L)
         except Exception as e:  # the baseline never decides the run
@@ -358,6 +358,10 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--samples", type=int, default=None,
+                    help="states per projector per step (default: the workload's L = 4096); smaller values are "
+                         "profiling cases, not bench lines")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
