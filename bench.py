@@ -138,6 +138,15 @@ class ClockSampler:
 ROWOPS_PER_PAIR_T40 = 2576.0
 
 
+def dram_bytes_per_launch(states, k):
+    """DRAM bytes of one pair-kernel launch, scaled from the ncu capture of a
+    64-state launch (profiles/k_terms_tp_c2_small.md: 661 KB read + 439 KB
+    written): reads are the states (1584 B each) and the 8-byte codeword table,
+    writes the 64-byte partial sums of each (state, 1024-term) work item; both
+    grow in proportion to the states."""
+    return states * 1584 + 8 * 2 ** k + states * (2 ** k // 1024) * 64
+
+
 def alu_peak_gops(num_sms, mhz):
     """Integer lane-op issue peak: SMs x 4 schedulers x 32 lanes x clock."""
     return num_sms * 4 * 32 * mhz * 1e6 / 1e9
@@ -265,7 +274,7 @@ def run_ours(args, rank, world, local_rank):
     roofline = {"bound": "alu", "kernel": "k_terms<2,0> (theta x prepL term pairs)",
                 "achieved": achieved, "peak": peak, "unit": "G packed row-ops/s",
                 "frac": (achieved / peak) if achieved else None,
-                "traffic": None,
+                "traffic": dram_bytes_per_launch(samples, k),
                 "work_unit": "packed row-op (one 64-bit row test/XOR/update of the elementary-update algorithm)",
                 "rowops_per_pair": per_pair,
                 "peak_source": "SMs x 4 x 32 lanes x sm_max_mhz (MEASURED_PEAKS.json holds no integer peak)",
