@@ -38,33 +38,9 @@ L2_FLUSH_BYTES = 256 << 20
 
 # ------------------------------------------------------------------ workload
 def parse_protocol(text):
-    """13 scalars + two projectors (libcirc/probability.py:249-272, comms.c:9-36)."""
-    tok = text.split()
-    names = ["quiet", "verbose", "noapprox", "samples", "bins", "t", "k", "exact", "fidbound", "fidelity", "rank",
-             "forceL", "forceSample"]
-    cfg = {}
-    for i, nme in enumerate(names):
-        cfg[nme] = float(tok[i]) if nme == "fidbound" else int(tok[i])
-    pos = len(names)
-    projs = []
-    for _ in range(2):
-        ns, nq = int(tok[pos]), int(tok[pos + 1])
-        pos += 2
-        ph, xs, zs = [], [], []
-        for _ in range(ns):
-            ph.append(int(tok[pos]))
-            pos += 1
-            x = z = 0
-            for j in range(nq):
-                if int(tok[pos]) & 1:
-                    x |= 1 << j
-                if int(tok[pos + 1]) & 1:
-                    z |= 1 << j
-                pos += 2
-            xs.append(x)
-            zs.append(z)
-        projs.append((ph, xs, zs, nq))
-    return cfg, projs
+    from circuitsimulator_gb300 import backend
+
+    return backend.parse_protocol(text)
 
 
 def load_workload():

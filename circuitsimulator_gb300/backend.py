@@ -14,6 +14,7 @@ GB300 is visible, construction fails with an exception.
     multiSampledProjector  libcirc/innerprod.c:23
     exactProjector         libcirc/innerprod.c:148
     decompose              libcirc/probability.c:307
+    run_queries            many backend runs (libcirc/probability.c:44-221) in shared launches
 """
 import ctypes as C
 import os
@@ -58,6 +59,56 @@ class _Projector(C.Structure):
                 ("zs", C.c_void_p)]
 
 
+class _Query(C.Structure):
+    """csim_query of include/csim.h."""
+    _fields_ = ([(n, C.c_int32) for n in ("quiet", "verbose", "noapprox", "samples", "bins", "t", "k", "exact")]
+                + [("fidbound", C.c_double)]
+                + [(n, C.c_int32) for n in ("fidelity", "rank", "force_l", "force_sample")]
+                + [("G", _Projector), ("H", _Projector), ("rng", C.c_int32), ("reserved", C.c_int32),
+                   ("seed", C.c_uint64)])
+
+
+class _QueryResult(C.Structure):
+    """csim_query_result of include/csim.h."""
+    _fields_ = [("numerator", C.c_double), ("denominator", C.c_double), ("norm", C.c_double),
+                ("status", C.c_int32), ("exact", C.c_int32), ("k", C.c_int32), ("noapprox", C.c_int32),
+                ("pairs", C.c_int64)]
+
+
+PROTOCOL_FIELDS = ["quiet", "verbose", "noapprox", "samples", "bins", "t", "k", "exact", "fidbound", "fidelity",
+                   "rank", "forceL", "forceSample"]
+
+
+def parse_protocol(text):
+    """The backend's stdin input: 13 scalars, then the projectors G' and H'
+    (libcirc/probability.py:249-272, libcirc/utils/comms.c:9-36).  Returns
+    (cfg dict, [(phases, xs, zs, nqubits)] * 2) with x/z rows as bit masks."""
+    tok = text.split()
+    cfg = {}
+    for i, name in enumerate(PROTOCOL_FIELDS):
+        cfg[name] = float(tok[i]) if name == "fidbound" else int(tok[i])
+    pos = len(PROTOCOL_FIELDS)
+    projs = []
+    for _ in range(2):
+        ns, nq = int(tok[pos]), int(tok[pos + 1])
+        pos += 2
+        ph, xs, zs = [], [], []
+        for _ in range(ns):
+            ph.append(int(tok[pos]))
+            pos += 1
+            x = z = 0
+            for j in range(nq):
+                if int(tok[pos]) & 1:
+                    x |= 1 << j
+                if int(tok[pos + 1]) & 1:
+                    z |= 1 << j
+                pos += 2
+            xs.append(x)
+            zs.append(z)
+        projs.append((ph, xs, zs, nq))
+    return cfg, projs
+
+
 _lib = None
 
 
@@ -92,6 +143,7 @@ def load_library(path=LIB_PATH):
         "csim_multi_sampled_projector": ([vp, vp, vp, i32, i32, C.c_double, i32, i32, i32, u64, vp], C.c_int),
         "csim_exact_projector": ([vp, vp, vp, i32, i32, C.c_double, vp], C.c_int),
         "csim_decompose": ([i32, C.c_double, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp], C.c_int),
+        "csim_run_queries": ([vp, i64, vp, vp, i32], C.c_int),
         "csim_libc_rand_size": ([], i64),
         "csim_libc_rand_seed": ([vp, C.c_uint32], None),
         "csim_libc_rand_next": ([vp], i32),
@@ -296,6 +348,41 @@ class Backend:
         self._check(self.lib.csim_exact_projector(self.ctx, C.byref(P), _p(Lp), int(k), int(bool(exact)),
                                                   float(norm), C.byref(out)))
         return out.value
+
+    def run_queries(self, queries, batched=True, check=True):
+        """Runs backend queries (libcirc/probability.c:44-221) through csim_run_queries.
+
+        queries: list of dicts with the protocol text under "input" (or "cfg" and
+        "projs" from parse_protocol), "seed", and optionally "rng" (RNG_LIBC by
+        default, like the reference's rand()).  batched=False runs them one after
+        another through the single-query entry points.  Returns one dict per
+        query: numerator, denominator, norm, status, exact, k, noapprox, pairs."""
+        n = len(queries)
+        qs = (_Query * max(n, 1))()
+        keep = []
+        for i, q in enumerate(queries):
+            cfg, projs = (q["cfg"], q["projs"]) if "cfg" in q else parse_protocol(q["input"])
+            G = projector(*projs[0])
+            H = projector(*projs[1])
+            keep += [G, H]
+            qq = qs[i]
+            qq.quiet, qq.verbose, qq.noapprox = cfg["quiet"], cfg["verbose"], cfg["noapprox"]
+            qq.samples, qq.bins, qq.t, qq.k, qq.exact = cfg["samples"], cfg["bins"], cfg["t"], cfg["k"], cfg["exact"]
+            qq.fidbound = cfg["fidbound"]
+            qq.fidelity, qq.rank, qq.force_l, qq.force_sample = (cfg["fidelity"], cfg["rank"], cfg["forceL"],
+                                                                 cfg["forceSample"])
+            qq.G, qq.H = G, H
+            qq.rng = int(q.get("rng", RNG_LIBC))
+            qq.seed = int(q["seed"])
+        rs = (_QueryResult * max(n, 1))()
+        rc = self.lib.csim_run_queries(self.ctx, n, qs, rs, int(bool(batched)))
+        if check:
+            self._check(rc)
+        out = []
+        for i in range(n):
+            r = rs[i]
+            out.append({f: getattr(r, f) for f, _ in r._fields_})
+        return out
 
 
 def run_backend(protocol_text, seed=None, rng=None, timeout=None, exe=EXE_PATH):

@@ -1,0 +1,54 @@
+// csim_batch.h — descriptor tables of the batched executor (csim_run_queries)
+// shared by its host driver (csim_host.cpp) and kernels (csim_batch_kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "csim_internal.h"
+
+namespace csim {
+
+struct GState;
+
+// one state to prepare: draw it (mode 0 Philox, 1 replayed rand() words) or copy
+// `src` (mode 2, a term state of the exact projector), then project it onto the
+// query's projector (nstabs rows pm/pz/px)
+struct DrawDesc {
+    int32_t n, mode, nstabs, pad;
+    uint64_t seed, id;
+    int64_t wbegin, wend;
+    const uint32_t* words;
+    const double* cum;
+    const GState* src;
+    const int32_t* pm;
+    const uint64_t* pz;
+    const uint64_t* px;
+};
+
+// one work item of the pair kernels: state `theta` against terms [j0, j0+nj) of
+// either a codeword table (cw, |L> terms) or a term-state array (phis); the term
+// j == diag (if >= 0) is summed apart (exactProjector's diagonal)
+struct PairItem {
+    int64_t theta, j0, nj, diag;
+    const uint64_t* cw;
+    const GState* phis;
+};
+
+// codeword table of one code: x_j = bits(j) L for j < 2^k, written at out + offset
+struct CodeDesc {
+    const uint64_t* L;
+    int32_t k, pad;
+    int64_t offset;
+};
+
+int launch_draw_project(const Launch& L, const DrawDesc* desc, int64_t count, GState* out, int* code);
+int launch_items_tp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,
+                    int per_thread, int nmax, __int128* part, __int128* part_diag);
+int launch_items_warp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,
+                      __int128* part, __int128* part_diag);
+int launch_reduce_slots(const Launch& L, const __int128* part, const int64_t* first, int64_t nslots, __int128* out);
+int launch_codewords_multi(const Launch& L, const CodeDesc* codes, int ncodes, int64_t maxchi, uint64_t* out);
+
+}  // namespace csim

@@ -1,0 +1,308 @@
+// csim_batch_kernels.cu — kernels that run many probability queries at once
+// (the batched executor, csim_run_queries).  They are the single-query kernels
+// driven by descriptor tables, so states and (theta, term) pairs of queries
+// with different t, codes and term counts share launches:
+//   k_draw_project  one warp per state: draw it (Philox or replayed rand()
+//                   words) or copy a term state, then project it onto its
+//                   query's projector (innerprod.c:97-116 / :224-241)
+//   k_items_tp      the thread-per-pair kernel over an item table of
+//                   (state, range of |L> terms) work items
+//   k_items_warp    the warp-per-pair kernel over (state, range of term states)
+//   k_reduce_slots  per-slot sums of the items' partial sums
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "csim_batch.h"
+#include "csim_internal.h"
+#include "csim_pair_core.cuh"
+#include "csim_rng.cuh"
+#include "csim_warp.cuh"
+
+namespace csim {
+
+namespace {
+
+__device__ __forceinline__ int64_t wglobal() { return ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
+__device__ __forceinline__ int64_t wcount() { return ((int64_t)gridDim.x * blockDim.x) >> 5; }
+
+__device__ __forceinline__ void flush(int e, int* err) {
+    e = (int)__reduce_or_sync(kFull, (unsigned)e);
+    if (e && lane_id() == 0) atomicOr(err, e);
+}
+
+template <int NR>
+__device__ void draw_project(const DrawDesc& d, GState* out, int* code, int& e) {
+    WS<NR> st;
+    if (d.mode == 2) {
+        load_state<NR>(d.src, st);
+    } else {
+        DevRng rng;
+        rng.mode = d.mode;
+        rng.k0 = (uint32_t)d.seed;
+        rng.k1 = (uint32_t)(d.seed >> 32);
+        rng.id0 = (uint32_t)d.id;
+        rng.id1 = (uint32_t)(d.id >> 32);
+        rng.words = d.words;
+        rng.base = d.wbegin;
+        rng.end = d.wend;
+        rng.cur = 0;
+        random_state<NR>(st, d.n, rng, d.cum, e);
+    }
+    int c = 0;
+    for (int r = 0; r < d.nstabs; r++) {
+        const int res = measure_pauli<NR>(st, d.pm[r], d.pz[r], d.px[r]);
+        if (res < 0) {
+            e |= kErrRange;
+            c = -1;
+            break;
+        }
+        if (res == 0) {
+            c = -1;
+            break;
+        }
+        if (res == 2) c++;
+    }
+    store_state<NR>(out, st);
+    if (lane_id() == 0) *code = c;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(256) k_draw_project(const DrawDesc* desc, int64_t count, GState* out, int* code,
+                                                      int* err) {
+    int e = 0;
+    for (int64_t i = wglobal(); i < count; i += wcount()) {
+        const DrawDesc d = desc[i];
+        if (d.n <= 32) draw_project<1>(d, out + i, code + i, e);
+        else draw_project<2>(d, out + i, code + i, e);
+    }
+    flush(e, err);
+}
+
+// ------------------------------------------------------------ thread-per-pair items
+constexpr int kTPB = 64;
+
+struct ItemShared {
+    uint64_t pJ[64];
+    uint64_t pGT[64];
+    uint64_t h, D1, D2;
+    int n, k, Q, live;
+    __int128 red[kTPB / 32][8];
+};
+
+__device__ __forceinline__ __int128 shfl_xor_128(__int128 v, int m) {
+    uint64_t lo = (uint64_t)v, hi = (uint64_t)((unsigned __int128)v >> 64);
+    lo = ((uint64_t)__shfl_xor_sync(kFull, (uint32_t)(lo >> 32), m) << 32) | __shfl_xor_sync(kFull, (uint32_t)lo, m);
+    hi = ((uint64_t)__shfl_xor_sync(kFull, (uint32_t)(hi >> 32), m) << 32) | __shfl_xor_sync(kFull, (uint32_t)hi, m);
+    return (__int128)(((unsigned __int128)hi << 64) | lo);
+}
+
+// One block per item: up to kTPB * per_thread terms of one state.  part[4w..]:
+// the item's sum; part_diag[4w..]: the term j == item.diag (exactProjector).
+__global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_t nitems, const GState* states,
+                                                   const int* codes, int per_thread, int nmax, __int128* part,
+                                                   __int128* part_diag, int* err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ItemShared& sh = *reinterpret_cast<ItemShared*>(smem_raw);
+    const int tid = threadIdx.x;
+    int e = 0;
+    for (int64_t w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const PairItem it = items[w];
+        __syncthreads();
+        const GState* g = states + it.theta;
+        if (tid == 0) {
+            sh.live = codes[it.theta] >= 0;
+            sh.n = g->n;
+            sh.k = g->k;
+            sh.Q = g->Q;
+            sh.h = g->h;
+            sh.D1 = g->D1;
+            sh.D2 = g->D2;
+        }
+        {
+            sh.pJ[tid] = g->J[tid];
+            const int n = g->n, k = g->k;
+            uint64_t col = 0ull;
+            if (tid < n)
+                for (int r = 0; r < k; r++) col |= ((g->G[r] >> tid) & 1ull) << r;
+            sh.pGT[tid] = col;
+        }
+        __syncthreads();
+        bool asym = false;
+        if (tid < sh.k)
+            for (int r = 0; r < sh.k; r++) asym |= ((sh.pJ[tid] >> r) & 1ull) != ((sh.pJ[r] >> tid) & 1ull);
+        asym = __syncthreads_or(asym) != 0;
+        __int128 z[4] = {0, 0, 0, 0}, zd[4] = {0, 0, 0, 0};
+        const int n = sh.n;
+        if (n > nmax || asym) e |= kErrArg;
+        if (sh.live && !asym && n >= 1 && n <= nmax) {
+            const int nrow2 = (nmax + 1) & ~1;
+            uint64_t* sJ = reinterpret_cast<uint64_t*>(smem_raw + sizeof(ItemShared));
+            uint64_t* sGT = sJ + (size_t)nrow2 * kTPB;
+            const int P = 2 * n;
+            for (int r = 0; r < per_thread; r++) {
+                const int64_t j = it.j0 + tid + (int64_t)kTPB * r;
+                const bool valid = j < it.j0 + it.nj;
+                if (__all_sync(kFull, !valid)) break;
+                const uint64_t x = valid ? it.cw[j] : 0ull;
+                int eps, pp, mm;
+                pc::pair_l(valid, n, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ, sh.pGT, x, sJ + 2 * tid, sGT + tid, kTPB,
+                           eps, pp, mm, e);
+                if (!valid) continue;
+                if (j == it.diag) pc::zacc(zd, eps, pp, mm, P, e);
+                else pc::zacc(z, eps, pp, mm, P, e);
+            }
+        }
+        for (int q = 0; q < 4; q++)
+            for (int o = 16; o > 0; o >>= 1) {
+                z[q] += shfl_xor_128(z[q], o);
+                zd[q] += shfl_xor_128(zd[q], o);
+            }
+        if ((tid & 31) == 0)
+            for (int q = 0; q < 4; q++) {
+                sh.red[tid >> 5][q] = z[q];
+                sh.red[tid >> 5][4 + q] = zd[q];
+            }
+        __syncthreads();
+        if (tid < 8) {
+            __int128 acc = 0;
+            for (int ww = 0; ww < kTPB / 32; ww++) acc += sh.red[ww][tid];
+            if (tid < 4) part[4 * w + tid] = acc;
+            else if (part_diag) part_diag[4 * w + tid - 4] = acc;
+        }
+    }
+    e = (int)__reduce_or_sync(kFull, (unsigned)e);
+    if (e && (tid & 31) == 0) atomicOr(err, e);
+}
+
+// ------------------------------------------------------------ warp-per-pair items
+__device__ __forceinline__ void zacc_w(__int128 (&z)[4], int eps, int p, int m, int P, int& err) {
+    pc::zacc(z, eps, p, m, P, err);
+}
+
+template <int NR>
+__device__ void item_warp(const PairItem& it, const GState* states, const int* codes, __int128* part,
+                          __int128* part_diag, int64_t w, int& e) {
+    __int128 z[4] = {0, 0, 0, 0}, zd[4] = {0, 0, 0, 0};
+    if (codes[it.theta] >= 0) {
+        WS<NR> base;
+        load_state<NR>(states + it.theta, base);
+        const int P = 2 * base.n;
+        for (int64_t j = it.j0; j < it.j0 + it.nj; j++) {
+            WS<NR> phi;
+            load_state<NR>(it.phis + j, phi);
+            int ee = 0, pp = 0, mm = 0;
+            inner_product<NR>(base, phi, base.k, ee, pp, mm, e);
+            if (j == it.diag) zacc_w(zd, ee, pp, mm, P, e);
+            else zacc_w(z, ee, pp, mm, P, e);
+        }
+    }
+    if (lane_id() == 0) {
+        for (int q = 0; q < 4; q++) part[4 * w + q] = z[q];
+        if (part_diag)
+            for (int q = 0; q < 4; q++) part_diag[4 * w + q] = zd[q];
+    }
+}
+
+__global__ void __launch_bounds__(256) k_items_warp(const PairItem* items, int64_t nitems, const GState* states,
+                                                    const int* codes, __int128* part, __int128* part_diag, int* err) {
+    int e = 0;
+    for (int64_t w = wglobal(); w < nitems; w += wcount()) {
+        const PairItem it = items[w];
+        const int n = states[it.theta].n;
+        if (n <= 32) item_warp<1>(it, states, codes, part, part_diag, w, e);
+        else item_warp<2>(it, states, codes, part, part_diag, w, e);
+    }
+    flush(e, err);
+}
+
+// slot s sums items [first[s], first[s+1]) (items are grouped by slot)
+__global__ void k_reduce_slots(const __int128* part, const int64_t* first, int64_t nslots, __int128* out) {
+    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nslots * 4;
+         w += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = w / 4, q = w % 4;
+        __int128 acc = 0;
+        for (int64_t i = first[s]; i < first[s + 1]; i++) acc += part[4 * i + q];
+        out[w] = acc;
+    }
+}
+
+// codewords of several codes: descriptor c writes x_j = bits(j) L_c for j < 2^k_c at out + off_c
+__global__ void k_codewords_multi(const CodeDesc* codes, int ncodes, uint64_t* out) {
+    for (int c = 0; c < ncodes; c++) {
+        const CodeDesc d = codes[c];
+        const int64_t chi = (int64_t)1 << d.k;
+        for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < chi;
+             j += (int64_t)gridDim.x * blockDim.x) {
+            uint64_t x = 0ull;
+            for (int r = 0; r < d.k; r++)
+                if ((j >> (d.k - 1 - r)) & 1) x ^= d.L[r];
+            out[d.offset + j] = x;
+        }
+    }
+}
+
+// ------------------------------------------------------------ launchers
+size_t items_tp_smem(int nmax) {
+    return sizeof(ItemShared) + (size_t)(((nmax + 1) & ~1) + nmax) * kTPB * sizeof(uint64_t);
+}
+
+int launch_draw_project(const Launch& L, const DrawDesc* desc, int64_t count, GState* out, int* code) {
+    if (count <= 0) return 0;
+    int64_t blocks = (count + 7) / 8;
+    if (blocks > (int64_t)L.num_sms * 8) blocks = (int64_t)L.num_sms * 8;
+    k_draw_project<<<(int)blocks, 256, 0, L.stream>>>(desc, count, out, code, L.d_err);
+    (*L.launches)++;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_items_tp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,
+                    int per_thread, int nmax, __int128* part, __int128* part_diag) {
+    if (nitems <= 0) return 0;
+    if (nmax < 1 || nmax > 64) return -1;
+    const size_t smem = items_tp_smem(nmax);
+    if (cudaFuncSetAttribute(k_items_tp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)items_tp_smem(64)) !=
+        cudaSuccess)
+        return -1;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_items_tp, kTPB, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    int64_t grid = (int64_t)L.num_sms * per_sm;
+    if (grid > nitems) grid = nitems;
+    k_items_tp<<<(int)grid, kTPB, smem, L.stream>>>(items, nitems, states, codes, per_thread, nmax, part, part_diag,
+                                                    L.d_err);
+    (*L.launches)++;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_items_warp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,
+                      __int128* part, __int128* part_diag) {
+    if (nitems <= 0) return 0;
+    int64_t blocks = (nitems + 7) / 8;
+    if (blocks > (int64_t)L.num_sms * 8) blocks = (int64_t)L.num_sms * 8;
+    k_items_warp<<<(int)blocks, 256, 0, L.stream>>>(items, nitems, states, codes, part, part_diag, L.d_err);
+    (*L.launches)++;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_reduce_slots(const Launch& L, const __int128* part, const int64_t* first, int64_t nslots, __int128* out) {
+    if (nslots <= 0) return 0;
+    int64_t blocks = (nslots * 4 + 255) / 256;
+    if (blocks > (int64_t)L.num_sms * 16) blocks = (int64_t)L.num_sms * 16;
+    k_reduce_slots<<<(int)blocks, 256, 0, L.stream>>>(part, first, nslots, out);
+    (*L.launches)++;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_codewords_multi(const Launch& L, const CodeDesc* codes, int ncodes, int64_t maxchi, uint64_t* out) {
+    if (ncodes <= 0) return 0;
+    int64_t blocks = (maxchi + 255) / 256;
+    if (blocks > (int64_t)L.num_sms * 16) blocks = (int64_t)L.num_sms * 16;
+    if (blocks < 1) blocks = 1;
+    k_codewords_multi<<<(int)blocks, 256, 0, L.stream>>>(codes, ncodes, out);
+    (*L.launches)++;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace csim

@@ -198,6 +198,39 @@ int csim_multi_sampled_projector(csim_ctx *ctx, const csim_projector *P, const u
 int csim_exact_projector(csim_ctx *ctx, const csim_projector *P, const uint64_t *L, int32_t k,
                          int32_t exact, double norm, double *out);
 
+/* ------------------------------------------------------------- many queries */
+
+/* One probability query as the backend process receives it: the 13 scalars of
+ * the stdin protocol (libcirc/probability.py:249-268), the projectors G' and H',
+ * and the sampler's generator and seed (the reference seeds with getpid(),
+ * libcirc/probability.c:182). */
+typedef struct csim_query {
+    int32_t quiet, verbose, noapprox, samples, bins, t, k, exact;
+    double fidbound;
+    int32_t fidelity, rank, force_l, force_sample;
+    csim_projector G, H;
+    int32_t rng; /* CSIM_RNG_LIBC or CSIM_RNG_PHILOX */
+    int32_t reserved;
+    uint64_t seed;
+} csim_query;
+
+typedef struct csim_query_result {
+    double numerator, denominator; /* the backend's last two output lines */
+    double norm;                   /* decompose()'s norm                  */
+    int32_t status;                /* CSIM_OK or this query's error        */
+    int32_t exact, k, noapprox;    /* decomposition and estimator used     */
+    int64_t pairs;                 /* inner products computed              */
+} csim_query_result;
+
+/* Runs nq queries, each exactly as the backend process would (decompose, the
+ * noapprox rule, then multiSampledProjector or exactProjector on G' and H';
+ * libcirc/probability.c:146-216).  batched == 0: one query after another through
+ * the single-query entry points above.  batched == 1: the states, projections and
+ * (state, term) pairs of all queries share launches.  Each query draws from its
+ * own seed, so both modes give the same results.  Returns the first error;
+ * per-query status is in r[i].status. */
+int csim_run_queries(csim_ctx *ctx, int64_t nq, const csim_query *q, csim_query_result *r, int32_t batched);
+
 /* The sampler above for terms of |L> (exact == 0) with CSIM_RNG_PHILOX and an
  * explicit seed, for callers that must not allocate device memory: a program
  * whose GPU memory is owned by its own pool allocator or pre-planned to the

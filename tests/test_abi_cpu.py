@@ -61,3 +61,35 @@ def test_no_device_is_reported_not_faked(lib):
         pytest.skip("a GPU is present")
     with pytest.raises(backend.CsimError):
         backend.Backend(0)
+
+
+def test_query_struct_layout_matches_header(tmp_path):
+    """csim_query / csim_query_result as gcc lays them out == the ctypes binding."""
+    import ctypes
+    import subprocess
+
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "csim.h"\n'
+                   'int main(void) { printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(csim_query), '
+                   'offsetof(csim_query, G), offsetof(csim_query, H), offsetof(csim_query, seed), '
+                   'sizeof(csim_query_result), offsetof(csim_query_result, pairs)); return 0; }\n')
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    Q, R = backend._Query, backend._QueryResult
+    assert got == [ctypes.sizeof(Q), Q.G.offset, Q.H.offset, Q.seed.offset, ctypes.sizeof(R), R.pairs.offset]
+
+
+def test_parse_protocol_reads_the_e2e_inputs():
+    import gzip
+    import json
+
+    with gzip.open(os.path.join(ROOT, "tests", "golden", "e2e_cases.json.gz"), "rt") as f:
+        cases = json.load(f)
+    for c in cases:
+        cfg, projs = backend.parse_protocol(c["input"])
+        assert set(cfg) == set(backend.PROTOCOL_FIELDS)
+        assert len(projs) == 2
+        for ph, xs, zs, nq in projs:
+            assert len(ph) == len(xs) == len(zs)
+            assert all(x < (1 << nq) and z < (1 << nq) for x, z in zip(xs, zs))

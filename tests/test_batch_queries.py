@@ -1,0 +1,108 @@
+"""Many backend queries at once (csim_run_queries).
+
+Batched mode shares launches between queries of different t, codes and
+estimators, but every query draws from its own seed.  So each query must give
+bit-identical numerator/denominator to the plain one-after-another mode, and
+to itself when run alone.  The plain mode matches the reference backend
+(tests/golden/e2e_cases.json.gz) within 1e-12 relative."""
+import gzip
+import json
+import os
+
+import numpy as np
+import pytest
+
+from circuitsimulator_gb300 import backend
+from helpers import close, random_projector_rows
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+pytestmark = pytest.mark.gpu
+
+
+def e2e_cases():
+    with gzip.open(os.path.join(HERE, "golden", "e2e_cases.json.gz"), "rt") as f:
+        return json.load(f)
+
+
+@pytest.fixture(scope="module")
+def be():
+    b = backend.Backend(0)
+    yield b
+    b.close()
+
+
+def _key(r):
+    return (r["status"], r["numerator"].hex(), r["denominator"].hex(), r["norm"].hex(), r["exact"], r["k"],
+            r["noapprox"], r["pairs"])
+
+
+def _cfg(t, **kw):
+    cfg = dict(quiet=1, verbose=0, noapprox=0, samples=8, bins=1, t=t, k=0, exact=0, fidbound=1e-5, fidelity=0,
+               rank=0, forceL=0, forceSample=1)
+    cfg.update(kw)
+    return cfg
+
+
+def mixed_queries(seed=7, count=24):
+    """Queries of several t, both decompositions, sampled and exact estimators,
+    Philox and rand() draws."""
+    rs = np.random.RandomState(seed)
+    out = []
+    for i in range(count):
+        t = int(rs.choice([3, 6, 9, 12, 17, 24, 33, 40]))
+        exact = int(t <= 12 and rs.randint(2))
+        k = 0 if exact else int(min(t, rs.choice([2, 4, 6, 8])))
+        noapprox = int(t <= 12 and rs.randint(4) == 0)
+        cfg = _cfg(t, exact=exact, k=k, noapprox=noapprox, samples=int(rs.choice([4, 9, 16])),
+                   bins=int(rs.choice([1, 2, 3])), forceSample=0 if noapprox else 1)
+        ng = int(rs.randint(1, min(t, 8) + 1))
+        g = random_projector_rows(rs, t, ng)
+        h = (g[0][1:], g[1][1:], g[2][1:])  # H' drops the measured row, as probability.py's truncation does
+        out.append({"cfg": cfg, "projs": [(*g, t), (*h, t)], "seed": 1000 + i,
+                    "rng": backend.RNG_PHILOX if rs.randint(2) else backend.RNG_LIBC})
+    return out
+
+
+def test_e2e_cases_batched_equal_plain_and_reference(be):
+    cases = e2e_cases()
+    qs = [{"input": c["input"], "seed": c["seed"]} for c in cases]
+    plain = be.run_queries(qs, batched=False)
+    batched = be.run_queries(qs, batched=True)
+    for c, p, b in zip(cases, plain, batched):
+        assert _key(p) == _key(b), c["label"]
+        num, den = float(c["ref"][-2]), float(c["ref"][-1])
+        assert close(b["numerator"], num, 1e-12, 1e-12), (c["label"], b["numerator"], num)
+        assert close(b["denominator"], den, 1e-12, 1e-12), (c["label"], b["denominator"], den)
+
+
+def test_mixed_queries_batched_equal_plain(be):
+    qs = mixed_queries()
+    plain = be.run_queries(qs, batched=False)
+    batched = be.run_queries(qs, batched=True)
+    assert any(r["noapprox"] for r in batched) and any(not r["noapprox"] for r in batched)
+    assert any(r["exact"] for r in batched) and any(not r["exact"] for r in batched)
+    for i, (p, b) in enumerate(zip(plain, batched)):
+        assert _key(p) == _key(b), (i, p, b)
+
+
+def test_each_query_alone_equals_it_in_the_mix(be):
+    qs = mixed_queries(seed=11, count=12)
+    mix = be.run_queries(qs, batched=True)
+    for i, q in enumerate(qs):
+        alone = be.run_queries([q], batched=True)[0]
+        assert _key(alone) == _key(mix[i]), i
+
+
+def test_bad_query_fails_alone(be):
+    qs = mixed_queries(seed=3, count=4)
+    bad = dict(qs[1])
+    bad["cfg"] = dict(bad["cfg"], bins=0, noapprox=0, forceSample=1)
+    qs[1] = bad
+    res = be.run_queries(qs, batched=True, check=False)
+    assert res[1]["status"] == -1
+    ok = be.run_queries([qs[0], qs[2], qs[3]], batched=True)
+    assert [_key(r) for r in ok] == [_key(res[0]), _key(res[2]), _key(res[3])]
+
+
+def test_empty_batch(be):
+    assert be.run_queries([], batched=True) == []
