@@ -15,6 +15,7 @@ GB300 is visible, construction fails with an exception.
     exactProjector         libcirc/innerprod.c:148
     decompose              libcirc/probability.c:307
     run_queries            many backend runs (libcirc/probability.c:44-221) in shared launches
+    Server                 the same as a long-lived server with continuous batching
 """
 import ctypes as C
 import os
@@ -72,7 +73,7 @@ class _QueryResult(C.Structure):
     """csim_query_result of include/csim.h."""
     _fields_ = [("numerator", C.c_double), ("denominator", C.c_double), ("norm", C.c_double),
                 ("status", C.c_int32), ("exact", C.c_int32), ("k", C.c_int32), ("noapprox", C.c_int32),
-                ("pairs", C.c_int64)]
+                ("pairs", C.c_int64), ("latency_s", C.c_double)]
 
 
 PROTOCOL_FIELDS = ["quiet", "verbose", "noapprox", "samples", "bins", "t", "k", "exact", "fidbound", "fidelity",
@@ -144,6 +145,13 @@ def load_library(path=LIB_PATH):
         "csim_exact_projector": ([vp, vp, vp, i32, i32, C.c_double, vp], C.c_int),
         "csim_decompose": ([i32, C.c_double, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp], C.c_int),
         "csim_run_queries": ([vp, i64, vp, vp, i32], C.c_int),
+        "csim_server_create": ([vp, vp], C.c_int),
+        "csim_submit": ([vp, vp, vp], C.c_int),
+        "csim_poll": ([vp, i64, vp], C.c_int),
+        "csim_wait": ([vp, i64, C.c_double, vp], C.c_int),
+        "csim_release": ([vp, i64], C.c_int),
+        "csim_server_get_stats": ([vp, vp], C.c_int),
+        "csim_server_destroy": ([vp], None),
         "csim_libc_rand_size": ([], i64),
         "csim_libc_rand_seed": ([vp, C.c_uint32], None),
         "csim_libc_rand_next": ([vp], i32),
@@ -361,28 +369,108 @@ class Backend:
         qs = (_Query * max(n, 1))()
         keep = []
         for i, q in enumerate(queries):
-            cfg, projs = (q["cfg"], q["projs"]) if "cfg" in q else parse_protocol(q["input"])
-            G = projector(*projs[0])
-            H = projector(*projs[1])
-            keep += [G, H]
-            qq = qs[i]
-            qq.quiet, qq.verbose, qq.noapprox = cfg["quiet"], cfg["verbose"], cfg["noapprox"]
-            qq.samples, qq.bins, qq.t, qq.k, qq.exact = cfg["samples"], cfg["bins"], cfg["t"], cfg["k"], cfg["exact"]
-            qq.fidbound = cfg["fidbound"]
-            qq.fidelity, qq.rank, qq.force_l, qq.force_sample = (cfg["fidelity"], cfg["rank"], cfg["forceL"],
-                                                                 cfg["forceSample"])
-            qq.G, qq.H = G, H
-            qq.rng = int(q.get("rng", RNG_LIBC))
-            qq.seed = int(q["seed"])
+            _fill_query(qs[i], q, keep)
         rs = (_QueryResult * max(n, 1))()
         rc = self.lib.csim_run_queries(self.ctx, n, qs, rs, int(bool(batched)))
         if check:
             self._check(rc)
-        out = []
-        for i in range(n):
-            r = rs[i]
-            out.append({f: getattr(r, f) for f, _ in r._fields_})
-        return out
+        return [_result_dict(rs[i]) for i in range(n)]
+
+
+def _fill_query(qq, q, keep):
+    cfg, projs = (q["cfg"], q["projs"]) if "cfg" in q else parse_protocol(q["input"])
+    G = projector(*projs[0])
+    H = projector(*projs[1])
+    keep += [G, H]
+    qq.quiet, qq.verbose, qq.noapprox = cfg["quiet"], cfg["verbose"], cfg["noapprox"]
+    qq.samples, qq.bins, qq.t, qq.k, qq.exact = cfg["samples"], cfg["bins"], cfg["t"], cfg["k"], cfg["exact"]
+    qq.fidbound = cfg["fidbound"]
+    qq.fidelity, qq.rank, qq.force_l, qq.force_sample = cfg["fidelity"], cfg["rank"], cfg["forceL"], cfg["forceSample"]
+    qq.G, qq.H = G, H
+    qq.rng = int(q.get("rng", RNG_LIBC))
+    qq.seed = int(q["seed"])
+
+
+def _result_dict(r):
+    return {f: getattr(r, f) for f, _ in r._fields_}
+
+
+class _ServerConfig(C.Structure):
+    """csim_server_config of include/csim.h."""
+    _fields_ = [("device", C.c_int32), ("per_thread", C.c_int32), ("hbm_budget_bytes", C.c_int64),
+                ("round_pairs", C.c_int64), ("round_states", C.c_int64)]
+
+
+class _ServerStats(C.Structure):
+    """csim_server_stats of include/csim.h."""
+    _fields_ = [(n, C.c_int64) for n in ("submitted", "completed", "failed", "rounds", "pairs", "resident_bytes",
+                                         "resident_decompositions", "queued")] + [("device_ms", C.c_double)]
+
+
+PENDING = 1
+
+
+class Server:
+    """A query server on one GPU (csim_server_*): submit backend queries from
+    any thread, poll or wait for their results.  Queries that arrive while
+    others run join the next round of shared launches."""
+
+    def __init__(self, device=0, hbm_budget_bytes=0, round_pairs=0, round_states=0, per_thread=0):
+        self.lib = load_library()
+        cfg = _ServerConfig(int(device), int(per_thread), int(hbm_budget_bytes), int(round_pairs),
+                            int(round_states))
+        h = C.c_void_p()
+        rc = self.lib.csim_server_create(C.byref(cfg), C.byref(h))
+        if rc:
+            raise CsimError(rc, "csim_server_create on device %d" % device)
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.csim_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, query):
+        qq = _Query()
+        keep = []
+        _fill_query(qq, query, keep)
+        t = C.c_int64()
+        rc = self.lib.csim_submit(self.h, C.byref(qq), C.byref(t))
+        if rc:
+            raise CsimError(rc, "csim_submit")
+        return t.value
+
+    def poll(self, ticket):
+        r = _QueryResult()
+        rc = self.lib.csim_poll(self.h, int(ticket), C.byref(r))
+        if rc == PENDING:
+            return None
+        if rc:
+            raise CsimError(rc, "csim_poll %d" % ticket)
+        return _result_dict(r)
+
+    def wait(self, ticket, timeout=None):
+        r = _QueryResult()
+        rc = self.lib.csim_wait(self.h, int(ticket), -1.0 if timeout is None else float(timeout), C.byref(r))
+        if rc == PENDING:
+            return None
+        if rc:
+            raise CsimError(rc, "csim_wait %d" % ticket)
+        return _result_dict(r)
+
+    def release(self, ticket):
+        return self.lib.csim_release(self.h, int(ticket))
+
+    def stats(self):
+        st = _ServerStats()
+        self.lib.csim_server_get_stats(self.h, C.byref(st))
+        return _result_dict(st)
 
 
 def run_backend(protocol_text, seed=None, rng=None, timeout=None, exe=EXE_PATH):

@@ -21,7 +21,7 @@ EXE = os.path.join(PKG, "gpubackend")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-I" + os.path.join(ROOT, "include")]
-SOURCES = ["csim_kernels.cu", "csim_terms_tp.cu", "csim_static.cu", "csim_batch_kernels.cu", "csim_host.cpp", "csim_backend.cpp"]
+SOURCES = ["csim_kernels.cu", "csim_terms_tp.cu", "csim_static.cu", "csim_batch_kernels.cu", "csim_host.cpp", "csim_engine.cpp", "csim_backend.cpp"]
 
 
 def _nvcc():

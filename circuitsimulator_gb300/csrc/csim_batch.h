@@ -1,5 +1,5 @@
-// csim_batch.h — descriptor tables of the batched executor (csim_run_queries)
-// shared by its host driver (csim_host.cpp) and kernels (csim_batch_kernels.cu).
+// csim_batch.h — descriptor tables of the query engine (csim_engine.cpp),
+// shared with its kernels (csim_batch_kernels.cu).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -48,7 +48,8 @@ int launch_items_tp(const Launch& L, const PairItem* items, int64_t nitems, cons
                     int per_thread, int nmax, __int128* part, __int128* part_diag);
 int launch_items_warp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,
                       __int128* part, __int128* part_diag);
-int launch_reduce_slots(const Launch& L, const __int128* part, const int64_t* first, int64_t nslots, __int128* out);
+// per-slot sums of item partials; slot s owns items [range[2s], range[2s+1])
+int launch_reduce_slots(const Launch& L, const __int128* part, const int64_t* range, int64_t nslots, __int128* out);
 int launch_codewords_multi(const Launch& L, const CodeDesc* codes, int ncodes, int64_t maxchi, uint64_t* out);
 
 }  // namespace csim

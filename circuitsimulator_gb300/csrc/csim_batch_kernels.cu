@@ -217,13 +217,13 @@ __global__ void __launch_bounds__(256) k_items_warp(const PairItem* items, int64
     flush(e, err);
 }
 
-// slot s sums items [first[s], first[s+1]) (items are grouped by slot)
-__global__ void k_reduce_slots(const __int128* part, const int64_t* first, int64_t nslots, __int128* out) {
+// slot s sums the items [range[2s], range[2s+1])
+__global__ void k_reduce_slots(const __int128* part, const int64_t* range, int64_t nslots, __int128* out) {
     for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nslots * 4;
          w += (int64_t)gridDim.x * blockDim.x) {
         const int64_t s = w / 4, q = w % 4;
         __int128 acc = 0;
-        for (int64_t i = first[s]; i < first[s + 1]; i++) acc += part[4 * i + q];
+        for (int64_t i = range[2 * s]; i < range[2 * s + 1]; i++) acc += part[4 * i + q];
         out[w] = acc;
     }
 }
@@ -286,11 +286,11 @@ int launch_items_warp(const Launch& L, const PairItem* items, int64_t nitems, co
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-int launch_reduce_slots(const Launch& L, const __int128* part, const int64_t* first, int64_t nslots, __int128* out) {
+int launch_reduce_slots(const Launch& L, const __int128* part, const int64_t* range, int64_t nslots, __int128* out) {
     if (nslots <= 0) return 0;
     int64_t blocks = (nslots * 4 + 255) / 256;
     if (blocks > (int64_t)L.num_sms * 16) blocks = (int64_t)L.num_sms * 16;
-    k_reduce_slots<<<(int)blocks, 256, 0, L.stream>>>(part, first, nslots, out);
+    k_reduce_slots<<<(int)blocks, 256, 0, L.stream>>>(part, range, nslots, out);
     (*L.launches)++;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -1,0 +1,1065 @@
+// csim_engine.cpp — the query engine behind csim_run_queries and the server.
+//
+// Runs many probability queries.  Each query runs as the backend process
+// would run it (libcirc/probability.c:146-216): decompose, the noapprox rule,
+// then multiSampledProjector or exactProjector on G' and H'.  All admitted
+// queries share launches.
+//
+// Work is cut into rounds.  A round takes the next states of the admitted
+// evaluations (one evaluation = one projector of one query), up to a budget
+// of inner products, and runs:
+//   k_draw_project  draw or copy every state, then project it (innerprod.c:97-116)
+//   k_items_tp      (state, |L> term range) items, thread per pair
+//   k_items_warp    (state, prepH term range) items, warp per pair
+//   k_reduce_slots  exact Z[w] sums per state
+// Two round buffers alternate.  The host builds round r+1 and queues it behind
+// round r, then reads round r's results.
+//
+// Per-state values are kept until an evaluation's last state is in.  The
+// estimator then reduces them in draw (row) order, the same order the
+// single-query entry points use.  So a result does not depend on how its
+// states were split into rounds, nor on which other queries shared them.
+//
+// Decompositions (codeword tables, term states) stay resident on the device.
+// Queries with the same t and code share them; unused ones are evicted,
+// least recently used first, when a new one does not fit the memory budget.
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+
+#include "csim_batch.h"
+#include "csim_host_common.h"
+
+using namespace csim_host;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+constexpr size_t kAlign = 256;
+inline size_t align_up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
+
+// device memory that grows on demand (contents are not kept)
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    int ensure(size_t bytes) {
+        if (bytes <= cap) return 0;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        const size_t c = align_up(bytes + bytes / 4);
+        if (cudaMalloc(&p, c) != cudaSuccess) {
+            p = nullptr;
+            return CSIM_ERR_NOMEM;
+        }
+        cap = c;
+        return 0;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+// pinned host memory that grows on demand
+struct HostBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    int ensure(size_t bytes) {
+        if (bytes <= cap) return 0;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        const size_t c = align_up(bytes + bytes / 4);
+        if (cudaMallocHost(&p, c) != cudaSuccess) {
+            p = nullptr;
+            return CSIM_ERR_NOMEM;
+        }
+        cap = c;
+        return 0;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+// one decomposition of |H^t> resident on the device
+struct Decomp {
+    int t = 0, exact = 0, k = 0;
+    int64_t chi = 0;
+    std::vector<uint64_t> L;
+    uint64_t* cw = nullptr;      // codewords (exact == 0)
+    csim_state* phis = nullptr;  // term states: prepH (exact == 1), prepL (exact projector on |L>)
+    uint64_t* dL = nullptr;
+    size_t bytes = 0;
+    int refs = 0;
+    int64_t last_use = 0;
+    void release() {
+        if (cw) cudaFree(cw);
+        if (phis) cudaFree(phis);
+        if (dL) cudaFree(dL);
+        cw = nullptr;
+        phis = nullptr;
+        dL = nullptr;
+    }
+};
+
+struct QueryRec;
+
+// one projector of one query evaluated on the device
+struct Eval {
+    QueryRec* q = nullptr;
+    int which = 0;  // 0 G', 1 H'
+    int kind = 1;   // 1 sampled (multiSampledProjector), 2 exactProjector
+    int t = 0;
+    int64_t chi = 0, ns = 0;
+    int samples = 0, bins = 1;
+    int64_t next = 0, done = 0;
+    std::vector<double> val;  // sampled: value per state; exact: re, im per row
+    std::vector<char> live;   // exact: row survived the projection
+    int nstabs = 0;
+    int32_t pm[64];
+    uint64_t pz[64], px[64];
+    uint64_t id0 = 0;  // first Philox draw id
+    double value = 0;
+    bool finished = false;
+};
+
+struct QueryRec {
+    int64_t ticket = 0;
+    csim_query q{};
+    std::vector<int32_t> ph[2];
+    std::vector<uint64_t> xs[2], zs[2];
+    int exact = 0, k = 0, noapprox = 0;
+    double norm = 0;
+    uint64_t L[CSIM_MAX_QUBITS] = {0};
+    int64_t chi = 0;
+    LibcRand lr;
+    Decomp* dec = nullptr;
+    double host_value[2] = {0, 0};
+    bool host_only[2] = {false, false};
+    std::unique_ptr<Eval> ev[2];
+    int pending = 0;
+    std::atomic<int64_t> inflight{0};  // its states in rounds not yet read back
+    bool admitted = false, done = false;
+    csim_query_result res{};
+    Clock::time_point t_submit;
+};
+
+struct Slot {
+    Eval* e;
+    int64_t s;
+};
+
+// one round's buffers and contents
+struct RoundSet {
+    DevBuf up, work, down;
+    HostBuf hup, hdown;
+    cudaEvent_t ev[4] = {};  // start, pair kernels start, pair kernels end, end
+    std::vector<Slot> slots;
+    int64_t pairs = 0;
+    size_t off_codes = 0, off_sum = 0, off_sumd = 0;
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------- engine
+class Engine {
+  public:
+    Engine(csim_ctx* ctx, int64_t round_pairs, int64_t round_states, int per_thread, int64_t budget)
+        : ctx_(ctx),
+          round_pairs_(round_pairs > 0 ? round_pairs : ((int64_t)1 << 26)),
+          round_states_(round_states > 0 ? round_states : ((int64_t)1 << 16)),
+          per_thread_(per_thread > 0 ? per_thread : 16),
+          budget_(budget > 0 ? budget : ((int64_t)8 << 30)) {}
+
+    ~Engine() {
+        cudaStreamSynchronize(ctx_->stream);
+        for (auto& rs : sets_) {
+            rs.up.release();
+            rs.work.release();
+            rs.down.release();
+            rs.hup.release();
+            rs.hdown.release();
+            for (auto& e : rs.ev)
+                if (e) cudaEventDestroy(e);
+        }
+        for (auto& kv : decomps_) kv.second->release();
+        cum_.release();
+        iota_.release();
+    }
+
+    int init() {
+        csim_ctx* const ctx = ctx_;  // for CK
+        for (auto& rs : sets_)
+            for (auto& e : rs.ev)
+                if (cudaEventCreate(&e) != cudaSuccess) return fail(ctx_, CSIM_ERR_CUDA, "event create failed");
+        // randomStabilizerState's cumulative tables for every n (stabilizer.c:694-716)
+        std::vector<double> cum(65 * 65, 0.0);
+        for (int t = 1; t <= CSIM_MAX_QUBITS; t++) cum_table(t, &cum[65 * t]);
+        if (cum_.ensure(cum.size() * 8)) return fail(ctx_, CSIM_ERR_NOMEM, "cum table");
+        CK(cudaMemcpy(cum_.p, cum.data(), cum.size() * 8, cudaMemcpyHostToDevice));
+        return 0;
+    }
+
+    // host plan of one query (decompose, noapprox rule); completes host-only and failed queries
+    void plan(QueryRec* r);
+    // makes the query's decomposition resident and creates its evaluations;
+    // false when it does not fit the memory budget now
+    int admit(QueryRec* r, bool force, bool* admitted);
+    bool schedulable() const;
+    int launch_round();
+    int complete_round();
+    int inflight() const { return (int)inflight_.size(); }
+    bool idle() const { return inflight_.empty() && !schedulable(); }
+
+    // finished queries (the caller collects them)
+    std::vector<QueryRec*> finished;
+
+    int64_t rounds = 0, pairs = 0, states = 0, states_live = 0;
+    double device_ms = 0, pair_ms = 0;
+    int64_t resident_bytes() const { return resident_; }
+    int64_t resident_count() const { return (int64_t)decomps_.size(); }
+
+  private:
+    csim_ctx* ctx_;
+    int64_t round_pairs_, round_states_;
+    int per_thread_;
+    int64_t budget_;
+    int64_t resident_ = 0, use_clock_ = 0;
+    std::map<std::vector<uint64_t>, std::unique_ptr<Decomp>> decomps_;
+    std::vector<Eval*> active_;
+    RoundSet sets_[2];
+    int next_set_ = 0;
+    std::deque<RoundSet*> inflight_;
+    DevBuf cum_, iota_;
+    int64_t iota_n_ = 0;
+
+    csim::Launch launch_on(int* d_err) { return csim::Launch{ctx_->stream, d_err, &ctx_->launches, ctx_->num_sms}; }
+    int ensure_decomp(QueryRec* r, bool need_phis, bool force, Decomp** out);
+    void finish_eval(Eval* e);
+    void finish_query(QueryRec* r);
+    void fail_query(QueryRec* r, int status);
+    bool eval_ready(const Eval* e) const;
+};
+
+void Engine::plan(QueryRec* r) {
+    const csim_query& Q = r->q;
+    csim_query_result& R = r->res;
+    R = csim_query_result{};
+    if (Q.t < 0 || Q.t > CSIM_MAX_QUBITS || (Q.rng != CSIM_RNG_LIBC && Q.rng != CSIM_RNG_PHILOX) ||
+        check_projector(ctx_, &Q.G) || check_projector(ctx_, &Q.H) || (Q.G.nstabs && Q.G.nqubits != Q.t) ||
+        (Q.H.nstabs && Q.H.nqubits != Q.t) || Q.G.nstabs > 64 || Q.H.nstabs > 64) {
+        fail_query(r, fail(ctx_, CSIM_ERR_ARG, "query %lld: bad t, rng or projectors", (long long)r->ticket));
+        return;
+    }
+    // decompose() runs on rand()'s default stream, before the sampler is seeded (probability.c:146-153)
+    LibcRand ds;
+    ds.seed(1);
+    r->exact = Q.exact;
+    r->k = Q.k;
+    const int rc = csim_decompose(Q.t, Q.fidbound, Q.rank, Q.fidelity, Q.force_l, Q.verbose, Q.quiet, &r->exact,
+                                  &r->k, &r->norm, r->L, &ds, nullptr);
+    if (rc != CSIM_OK) {
+        fail_query(r, rc);
+        return;
+    }
+    r->noapprox = Q.noapprox;
+    if (Q.noapprox == 0 && Q.force_sample == 0) {  // probability.c:162-174
+        const double terms = r->exact ? pow(2, (Q.t + 1) / 2) : pow(2, r->k);
+        if (Q.samples * Q.bins * 2 > (terms - 1)) r->noapprox = 1;
+    }
+    if (r->noapprox == 0 && (Q.bins < 1 || Q.samples < 0)) {
+        fail_query(r, fail(ctx_, CSIM_ERR_ARG, "query %lld: samples=%d bins=%d", (long long)r->ticket, Q.samples,
+                           Q.bins));
+        return;
+    }
+    R.exact = r->exact;
+    R.k = r->k;
+    R.noapprox = r->noapprox;
+    R.norm = r->norm;
+    r->chi = Q.t == 0 ? 0 : (r->exact ? ((int64_t)1 << ((Q.t + 1) / 2)) : ((int64_t)1 << r->k));
+    for (int w = 0; w < 2; w++) {
+        const csim_projector& P = w == 0 ? Q.G : Q.H;
+        if (P.nstabs == 0) {  // innerprod.c:47 / :150
+            r->host_only[w] = true;
+            r->host_value[w] = pow(r->norm, 2);
+        } else if (Q.t == 0) {  // innerprod.c:52-62; exactProjector's branch has no norm^2
+            r->host_only[w] = true;
+            r->host_value[w] = (r->noapprox ? 1.0 : pow(r->norm, 2)) * clifford_sum(&P) / (1 + (double)P.nstabs);
+        }
+    }
+    if (!(r->host_only[0] && r->host_only[1])) {
+        if (check_code(ctx_, Q.t, r->exact, r->L, r->k)) {
+            fail_query(r, CSIM_ERR_ARG);
+            return;
+        }
+        if (r->noapprox && r->chi > ((int64_t)1 << 20)) {
+            fail_query(r, fail(ctx_, CSIM_ERR_ARG, "query %lld: chi too large for the exact projector",
+                               (long long)r->ticket));
+            return;
+        }
+    } else {
+        r->res.numerator = r->host_value[0];
+        r->res.denominator = r->host_value[1];
+        r->done = true;
+        finished.push_back(r);
+    }
+}
+
+int Engine::ensure_decomp(QueryRec* r, bool need_phis, bool force, Decomp** out) {
+    csim_ctx* const ctx = ctx_;  // for CK
+    *out = nullptr;
+    std::vector<uint64_t> key = {(uint64_t)r->q.t, (uint64_t)r->exact, (uint64_t)(r->exact ? 0 : r->k)};
+    if (!r->exact) key.insert(key.end(), r->L, r->L + r->k);
+    auto it = decomps_.find(key);
+    Decomp* d = it == decomps_.end() ? nullptr : it->second.get();
+    const int64_t chi = r->chi;
+    const bool want_cw = !r->exact, want_phis = r->exact || need_phis;
+    size_t add = 0;
+    if (!d && want_cw) add += align_up((size_t)chi * 8) + kAlign;
+    if (want_phis && !(d && d->phis)) add += align_up((size_t)chi * sizeof(csim_state));
+    if (add && resident_ + (int64_t)add > budget_) {  // evict unused decompositions, least recently used first
+        std::vector<std::pair<int64_t, std::vector<uint64_t>>> lru;
+        for (auto& kv : decomps_)
+            if (kv.second->refs == 0 && kv.second.get() != d) lru.push_back({kv.second->last_use, kv.first});
+        std::sort(lru.begin(), lru.end());
+        for (auto& e : lru) {
+            if (resident_ + (int64_t)add <= budget_) break;
+            auto jt = decomps_.find(e.second);
+            cudaStreamSynchronize(ctx_->stream);
+            resident_ -= (int64_t)jt->second->bytes;
+            jt->second->release();
+            decomps_.erase(jt);
+        }
+        if (resident_ + (int64_t)add > budget_ && !force) return 0;
+    }
+    if (!d) {
+        auto nd = std::make_unique<Decomp>();
+        nd->t = r->q.t;
+        nd->exact = r->exact;
+        nd->k = r->exact ? 0 : r->k;
+        nd->chi = chi;
+        nd->L.assign(r->L, r->L + (r->exact ? 0 : r->k));
+        d = nd.get();
+        decomps_[key] = std::move(nd);
+        if (want_cw) {
+            if (cudaMalloc(&d->cw, (size_t)chi * 8) != cudaSuccess ||
+                cudaMalloc(&d->dL, 8 * (size_t)CSIM_MAX_QUBITS) != cudaSuccess) {
+                d->release();
+                decomps_.erase(key);
+                return fail(ctx_, CSIM_ERR_NOMEM, "codeword table of 2^%d terms", r->k);
+            }
+            d->bytes += align_up((size_t)chi * 8) + kAlign;
+            uint64_t rows[CSIM_MAX_QUBITS] = {0};
+            for (int i = 0; i < d->k; i++) rows[i] = d->L[i];
+            CK(cudaMemcpy(d->dL, rows, sizeof(rows), cudaMemcpyHostToDevice));
+            if (csim::launch_codewords(launch_of(ctx_), d->dL, d->k, 0, chi, d->cw))
+                return fail(ctx_, CSIM_ERR_CUDA, "codeword launch failed");
+        }
+        resident_ += (int64_t)d->bytes;
+    }
+    if (want_phis && !d->phis) {
+        if (cudaMalloc(&d->phis, (size_t)chi * sizeof(csim_state)) != cudaSuccess) {
+            d->phis = nullptr;
+            return fail(ctx_, CSIM_ERR_NOMEM, "term states of 2^%lld terms", (long long)chi);
+        }
+        d->bytes += align_up((size_t)chi * sizeof(csim_state));
+        resident_ += (int64_t)align_up((size_t)chi * sizeof(csim_state));
+        if (d->exact) {
+            if (iota_n_ < chi) {  // prepH term indices 0..chi-1
+                std::vector<int64_t> idx(chi);
+                for (int64_t j = 0; j < chi; j++) idx[j] = j;
+                cudaStreamSynchronize(ctx_->stream);
+                if (iota_.ensure((size_t)chi * 8)) return fail(ctx_, CSIM_ERR_NOMEM, "term indices");
+                CK(cudaMemcpy(iota_.p, idx.data(), (size_t)chi * 8, cudaMemcpyHostToDevice));
+                iota_n_ = chi;
+            }
+            if (csim::launch_prep(launch_of(ctx_), d->t, 1, nullptr, (const int64_t*)iota_.p, chi,
+                                  (csim::GState*)d->phis))
+                return fail(ctx_, CSIM_ERR_CUDA, "prepH launch failed");
+        } else if (csim::launch_prep(launch_of(ctx_), d->t, 0, d->cw, nullptr, chi, (csim::GState*)d->phis)) {
+            return fail(ctx_, CSIM_ERR_CUDA, "prepL launch failed");
+        }
+    }
+    d->last_use = ++use_clock_;
+    *out = d;
+    return 0;
+}
+
+int Engine::admit(QueryRec* r, bool force, bool* admitted) {
+    *admitted = false;
+    if (r->done) {
+        *admitted = true;
+        return 0;
+    }
+    Decomp* d = nullptr;
+    const int rc = ensure_decomp(r, r->noapprox != 0, force, &d);
+    if (rc) {
+        fail_query(r, rc);
+        *admitted = true;
+        return 0;
+    }
+    if (!d) return 0;  // does not fit yet
+    d->refs++;
+    r->dec = d;
+    r->admitted = true;
+    *admitted = true;
+    const csim_query& Q = r->q;
+    uint64_t philox_next = 0;
+    if (Q.rng == CSIM_RNG_LIBC) r->lr.seed((uint32_t)Q.seed);
+    for (int w = 0; w < 2; w++) {
+        if (r->host_only[w]) continue;
+        const csim_projector& P = w == 0 ? Q.G : Q.H;
+        auto e = std::make_unique<Eval>();
+        e->q = r;
+        e->which = w;
+        e->kind = r->noapprox ? 2 : 1;
+        e->t = Q.t;
+        e->chi = r->chi;
+        e->samples = Q.samples;
+        e->bins = Q.bins;
+        e->ns = e->kind == 1 ? (int64_t)Q.samples * Q.bins : r->chi;
+        e->nstabs = P.nstabs;
+        for (int i = 0; i < P.nstabs; i++) {
+            e->pm[i] = phase_m(P.phase[i]);
+            e->pz[i] = P.zs[i];
+            e->px[i] = P.xs[i];
+        }
+        e->id0 = philox_next;
+        if (e->kind == 1) philox_next += (uint64_t)e->ns;
+        e->val.assign(e->kind == 1 ? (size_t)e->ns : 2 * (size_t)e->ns, 0.0);
+        if (e->kind == 2) e->live.assign((size_t)e->ns, 0);
+        r->pending++;
+        r->ev[w] = std::move(e);
+    }
+    for (int w = 0; w < 2; w++)
+        if (r->ev[w]) {
+            if (r->ev[w]->ns == 0) finish_eval(r->ev[w].get());
+            else active_.push_back(r->ev[w].get());
+        }
+    return 0;
+}
+
+bool Engine::eval_ready(const Eval* e) const {
+    if (e->next >= e->ns) return false;
+    // rand() draws: H' continues G''s stream, so its states are drawn after all of G''s
+    if (e->which == 1 && e->kind == 1 && e->q->q.rng == CSIM_RNG_LIBC && e->q->ev[0] && e->q->ev[0]->kind == 1 &&
+        e->q->ev[0]->next < e->q->ev[0]->ns)
+        return false;
+    return true;
+}
+
+bool Engine::schedulable() const {
+    for (const Eval* e : active_)
+        if (eval_ready(e)) return true;
+    return false;
+}
+
+int Engine::launch_round() {
+    csim_ctx* const ctx = ctx_;  // for CK
+    RoundSet& rs = sets_[next_set_];
+    next_set_ ^= 1;
+    rs.slots.clear();
+    rs.pairs = 0;
+    // pick states: a fair share per evaluation first, then first come first served
+    int nready = 0;
+    for (Eval* e : active_) nready += eval_ready(e) ? 1 : 0;
+    const int64_t share = std::max<int64_t>(1, round_pairs_ / std::max(1, nready));
+    auto cost = [](const Eval* e) { return e->kind == 1 ? e->chi : e->chi - e->next; };
+    for (int pass = 0; pass < 2; pass++) {
+        for (Eval* e : active_) {
+            int64_t mine = 0;
+            while (eval_ready(e) && (int64_t)rs.slots.size() < round_states_) {
+                const int64_t c = cost(e);
+                if (!rs.slots.empty() && rs.pairs + c > round_pairs_) break;
+                if (pass == 0 && mine > 0 && mine + c > share) break;
+                rs.slots.push_back(Slot{e, e->next});
+                e->q->inflight++;
+                e->next++;
+                rs.pairs += c;
+                mine += c;
+            }
+        }
+    }
+    const int64_t ns = (int64_t)rs.slots.size();
+    if (ns == 0) return 0;
+
+    // rand() words of the sampled states, drawn in each query's own order
+    std::vector<uint32_t> words;
+    std::vector<std::pair<int64_t, int64_t>> wr(ns, {0, 0});
+    std::map<Eval*, int> evix;  // evaluations in this round -> projector block
+    int64_t nitp = 0, niw = 0;
+    const int64_t span_tp = 64 * (int64_t)per_thread_, span_w = 64;
+    int nmax_tp = 1;
+    double hcum[CSIM_MAX_QUBITS + 1];
+    int hcum_t = -1;
+    for (int64_t i = 0; i < ns; i++) {
+        Eval* e = rs.slots[i].e;
+        if (!evix.count(e)) {
+            const int ix = (int)evix.size();
+            evix[e] = ix;
+        }
+        if (e->kind == 1 && e->q->q.rng == CSIM_RNG_LIBC) {
+            if (hcum_t != e->t) {
+                cum_table(e->t, hcum);
+                hcum_t = e->t;
+            }
+            wr[i].first = (int64_t)words.size();
+            draw_state_words(e->q->lr, e->t, hcum, words);
+            wr[i].second = (int64_t)words.size();
+        }
+        const int64_t jb = e->kind == 2 ? rs.slots[i].s : 0;
+        const int64_t nj = e->chi - jb;
+        if (!e->q->exact) {
+            nitp += (nj + span_tp - 1) / span_tp;
+            nmax_tp = std::max(nmax_tp, e->t);
+        } else {
+            niw += (nj + span_w - 1) / span_w;
+        }
+    }
+    const int64_t nitems = nitp + niw;
+    // upload block: desc | proj | words | items | ranges
+    const size_t o_desc = 0;
+    const size_t o_proj = align_up(o_desc + (size_t)ns * sizeof(csim::DrawDesc));
+    const size_t o_words = align_up(o_proj + evix.size() * 192 * 8);
+    const size_t o_items = align_up(o_words + words.size() * 4);
+    const size_t o_range = align_up(o_items + (size_t)nitems * sizeof(csim::PairItem));
+    const size_t up_bytes = align_up(o_range + (size_t)ns * 16);
+    // work block: states | parts | parts diag
+    const size_t w_states = 0;
+    const size_t w_part = align_up((size_t)ns * sizeof(csim_state));
+    const size_t w_partd = align_up(w_part + (size_t)std::max<int64_t>(nitems, 1) * 64);
+    const size_t work_bytes = align_up(w_partd + (size_t)std::max<int64_t>(nitems, 1) * 64);
+    // download block: err | codes | sums | sums diag
+    rs.off_codes = 256;
+    rs.off_sum = align_up(rs.off_codes + (size_t)ns * 4);
+    rs.off_sumd = align_up(rs.off_sum + (size_t)ns * 64);
+    const size_t down_bytes = align_up(rs.off_sumd + (size_t)ns * 64);
+    if (rs.up.ensure(up_bytes) || rs.work.ensure(work_bytes) || rs.down.ensure(down_bytes) ||
+        rs.hup.ensure(up_bytes) || rs.hdown.ensure(down_bytes))
+        return fail(ctx_, CSIM_ERR_NOMEM, "round buffers (%lld states, %lld items)", (long long)ns,
+                    (long long)nitems);
+    unsigned char* hb = (unsigned char*)rs.hup.p;
+    unsigned char* db = (unsigned char*)rs.up.p;
+    unsigned char* wb = (unsigned char*)rs.work.p;
+    unsigned char* dd = (unsigned char*)rs.down.p;
+    uint64_t* hproj = (uint64_t*)(hb + o_proj);
+    for (auto& kv : evix) {
+        uint64_t* blk = hproj + 192 * kv.second;
+        memset(blk, 0, 192 * 8);
+        memcpy(blk, kv.first->pm, sizeof(int32_t) * kv.first->nstabs);
+        memcpy(blk + 64, kv.first->pz, 8 * kv.first->nstabs);
+        memcpy(blk + 128, kv.first->px, 8 * kv.first->nstabs);
+    }
+    if (!words.empty()) memcpy(hb + o_words, words.data(), words.size() * 4);
+    const uint64_t* dproj = (const uint64_t*)(db + o_proj);
+    const uint32_t* dwords = (const uint32_t*)(db + o_words);
+    csim::DrawDesc* hdesc = (csim::DrawDesc*)(hb + o_desc);
+    csim::PairItem* hitems = (csim::PairItem*)(hb + o_items);
+    int64_t* hrange = (int64_t*)(hb + o_range);
+    const double* dcum = (const double*)cum_.p;
+    const csim::GState* dstates = (const csim::GState*)(wb + w_states);
+    int64_t itp = 0, iw = nitp;
+    for (int64_t i = 0; i < ns; i++) {
+        Eval* e = rs.slots[i].e;
+        const int64_t s = rs.slots[i].s;
+        const QueryRec* r = e->q;
+        const int b = evix[e];
+        csim::DrawDesc d{};
+        d.n = e->t;
+        d.nstabs = e->nstabs;
+        d.cum = dcum + 65 * e->t;
+        d.pm = (const int32_t*)(dproj + 192 * b);
+        d.pz = dproj + 192 * b + 64;
+        d.px = dproj + 192 * b + 128;
+        if (e->kind == 2) {
+            d.mode = 2;
+            d.src = (const csim::GState*)(r->dec->phis + s);
+        } else if (r->q.rng == CSIM_RNG_LIBC) {
+            d.mode = 1;
+            d.words = dwords;
+            d.wbegin = wr[i].first;
+            d.wend = wr[i].second;
+        } else {
+            d.mode = 0;
+            d.seed = r->q.seed;
+            d.id = e->id0 + (uint64_t)s;
+        }
+        hdesc[i] = d;
+        const int64_t jb = e->kind == 2 ? s : 0;
+        const int64_t diag = e->kind == 2 ? s : -1;
+        if (!r->exact) {
+            hrange[2 * i] = itp;
+            for (int64_t j = jb; j < e->chi; j += span_tp)
+                hitems[itp++] = csim::PairItem{i, j, std::min(span_tp, e->chi - j), diag, r->dec->cw, nullptr};
+            hrange[2 * i + 1] = itp;
+        } else {
+            hrange[2 * i] = iw;
+            for (int64_t j = jb; j < e->chi; j += span_w)
+                hitems[iw++] = csim::PairItem{i, j, std::min(span_w, e->chi - j), diag, nullptr,
+                                              (const csim::GState*)r->dec->phis};
+            hrange[2 * i + 1] = iw;
+        }
+    }
+    int* derr = (int*)dd;
+    const csim::Launch L = launch_on(derr);
+    CK(cudaEventRecord(rs.ev[0], ctx_->stream));
+    CK(cudaMemcpyAsync(db, hb, up_bytes, cudaMemcpyHostToDevice, ctx_->stream));
+    CK(cudaMemsetAsync(derr, 0, 16, ctx_->stream));
+    __int128* part = (__int128*)(wb + w_part);
+    __int128* partd = (__int128*)(wb + w_partd);
+    int* dcode = (int*)(dd + rs.off_codes);
+    if (csim::launch_draw_project(L, (const csim::DrawDesc*)(db + o_desc), ns, (csim::GState*)(wb + w_states), dcode))
+        return fail(ctx_, CSIM_ERR_CUDA, "draw/project launch failed");
+    CK(cudaEventRecord(rs.ev[1], ctx_->stream));
+    const csim::PairItem* ditems = (const csim::PairItem*)(db + o_items);
+    if (csim::launch_items_tp(L, ditems, nitp, dstates, dcode, per_thread_, nmax_tp, part, partd) ||
+        csim::launch_items_warp(L, ditems + nitp, niw, dstates, dcode, part + 4 * nitp, partd + 4 * nitp))
+        return fail(ctx_, CSIM_ERR_CUDA, "pair launch failed");
+    CK(cudaEventRecord(rs.ev[2], ctx_->stream));
+    const int64_t* drange = (const int64_t*)(db + o_range);
+    if (csim::launch_reduce_slots(L, part, drange, ns, (__int128*)(dd + rs.off_sum)) ||
+        csim::launch_reduce_slots(L, partd, drange, ns, (__int128*)(dd + rs.off_sumd)))
+        return fail(ctx_, CSIM_ERR_CUDA, "reduce launch failed");
+    CK(cudaMemcpyAsync(rs.hdown.p, dd, down_bytes, cudaMemcpyDeviceToHost, ctx_->stream));
+    CK(cudaEventRecord(rs.ev[3], ctx_->stream));
+    ctx_->stats.h2d_bytes += (int64_t)up_bytes;
+    ctx_->stats.d2h_bytes += (int64_t)down_bytes;
+    inflight_.push_back(&rs);
+    rounds++;
+    return 0;
+}
+
+int Engine::complete_round() {
+    csim_ctx* const ctx = ctx_;  // for CK
+    if (inflight_.empty()) return 0;
+    RoundSet& rs = *inflight_.front();
+    inflight_.pop_front();
+    CK(cudaEventSynchronize(rs.ev[3]));
+    float a = 0, b = 0;
+    CK(cudaEventElapsedTime(&a, rs.ev[0], rs.ev[3]));
+    CK(cudaEventElapsedTime(&b, rs.ev[1], rs.ev[2]));
+    device_ms += a;
+    pair_ms += b;
+    const unsigned char* hd = (const unsigned char*)rs.hdown.p;
+    const int err = *(const int*)hd;
+    const int* code = (const int*)(hd + rs.off_codes);
+    const __int128* sum = (const __int128*)(hd + rs.off_sum);
+    const __int128* sumd = (const __int128*)(hd + rs.off_sumd);
+    if (err) {
+        fail(ctx_, CSIM_ERR_DEVICE, "kernel flagged error bits 0x%x (1 range, 2 replay, 4 expsum, 8 gamma, 16 arg)",
+             err);
+        for (const Slot& sl : rs.slots)
+            if (!sl.e->q->done) fail_query(sl.e->q, CSIM_ERR_DEVICE);
+        for (const Slot& sl : rs.slots) sl.e->q->inflight--;
+        return 0;
+    }
+    for (size_t i = 0; i < rs.slots.size(); i++) {
+        Eval* e = rs.slots[i].e;
+        const int64_t s = rs.slots[i].s;
+        e->q->inflight--;
+        if (e->q->done) continue;  // failed in an earlier round
+        const int P2 = 2 * e->t;
+        states++;
+        if (code[i] >= 0) {
+            states_live++;
+            const int64_t np = e->kind == 1 ? e->chi : e->chi - s;
+            pairs += np;
+            e->q->res.pairs += np;
+            const double pf = sqrt_half_power(code[i]);
+            double re, im;
+            if (e->kind == 1) {  // singleProjectorSample's value, innerprod.c:142
+                zomega_to_complex(&sum[4 * i], P2, &re, &im);
+                const double x = re * pf, y = im * pf;
+                e->val[s] = pow(2, e->t) * (x * x + y * y);
+            } else {  // exactProjector row s: diag + 2 Re(off), innerprod.c:187-195
+                const __int128* o = &sum[4 * i];
+                const __int128* d = &sumd[4 * i];
+                const __int128 z[4] = {d[0] + 2 * o[0], d[1] + (o[1] - o[3]), d[2], d[3] - (o[1] - o[3])};
+                zomega_to_complex(z, P2, &re, &im);
+                e->val[2 * s] = re * pf;
+                e->val[2 * s + 1] = im * pf;
+                e->live[s] = 1;
+            }
+        }
+        e->done++;
+        if (e->done == e->ns) finish_eval(e);
+    }
+    return 0;
+}
+
+void Engine::finish_eval(Eval* e) {
+    if (e->finished) return;
+    e->finished = true;
+    if (e->kind == 1) {  // multiSampledProjector, innerprod.c:64-84
+        std::vector<double> binv(e->bins);
+        for (int b = 0; b < e->bins; b++) {
+            double total = 0;
+            for (int i = 0; i < e->samples; i++) total += e->val[(size_t)b * e->samples + i];
+            binv[b] = total / e->samples;
+        }
+        if (e->bins == 1) {
+            e->value = binv[0];
+        } else {
+            qsort(binv.data(), (size_t)e->bins, sizeof(double), cmp_trunc);
+            e->value = (e->bins % 2 == 1) ? binv[(e->bins - 1) / 2] : (binv[e->bins / 2] + binv[e->bins / 2 - 1]) / 2;
+        }
+    } else {  // rows summed in row order, innerprod.c:187-198
+        double tr = 0, ti = 0;
+        for (int64_t s = 0; s < e->ns; s++)
+            if (e->live[s]) {
+                tr += e->val[2 * s];
+                ti += e->val[2 * s + 1];
+            }
+        e->value = sqrt(tr * tr + ti * ti);
+    }
+    e->val.clear();
+    e->val.shrink_to_fit();
+    active_.erase(std::remove(active_.begin(), active_.end(), e), active_.end());
+    QueryRec* r = e->q;
+    if (--r->pending == 0 && !r->done) finish_query(r);
+}
+
+void Engine::finish_query(QueryRec* r) {
+    r->res.numerator = r->host_only[0] ? r->host_value[0] : r->ev[0]->value;
+    r->res.denominator = r->host_only[1] ? r->host_value[1] : r->ev[1]->value;
+    r->res.status = CSIM_OK;
+    r->done = true;
+    if (r->dec) {
+        r->dec->refs--;
+        r->dec = nullptr;
+    }
+    finished.push_back(r);
+}
+
+void Engine::fail_query(QueryRec* r, int status) {
+    if (r->done) return;
+    r->res.status = status;
+    r->done = true;
+    for (auto& e : r->ev)
+        if (e) active_.erase(std::remove(active_.begin(), active_.end(), e.get()), active_.end());
+    if (r->dec) {
+        r->dec->refs--;
+        r->dec = nullptr;
+    }
+    finished.push_back(r);
+}
+
+// ---------------------------------------------------------------- queries in, results out
+namespace {
+
+void copy_query(const csim_query& in, QueryRec* r) {
+    r->q = in;
+    for (int w = 0; w < 2; w++) {
+        const csim_projector& P = w == 0 ? in.G : in.H;
+        csim_projector& D = w == 0 ? r->q.G : r->q.H;
+        const int n = (P.nstabs > 0 && P.nstabs <= 64 && P.phase && P.xs && P.zs) ? P.nstabs : 0;
+        r->ph[w].assign(P.phase, P.phase + n);
+        r->xs[w].assign(P.xs, P.xs + n);
+        r->zs[w].assign(P.zs, P.zs + n);
+        if (n) {
+            D.phase = r->ph[w].data();
+            D.xs = r->xs[w].data();
+            D.zs = r->zs[w].data();
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" int csim_run_queries(csim_ctx* ctx, int64_t nq, const csim_query* q, csim_query_result* r,
+                                int32_t batched) {
+    if (!ctx || nq < 0 || (nq && (!q || !r))) return fail(ctx, CSIM_ERR_ARG, "bad argument");
+    cudaSetDevice(ctx->device);
+    int first_err = CSIM_OK;
+    if (!batched) {  // one query after another through the single-query entry points
+        for (int64_t i = 0; i < nq; i++) {
+            QueryRec rec;
+            rec.ticket = i;
+            copy_query(q[i], &rec);
+            Engine plan_only(ctx, 0, 0, ctx->per_thread, 0);
+            plan_only.plan(&rec);
+            r[i] = rec.res;
+            if (rec.done) {
+                if (r[i].status && !first_err) first_err = r[i].status;
+                continue;
+            }
+            const csim_query& Q = q[i];
+            int rc;
+            int64_t pairs = 0;
+            if (rec.noapprox == 0) {
+                rc = csim_multi_sampled_projector(ctx, &Q.G, rec.L, rec.k, rec.exact, rec.norm, Q.samples, Q.bins,
+                                                  Q.rng, Q.rng == CSIM_RNG_LIBC ? (uint64_t)(uint32_t)Q.seed : Q.seed,
+                                                  &r[i].numerator);
+                pairs += ctx->stats.pairs;
+                if (rc == CSIM_OK)
+                    rc = csim_multi_sampled_projector(ctx, &Q.H, rec.L, rec.k, rec.exact, rec.norm, Q.samples, Q.bins,
+                                                      Q.rng, CSIM_SEED_CONTINUE, &r[i].denominator);
+                pairs += ctx->stats.pairs;
+            } else {
+                rc = csim_exact_projector(ctx, &Q.G, rec.L, rec.k, rec.exact, rec.norm, &r[i].numerator);
+                pairs += ctx->stats.pairs;
+                if (rc == CSIM_OK)
+                    rc = csim_exact_projector(ctx, &Q.H, rec.L, rec.k, rec.exact, rec.norm, &r[i].denominator);
+                pairs += ctx->stats.pairs;
+            }
+            r[i].pairs = pairs;
+            r[i].status = rc;
+            if (rc && !first_err) first_err = rc;
+        }
+        return first_err;
+    }
+    stats_begin(ctx);
+    Engine eng(ctx, (int64_t)1 << 28, (int64_t)1 << 16, ctx->per_thread, 0);
+    CKR(eng.init());
+    std::vector<std::unique_ptr<QueryRec>> recs(nq);
+    for (int64_t i = 0; i < nq; i++) {
+        recs[i] = std::make_unique<QueryRec>();
+        recs[i]->ticket = i;
+        copy_query(q[i], recs[i].get());
+        eng.plan(recs[i].get());
+        bool ok = false;
+        CKR(eng.admit(recs[i].get(), true, &ok));
+    }
+    while (!eng.idle()) {
+        bool launched = false;
+        if (eng.inflight() < 2 && eng.schedulable()) {
+            CKR(eng.launch_round());
+            launched = true;
+        }
+        if (eng.inflight() == 2 || (!launched && eng.inflight() > 0)) CKR(eng.complete_round());
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaGetLastError());
+    for (int64_t i = 0; i < nq; i++) {
+        r[i] = recs[i]->res;
+        if (r[i].status && !first_err) first_err = r[i].status;
+    }
+    ctx->stats.device_ms = eng.device_ms;
+    ctx->stats.pair_kernel_ms = eng.pair_ms;
+    ctx->stats.states = eng.states;
+    ctx->stats.states_live = eng.states_live;
+    ctx->stats.pairs = eng.pairs;
+    stats_end(ctx);
+    return first_err;
+}
+
+// ---------------------------------------------------------------- server
+struct csim_server {
+    csim_ctx* ctx = nullptr;
+    std::unique_ptr<Engine> eng;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<std::unique_ptr<QueryRec>> incoming;        // submitted, not yet planned
+    std::deque<QueryRec*> waiting;                         // planned, waiting for memory (worker only)
+    std::map<int64_t, std::unique_ptr<QueryRec>> tickets;  // every unreleased query
+    int64_t next_ticket = 1;
+    int64_t submitted = 0, completed = 0, failed = 0;
+    csim_server_stats snap{};  // engine counters as of the worker's last step
+    bool stop = false;
+    int worker_error = 0;
+    std::thread worker;
+
+    void run();
+};
+
+void csim_server::run() {
+    cudaSetDevice(ctx->device);
+    std::unique_lock<std::mutex> lk(mu);
+    while (true) {
+        // admit new queries (planning runs outside the lock)
+        std::deque<std::unique_ptr<QueryRec>> fresh;
+        fresh.swap(incoming);
+        lk.unlock();
+        std::vector<QueryRec*> planned;
+        for (auto& r : fresh) {
+            eng->plan(r.get());
+            planned.push_back(r.get());
+        }
+        lk.lock();
+        for (auto& r : fresh) tickets[r->ticket] = std::move(r);
+        for (QueryRec* r : planned)
+            if (!r->done) waiting.push_back(r);
+        lk.unlock();
+        int rc = 0;
+        while (!waiting.empty()) {  // first come first served while memory allows
+            QueryRec* r = waiting.front();
+            bool ok = false;
+            const bool alone = eng->idle();  // nothing else holds memory: admit regardless
+            rc = eng->admit(r, alone, &ok);
+            if (rc || !ok) break;
+            waiting.pop_front();
+        }
+        bool launched = false;
+        if (!rc && eng->inflight() < 2 && eng->schedulable()) {
+            rc = eng->launch_round();
+            launched = true;
+        }
+        if (!rc && (eng->inflight() == 2 || (!launched && eng->inflight() > 0))) rc = eng->complete_round();
+        lk.lock();
+        snap.rounds = eng->rounds;
+        snap.pairs = eng->pairs;
+        snap.resident_bytes = eng->resident_bytes();
+        snap.resident_decompositions = eng->resident_count();
+        snap.queued = (int64_t)waiting.size();
+        snap.device_ms = eng->device_ms;
+        const auto now = Clock::now();
+        for (QueryRec* r : eng->finished) {
+            r->res.latency_s = std::chrono::duration<double>(now - r->t_submit).count();
+            if (r->res.status) failed++;
+            else completed++;
+        }
+        if (!eng->finished.empty()) cv_done.notify_all();
+        eng->finished.clear();
+        if (rc) {
+            worker_error = rc;
+            stop = true;
+        }
+        if (stop) break;
+        if (eng->idle() && incoming.empty() && waiting.empty())
+            cv_work.wait(lk, [&] { return stop || !incoming.empty(); });
+    }
+    // fail what is left
+    lk.unlock();
+    cudaStreamSynchronize(ctx->stream);
+    lk.lock();
+    for (auto& kv : tickets)
+        if (!kv.second->done) {
+            kv.second->res.status = worker_error ? worker_error : CSIM_ERR_ARG;
+            kv.second->done = true;
+            failed++;
+        }
+    for (auto& r : incoming) {
+        r->res.status = worker_error ? worker_error : CSIM_ERR_ARG;
+        r->done = true;
+        failed++;
+        tickets[r->ticket] = std::move(r);
+    }
+    incoming.clear();
+    cv_done.notify_all();
+}
+
+extern "C" int csim_server_create(const csim_server_config* cfg, csim_server** out) {
+    if (!cfg || !out) return CSIM_ERR_ARG;
+    *out = nullptr;
+    csim_ctx* ctx = nullptr;
+    int rc = csim_ctx_create(cfg->device, &ctx);
+    if (rc) return rc;
+    auto s = std::make_unique<csim_server>();
+    s->ctx = ctx;
+    s->eng = std::make_unique<Engine>(ctx, cfg->round_pairs, cfg->round_states, cfg->per_thread,
+                                      cfg->hbm_budget_bytes);
+    rc = s->eng->init();
+    if (rc) {
+        s->eng.reset();
+        csim_ctx_destroy(ctx);
+        return rc;
+    }
+    s->worker = std::thread([p = s.get()] { p->run(); });
+    *out = s.release();
+    return CSIM_OK;
+}
+
+extern "C" int csim_submit(csim_server* s, const csim_query* q, int64_t* ticket) {
+    if (!s || !q || !ticket) return CSIM_ERR_ARG;
+    auto r = std::make_unique<QueryRec>();
+    copy_query(*q, r.get());
+    r->t_submit = Clock::now();
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->stop) return s->worker_error ? s->worker_error : CSIM_ERR_ARG;
+    r->ticket = s->next_ticket++;
+    *ticket = r->ticket;
+    s->incoming.push_back(std::move(r));
+    s->submitted++;
+    s->cv_work.notify_one();
+    return CSIM_OK;
+}
+
+namespace {
+
+// caller holds s->mu
+int lookup(csim_server* s, int64_t ticket, QueryRec** out) {
+    auto it = s->tickets.find(ticket);
+    if (it != s->tickets.end()) {
+        *out = it->second.get();
+        return CSIM_OK;
+    }
+    for (auto& r : s->incoming)
+        if (r->ticket == ticket) {
+            *out = r.get();
+            return CSIM_OK;
+        }
+    return CSIM_ERR_ARG;
+}
+
+}  // namespace
+
+extern "C" int csim_poll(csim_server* s, int64_t ticket, csim_query_result* out) {
+    if (!s || !out) return CSIM_ERR_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    QueryRec* r = nullptr;
+    if (lookup(s, ticket, &r)) return CSIM_ERR_ARG;
+    if (!r->done) return CSIM_PENDING;
+    *out = r->res;
+    return CSIM_OK;
+}
+
+extern "C" int csim_wait(csim_server* s, int64_t ticket, double timeout_s, csim_query_result* out) {
+    if (!s || !out) return CSIM_ERR_ARG;
+    std::unique_lock<std::mutex> lk(s->mu);
+    QueryRec* r = nullptr;
+    if (lookup(s, ticket, &r)) return CSIM_ERR_ARG;
+    auto ready = [&] {
+        QueryRec* x = nullptr;
+        return lookup(s, ticket, &x) == CSIM_OK && x->done;
+    };
+    if (timeout_s < 0) s->cv_done.wait(lk, ready);
+    else if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), ready)) return CSIM_PENDING;
+    lookup(s, ticket, &r);
+    *out = r->res;
+    return CSIM_OK;
+}
+
+extern "C" int csim_release(csim_server* s, int64_t ticket) {
+    if (!s) return CSIM_ERR_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->tickets.find(ticket);
+    if (it == s->tickets.end() || !it->second->done) return CSIM_ERR_ARG;
+    if (it->second->inflight > 0) return CSIM_PENDING;  // a failed query's states are still being read back
+    s->tickets.erase(it);
+    return CSIM_OK;
+}
+
+extern "C" int csim_server_get_stats(csim_server* s, csim_server_stats* out) {
+    if (!s || !out) return CSIM_ERR_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    *out = s->snap;
+    out->submitted = s->submitted;
+    out->completed = s->completed;
+    out->failed = s->failed;
+    out->queued += (int64_t)s->incoming.size();
+    return CSIM_OK;
+}
+
+extern "C" void csim_server_destroy(csim_server* s) {
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+        s->cv_work.notify_all();
+    }
+    if (s->worker.joinable()) s->worker.join();
+    s->eng.reset();
+    csim_ctx_destroy(s->ctx);
+    delete s;
+}

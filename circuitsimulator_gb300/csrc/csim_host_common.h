@@ -1,0 +1,338 @@
+// csim_host_common.h — host-side pieces shared by the single-query entry
+// points (csim_host.cpp) and the query engine (csim_engine.cpp): the C
+// library's rand() sequence, randomStabilizerState's tables, Z[w] -> double
+// conversion, the context with its device-buffer pool, error handling and the
+// argument checks.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/csim.h"
+#include "csim_internal.h"
+
+namespace csim_host {
+
+
+// ---------------------------------------------------------------- libc rand()
+// The C library's srand()/rand(): additive lagged-Fibonacci r_i = r_{i-3} +
+// r_{i-31} (mod 2^32) seeded by the Park–Miller recurrence (Schrage's method),
+// first 310 outputs discarded, outputs r_i >> 1 (P. Selinger, "The GLIBC
+// pseudo-random number generator").
+struct LibcRand {
+    uint32_t ring[34];
+    int idx;
+
+    LibcRand() { seed(1); }  // rand() before any srand() is seeded with 1
+
+    uint32_t step() {
+        const uint32_t v = ring[(idx + 31) % 34] + ring[(idx + 3) % 34];
+        ring[idx] = v;
+        idx = (idx + 1) % 34;
+        return v;
+    }
+    void seed(uint32_t s) {
+        int32_t word = (int32_t)(s == 0 ? 1u : s);
+        int32_t v[34];
+        v[0] = word;
+        for (int i = 1; i < 31; i++) {
+            const int64_t hi = word / 127773, lo = word % 127773;
+            word = (int32_t)(16807 * lo - 2836 * hi);
+            if (word < 0) word += 2147483647;
+            v[i] = word;
+        }
+        for (int i = 31; i < 34; i++) v[i] = v[i - 31];
+        for (int i = 0; i < 34; i++) ring[i] = (uint32_t)v[i];
+        idx = 0;
+        for (int i = 34; i < 344; i++) step();
+    }
+    int32_t next() { return (int32_t)(step() >> 1); }
+};
+
+// ---------------------------------------------------------------- helpers
+inline int popc(uint64_t x) { return __builtin_popcountll(x); }
+inline int par(uint64_t x) { return __builtin_popcountll(x) & 1; }
+inline int phase_m(int v) { return 2 * (((v / 2) % 2) & 1) + ((v % 2) & 1); }  // comms.c:23-25, innerprod.c:101-102
+
+// logeta (stabilizer.c:677-687) and the normalized cumulative table of
+// randomStabilizerState (stabilizer.c:694-716), same expressions, same libm
+inline double logeta(int d, int n) {
+    if (d == 0) return 0.;
+    double product = 0;
+    for (int a = 1; a <= d; a++) {
+        product += log2(1 - pow(2, d - n - a));
+        product -= log2(1 - pow(2, -a));
+    }
+    return (-d * (d + 1) / 2) + product;
+}
+
+inline void cum_table(int n, double* cum) {
+    double dist[CSIM_MAX_QUBITS + 1];
+    double sum = 0;
+    for (int d = 0; d <= n; d++) {
+        dist[d] = pow(2, logeta(d, n));
+        sum += dist[d];
+    }
+    for (int d = 0; d <= n; d++) dist[d] /= sum;
+    for (int i = 0; i <= n; i++) {
+        cum[i] = 0;
+        for (int d = 0; d <= i; d++) cum[i] += dist[d];
+    }
+    for (int i = 0; i <= n; i++) cum[i] /= cum[n];
+}
+
+inline uint64_t codeword(int64_t j, const uint64_t* L, int k) {
+    uint64_t x = 0;
+    for (int r = 0; r < k; r++)
+        if ((j >> (k - 1 - r)) & 1) x ^= L[r];
+    return x;
+}
+
+// The rand() words randomStabilizerState consumes for one n-qubit state, drawn
+// from `lr` in the reference's order.  The lazy shrink loop is simulated on G
+// alone to know how many random vectors are drawn (stabilizer.c:736-740).
+inline void draw_state_words(LibcRand& lr, int n, const double* cum, std::vector<uint32_t>& words) {
+    double sample;
+    do {
+        const int32_t w = lr.next();
+        words.push_back((uint32_t)w);
+        sample = 0. + (w / (2147483647 / 1.0));
+    } while (sample == 0.);
+    int d = 0;
+    for (; d <= n; d++)
+        if (sample <= cum[d]) break;
+    const int kt = n - d;
+    uint64_t G[CSIM_MAX_QUBITS];
+    for (int i = 0; i < n; i++) G[i] = 1ull << i;
+    int k = n;
+    const int bytes = (n + 7) / 8;
+    while (k > kt) {
+        uint64_t xi = 0;
+        for (int b = 0; b < bytes; b++) {
+            const int32_t w = lr.next();
+            words.push_back((uint32_t)w);
+            const int byte = w % 256;
+            for (int j = 0; j < 8; j++) {
+                const int loc = 8 * b + j;
+                if (loc < n && (byte & (0x80 >> j))) xi |= 1ull << loc;
+            }
+        }
+        int last = -1;
+        uint64_t S = 0;
+        for (int a = 0; a < k; a++)
+            if (par(G[a] & xi)) {
+                S |= 1ull << a;
+                last = a;
+            }
+        if (last < 0) continue;
+        for (int a = 0; a < k; a++)
+            if (a != last && ((S >> a) & 1)) G[a] ^= G[last];
+        std::swap(G[last], G[k - 1]);
+        k--;
+    }
+    const int64_t rest = 3 * bytes + (int64_t)k * (k - 1) / 2;
+    for (int64_t i = 0; i < rest; i++) words.push_back((uint32_t)lr.next());
+}
+
+// z0 + z1 w + z2 w^2 + z3 w^3 (w = e^{i pi/4}) times 2^{-P/2}, P even
+inline void zomega_to_complex(const __int128* z, int P, double* re, double* im) {
+    const double s = 0.70710678118654752440;
+    const double r = (double)z[0] + (double)(z[1] - z[3]) * s;
+    const double i = (double)z[2] + (double)(z[1] + z[3]) * s;
+    *re = std::ldexp(r, -P / 2);
+    *im = std::ldexp(i, -P / 2);
+}
+
+// terms per work item of the pair kernel: at most 64 items per theta
+inline int64_t chunk_for(int64_t chi) { return std::max<int64_t>(256, (chi + 63) / 64); }
+
+inline double sqrt_half_power(int c) {  // projfactor of innerprod.c:104-111: c successive *= 2^{-1/2}
+    double pf = 1;
+    const double r = pow(2, -0.5);
+    for (int i = 0; i < c; i++) pf *= r;
+    return pf;
+}
+
+}  // namespace csim_host
+
+// ---------------------------------------------------------------- context
+enum BufId {
+    kBufA, kBufB, kBufEps, kBufP, kBufM, kBufXi, kBufZeta, kBufAlpha, kBufCode, kBufWords, kBufOffsets,
+    kBufCum, kBufCodewords, kBufAcc, kBufAccDiag, kBufPhis, kBufIdx, kBufConsumed, kBufPm, kBufPz, kBufPx,
+    kBufL, kBufParts, kBufPartsDiag, kNumBufs
+};
+
+struct csim_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    int* d_err = nullptr;
+    int64_t launches = 0;
+    std::string last_error;
+    void* buf[kNumBufs + 32] = {};
+    size_t cap[kNumBufs + 32] = {};
+    csim_host::LibcRand lr;
+    uint64_t philox_seed = 0;
+    uint64_t philox_next = 0;
+    csim_stats stats = {};
+    int64_t stats_launch0 = 0;
+    int pair_kernel = 0;  // CSIM_OPT_PAIR_KERNEL
+    int per_thread = 16;  // CSIM_OPT_PER_THREAD
+    cudaEvent_t ev[4] = {};
+};
+
+namespace csim_host {
+
+inline int fail(csim_ctx* ctx, int code, const char* fmt, ...) {
+    char msg[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(msg, sizeof(msg), fmt, ap);
+    va_end(ap);
+    if (ctx) ctx->last_error = msg;
+    return code;
+}
+
+#define CK(call)                                                                                              \
+    do {                                                                                                      \
+        cudaError_t e_ = (call);                                                                              \
+        if (e_ != cudaSuccess) return fail(ctx, CSIM_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));      \
+    } while (0)
+
+#define CKR(expr)            \
+    do {                     \
+        int r_ = (expr);     \
+        if (r_ != 0) return r_; \
+    } while (0)
+
+inline int dbuf(csim_ctx* ctx, int id, size_t bytes, void** out) {
+    if (bytes == 0) bytes = 16;
+    if (ctx->cap[id] < bytes) {
+        if (ctx->buf[id]) {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(ctx->buf[id]);
+            ctx->buf[id] = nullptr;
+            ctx->cap[id] = 0;
+        }
+        size_t c = bytes + bytes / 4;
+        if (cudaMalloc(&ctx->buf[id], c) != cudaSuccess) {
+            ctx->buf[id] = nullptr;
+            return fail(ctx, CSIM_ERR_NOMEM, "cudaMalloc of %zu bytes failed", c);
+        }
+        ctx->cap[id] = c;
+    }
+    *out = ctx->buf[id];
+    return 0;
+}
+
+template <class T>
+inline int dput(csim_ctx* ctx, int id, const T* src, size_t count, T** out) {
+    void* p;
+    CKR(dbuf(ctx, id, count * sizeof(T), &p));
+    if (count) CK(cudaMemcpyAsync(p, src, count * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    ctx->stats.h2d_bytes += (int64_t)(count * sizeof(T));
+    *out = (T*)p;
+    return 0;
+}
+
+template <class T>
+inline int dget(csim_ctx* ctx, T* dst, const T* src, size_t count) {
+    if (count) CK(cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->stats.d2h_bytes += (int64_t)(count * sizeof(T));
+    return 0;
+}
+
+inline void stats_begin(csim_ctx* ctx) {
+    ctx->stats = csim_stats{};
+    ctx->stats_launch0 = ctx->launches;
+}
+
+// adds the event-timed spans of one batch: ev0..ev3 = start, pair kernel start, pair kernel end, end
+inline int stats_batch(csim_ctx* ctx) {
+    float a = 0, b = 0;
+    CK(cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[3]));
+    CK(cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]));
+    ctx->stats.device_ms += a;
+    ctx->stats.pair_kernel_ms += b;
+    return 0;
+}
+
+inline void stats_end(csim_ctx* ctx) { ctx->stats.kernels = ctx->launches - ctx->stats_launch0; }
+
+inline csim::Launch launch_of(csim_ctx* ctx) { return csim::Launch{ctx->stream, ctx->d_err, &ctx->launches, ctx->num_sms}; }
+
+// waits for the stream, then turns device error flags into a status
+inline int finish(csim_ctx* ctx) {
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaGetLastError());
+    if (h) {
+        CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        return fail(ctx, CSIM_ERR_DEVICE, "kernel flagged error bits 0x%x (1 range, 2 replay, 4 expsum, 8 gamma, 16 arg)",
+                    h);
+    }
+    return 0;
+}
+
+inline int check_states(csim_ctx* ctx, const csim_state* s, int64_t count, int* nr_out, int n_expect = -1) {
+    int nmax = 0;
+    for (int64_t i = 0; i < count; i++) {
+        const int n = s[i].n, k = s[i].k;
+        if (n < 1 || n > CSIM_MAX_QUBITS || k < 0 || k > n)
+            return fail(ctx, CSIM_ERR_ARG, "state %lld: n=%d k=%d out of range", (long long)i, n, k);
+        if (n_expect > 0 && n != n_expect)
+            return fail(ctx, CSIM_ERR_ARG, "state %lld: n=%d, expected %d", (long long)i, n, n_expect);
+        nmax = std::max(nmax, n);
+    }
+    *nr_out = nmax > 32 ? 2 : 1;
+    return 0;
+}
+
+constexpr int64_t kBatch = 1 << 18;  // states per device round trip in the batched primitives
+
+
+inline int check_projector(csim_ctx* ctx, const csim_projector* P) {
+    if (!P || P->nstabs < 0 || P->nqubits < 0 || P->nqubits > CSIM_MAX_QUBITS)
+        return fail(ctx, CSIM_ERR_ARG, "bad projector");
+    if (P->nstabs > 0 && (!P->phase || !P->xs || !P->zs)) return fail(ctx, CSIM_ERR_ARG, "bad projector arrays");
+    return 0;
+}
+
+inline int check_code(csim_ctx* ctx, int t, int exact, const uint64_t* L, int k) {
+    if (t < 1 || t > CSIM_MAX_QUBITS) return fail(ctx, CSIM_ERR_ARG, "t=%d out of range 1..64", t);
+    if (!exact) {
+        if (!L || k < 0 || k > 40) return fail(ctx, CSIM_ERR_ARG, "k=%d out of range 0..40", k);
+        const uint64_t tm = t >= 64 ? ~0ull : ((1ull << t) - 1);
+        for (int r = 0; r < k; r++)
+            if (L[r] & ~tm) return fail(ctx, CSIM_ERR_ARG, "row %d of L has bits beyond t", r);
+    } else if ((t + 1) / 2 > 40) {
+        return fail(ctx, CSIM_ERR_ARG, "exact decomposition of t=%d is too large", t);
+    }
+    return 0;
+}
+
+inline double clifford_sum(const csim_projector* P) {  // innerprod.c:52-62
+    double sum = 1;
+    for (int i = 0; i < P->nstabs; i++) {
+        const double ph = (double)phase_m(P->phase[i]);
+        if (ph == 0) sum += 1;
+        if (ph == 2) sum -= 1;
+    }
+    return sum;
+}
+
+inline int cmp_trunc(const void* a, const void* b) {  // innerprod.c:17-19
+    return (int)(*(const double*)a - *(const double*)b);
+}
+
+}  // namespace csim_host

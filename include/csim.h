@@ -220,6 +220,7 @@ typedef struct csim_query_result {
     int32_t status;                /* CSIM_OK or this query's error        */
     int32_t exact, k, noapprox;    /* decomposition and estimator used     */
     int64_t pairs;                 /* inner products computed              */
+    double latency_s;              /* server: submit -> result; else 0     */
 } csim_query_result;
 
 /* Runs nq queries, each exactly as the backend process would (decompose, the
@@ -230,6 +231,49 @@ typedef struct csim_query_result {
  * own seed, so both modes give the same results.  Returns the first error;
  * per-query status is in r[i].status. */
 int csim_run_queries(csim_ctx *ctx, int64_t nq, const csim_query *q, csim_query_result *r, int32_t batched);
+
+/* ------------------------------------------------------------- serving */
+
+/* A query server on one GPU, replacing one backend process per query
+ * (libcirc/probability.py:237-244).  A worker thread runs rounds: each round
+ * takes the next states of every admitted query, up to round_pairs inner
+ * products, and runs them in shared launches while the host prepares the next
+ * round.  Queries submitted while others are on the GPU join the next round
+ * once their decomposition fits the device-memory budget; decompositions
+ * (codeword tables, term states) stay resident and are shared by queries with
+ * the same t and code.  Results are the same as csim_run_queries gives. */
+typedef struct csim_server csim_server;
+
+typedef struct csim_server_config {
+    int32_t device;
+    int32_t per_thread;           /* terms per thread per work item (0: 16)    */
+    int64_t hbm_budget_bytes;     /* resident decompositions + round buffers   */
+    int64_t round_pairs;          /* inner products per round (0: 2^26)        */
+    int64_t round_states;         /* states per round (0: 2^16)                */
+} csim_server_config;
+
+typedef struct csim_server_stats {
+    int64_t submitted, completed, failed, rounds, pairs;
+    int64_t resident_bytes, resident_decompositions, queued;
+    double device_ms;             /* event-timed device work of all rounds     */
+} csim_server_stats;
+
+#define CSIM_PENDING 1            /* csim_poll: not finished yet               */
+
+int csim_server_create(const csim_server_config *cfg, csim_server **out);
+/* Copies the query (projector rows included) and returns its ticket. */
+int csim_submit(csim_server *s, const csim_query *q, int64_t *ticket);
+/* CSIM_OK with *out filled once the query is done, CSIM_PENDING before that;
+ * a finished ticket can be polled again until csim_release. */
+int csim_poll(csim_server *s, int64_t ticket, csim_query_result *out);
+/* Waits up to timeout_s seconds (< 0: no limit); CSIM_PENDING on timeout. */
+int csim_wait(csim_server *s, int64_t ticket, double timeout_s, csim_query_result *out);
+/* Frees a finished ticket; CSIM_PENDING while a failed query's states are
+ * still in a round on the device. */
+int csim_release(csim_server *s, int64_t ticket);
+int csim_server_get_stats(csim_server *s, csim_server_stats *out);
+/* Stops the worker after the rounds in flight; unfinished queries fail. */
+void csim_server_destroy(csim_server *s);
 
 /* The sampler above for terms of |L> (exact == 0) with CSIM_RNG_PHILOX and an
  * explicit seed, for callers that must not allocate device memory: a program

@@ -64,20 +64,29 @@ def test_no_device_is_reported_not_faked(lib):
 
 
 def test_query_struct_layout_matches_header(tmp_path):
-    """csim_query / csim_query_result as gcc lays them out == the ctypes binding."""
+    """The query, result and server structs as gcc lays them out == the ctypes binding."""
     import ctypes
     import subprocess
 
+    fields = [("csim_query", backend._Query, ["G", "H", "seed"]),
+              ("csim_query_result", backend._QueryResult, ["pairs", "latency_s"]),
+              ("csim_server_config", backend._ServerConfig, ["hbm_budget_bytes", "round_states"]),
+              ("csim_server_stats", backend._ServerStats, ["queued", "device_ms"])]
+    exprs = []
+    want = []
+    for cname, cls, names in fields:
+        exprs.append("sizeof(%s)" % cname)
+        want.append(ctypes.sizeof(cls))
+        for nm in names:
+            exprs.append("offsetof(%s, %s)" % (cname, nm))
+            want.append(getattr(cls, nm).offset)
     src = tmp_path / "layout.c"
-    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "csim.h"\n'
-                   'int main(void) { printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(csim_query), '
-                   'offsetof(csim_query, G), offsetof(csim_query, H), offsetof(csim_query, seed), '
-                   'sizeof(csim_query_result), offsetof(csim_query_result, pairs)); return 0; }\n')
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "csim.h"\nint main(void) {\n' +
+                   "".join('printf("%%zu\\n", (size_t)%s);\n' % e for e in exprs) + "return 0; }\n")
     exe = tmp_path / "layout"
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
-    Q, R = backend._Query, backend._QueryResult
-    assert got == [ctypes.sizeof(Q), Q.G.offset, Q.H.offset, Q.seed.offset, ctypes.sizeof(R), R.pairs.offset]
+    assert got == want
 
 
 def test_parse_protocol_reads_the_e2e_inputs():

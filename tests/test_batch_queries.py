@@ -106,3 +106,103 @@ def test_bad_query_fails_alone(be):
 
 def test_empty_batch(be):
     assert be.run_queries([], batched=True) == []
+
+
+def test_empty_numerator_projector_seeds_the_denominator(be):
+    """G' empty, H' sampled: H' draws from the query's fresh seed in both modes
+    (probability.c seeds rand() before either projector)."""
+    rs = np.random.RandomState(5)
+    qs = []
+    for i, rng in enumerate((backend.RNG_LIBC, backend.RNG_PHILOX)):
+        t = 9
+        h = random_projector_rows(rs, t, 3)
+        qs.append({"cfg": _cfg(t, exact=0, k=4, samples=6, bins=1), "projs": [([], [], [], t), (*h, t)],
+                   "seed": 77 + i, "rng": rng})
+    other = mixed_queries(seed=19, count=3)
+    plain_first = be.run_queries(other + qs, batched=False)[-2:]
+    plain_alone = be.run_queries(qs, batched=False)
+    batched = be.run_queries(qs, batched=True)
+    assert [_key(r) for r in plain_first] == [_key(r) for r in plain_alone] == [_key(r) for r in batched]
+
+
+def test_round_splitting_does_not_change_results():
+    """Tiny rounds (many per query) give the same results as one big round."""
+    qs = mixed_queries(seed=23, count=10)
+    ref = backend.Backend(0).run_queries(qs, batched=True)
+    srv = backend.Server(0, round_pairs=1 << 8, round_states=16)
+    try:
+        tickets = [srv.submit(q) for q in qs]
+        res = [srv.wait(t, timeout=300) for t in tickets]
+        st = srv.stats()
+    finally:
+        srv.close()
+    assert [_key(r) for r in res] == [_key(r) for r in ref]
+    assert st["rounds"] > len(qs)
+    assert st["completed"] == len(qs)
+
+
+def test_server_mix_equals_alone_with_staggered_arrivals():
+    """Queries submitted from several threads while others are on the GPU give
+    the same results as each query run alone."""
+    import threading
+    import time
+
+    qs = mixed_queries(seed=29, count=18)
+    alone = []
+    b = backend.Backend(0)
+    for q in qs:
+        alone.append(b.run_queries([q], batched=True)[0])
+    b.close()
+    srv = backend.Server(0, round_pairs=1 << 18)
+    tickets = [None] * len(qs)
+    try:
+        def client(idx):
+            for i in idx:
+                tickets[i] = srv.submit(qs[i])
+                time.sleep(0.002 * (i % 3))
+
+        th = [threading.Thread(target=client, args=(list(range(j, len(qs), 3)),)) for j in range(3)]
+        for x in th:
+            x.start()
+        for x in th:
+            x.join()
+        res = [srv.wait(t, timeout=300) for t in tickets]
+        for t in tickets:
+            assert srv.release(t) == 0
+        st = srv.stats()
+    finally:
+        srv.close()
+    for i, (a, r) in enumerate(zip(alone, res)):
+        assert _key(a) == _key(r), i
+        assert r["latency_s"] > 0
+    assert st["completed"] == len(qs) and st["failed"] == 0
+
+
+def test_server_memory_budget_admits_in_turn():
+    """A budget below two decompositions: queries wait for memory, unused
+    decompositions are evicted, results are unchanged."""
+    qs = [q for q in mixed_queries(seed=31, count=16) if q["cfg"]["t"] >= 17][:6]
+    ref = backend.Backend(0).run_queries(qs, batched=True)
+    srv = backend.Server(0, hbm_budget_bytes=1 << 16)
+    try:
+        tickets = [srv.submit(q) for q in qs]
+        res = [srv.wait(t, timeout=300) for t in tickets]
+        st = srv.stats()
+    finally:
+        srv.close()
+    assert [_key(r) for r in res] == [_key(r) for r in ref]
+    assert st["resident_bytes"] <= (1 << 16) + (1 << 21)
+
+
+def test_server_bad_query_fails_alone():
+    qs = mixed_queries(seed=37, count=3)
+    bad = dict(qs[1])
+    bad["cfg"] = dict(bad["cfg"], t=70)
+    srv = backend.Server(0)
+    try:
+        tickets = [srv.submit(q) for q in (qs[0], bad, qs[2])]
+        res = [srv.wait(t, timeout=300) for t in tickets]
+    finally:
+        srv.close()
+    assert res[1]["status"] == -1
+    assert res[0]["status"] == 0 and res[2]["status"] == 0
