@@ -20,8 +20,13 @@ LIB = os.path.join(PKG, "libcsimgpu.so")
 EXE = os.path.join(PKG, "gpubackend")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-I" + os.path.join(ROOT, "include")]
-SOURCES = ["csim_kernels.cu", "csim_terms_tp.cu", "csim_static.cu", "csim_batch_kernels.cu", "csim_host.cpp", "csim_engine.cpp", "csim_backend.cpp"]
+# Host code keeps every double rounding explicit (no fused multiply-add
+# contraction, which gcc does by default on aarch64), so the estimators give
+# the same bits on x86 and Arm hosts and in every code path.
+NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
+                  "-I" + os.path.join(ROOT, "include")]
+SOURCES = ["csim_kernels.cu", "csim_terms_tp.cu", "csim_static.cu", "csim_batch_kernels.cu", "csim_host.cpp",
+           "csim_engine.cpp", "csim_backend.cpp"]
 
 
 def _nvcc():

@@ -44,6 +44,8 @@ struct CodeDesc {
 };
 
 int launch_draw_project(const Launch& L, const DrawDesc* desc, int64_t count, GState* out, int* code);
+// resident blocks per SM of k_items_tp launched for states of up to nmax qubits
+int items_tp_occupancy(int nmax);
 int launch_items_tp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,
                     int per_thread, int nmax, __int128* part, __int128* part_diag);
 int launch_items_warp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,

@@ -134,6 +134,7 @@ __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_
             for (int r = 0; r < sh.k; r++) asym |= ((sh.pJ[tid] >> r) & 1ull) != ((sh.pJ[r] >> tid) & 1ull);
         asym = __syncthreads_or(asym) != 0;
         __int128 z[4] = {0, 0, 0, 0}, zd[4] = {0, 0, 0, 0};
+        int deps = 0, dp = 0, dm = 0;  // the diagonal pair, summed apart after the loop
         const int n = sh.n;
         if (n > nmax || asym) e |= kErrArg;
         if (sh.live && !asym && n >= 1 && n <= nmax) {
@@ -150,9 +151,15 @@ __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_
                 pc::pair_l(valid, n, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ, sh.pGT, x, sJ + 2 * tid, sGT + tid, kTPB,
                            eps, pp, mm, e);
                 if (!valid) continue;
-                if (j == it.diag) pc::zacc(zd, eps, pp, mm, P, e);
-                else pc::zacc(z, eps, pp, mm, P, e);
+                pc::zacc(z, eps, pp, mm, P, e);
+                if (j == it.diag) {
+                    deps = eps;
+                    dp = pp;
+                    dm = mm;
+                }
             }
+            pc::zacc(zd, deps, dp, dm, P, e);
+            for (int q = 0; q < 4; q++) z[q] -= zd[q];
         }
         for (int q = 0; q < 4; q++)
             for (int o = 16; o > 0; o >>= 1) {
@@ -255,6 +262,17 @@ int launch_draw_project(const Launch& L, const DrawDesc* desc, int64_t count, GS
     k_draw_project<<<(int)blocks, 256, 0, L.stream>>>(desc, count, out, code, L.d_err);
     (*L.launches)++;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int items_tp_occupancy(int nmax) {
+    if (nmax < 1 || nmax > 64) return -1;
+    if (cudaFuncSetAttribute(k_items_tp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)items_tp_smem(64)) !=
+        cudaSuccess)
+        return -1;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_items_tp, kTPB, items_tp_smem(nmax)) != cudaSuccess)
+        return -1;
+    return per_sm;
 }
 
 int launch_items_tp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,

@@ -44,6 +44,9 @@ using Clock = std::chrono::steady_clock;
 constexpr size_t kAlign = 256;
 inline size_t align_up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
 
+// at most one thread-per-pair launch per t
+constexpr int kBuckets = CSIM_MAX_QUBITS;
+
 // device memory that grows on demand (contents are not kept)
 struct DevBuf {
     void* p = nullptr;
@@ -208,6 +211,19 @@ class Engine {
         for (int t = 1; t <= CSIM_MAX_QUBITS; t++) cum_table(t, &cum[65 * t]);
         if (cum_.ensure(cum.size() * 8)) return fail(ctx_, CSIM_ERR_NOMEM, "cum table");
         CK(cudaMemcpy(cum_.p, cum.data(), cum.size() * 8, cudaMemcpyHostToDevice));
+        // t buckets of the thread-per-pair launches: consecutive t with the same
+        // resident blocks per SM share a launch sized for the bucket's largest t,
+        // so no t runs at a lower occupancy than a launch of its own would give
+        int occ_prev = -1;
+        nbuckets_ = 0;
+        for (int t = 1; t <= CSIM_MAX_QUBITS; t++) {
+            const int occ = csim::items_tp_occupancy(t);
+            if (occ <= 0) return fail(ctx_, CSIM_ERR_CUDA, "occupancy query failed");
+            if (occ != occ_prev) nbuckets_++;
+            occ_prev = occ;
+            bucket_of_[t] = nbuckets_ - 1;
+            bucket_hi_[nbuckets_ - 1] = t;
+        }
         return 0;
     }
 
@@ -220,6 +236,7 @@ class Engine {
     int launch_round();
     int complete_round();
     int inflight() const { return (int)inflight_.size(); }
+    int per_thread() const { return per_thread_; }
     bool idle() const { return inflight_.empty() && !schedulable(); }
 
     // finished queries (the caller collects them)
@@ -243,6 +260,9 @@ class Engine {
     std::deque<RoundSet*> inflight_;
     DevBuf cum_, iota_;
     int64_t iota_n_ = 0;
+    int bucket_of_[CSIM_MAX_QUBITS + 1] = {0};
+    int bucket_hi_[kBuckets] = {0};
+    int nbuckets_ = 0;
 
     csim::Launch launch_on(int* d_err) { return csim::Launch{ctx_->stream, d_err, &ctx_->launches, ctx_->num_sms}; }
     int ensure_decomp(QueryRec* r, bool need_phis, bool force, Decomp** out);
@@ -498,9 +518,11 @@ int Engine::launch_round() {
     std::vector<uint32_t> words;
     std::vector<std::pair<int64_t, int64_t>> wr(ns, {0, 0});
     std::map<Eval*, int> evix;  // evaluations in this round -> projector block
-    int64_t nitp = 0, niw = 0;
+    // thread-per-pair items are grouped by t bucket: each bucket's launch sizes
+    // its shared memory for that bucket's largest t, not the round's
+    int64_t nbucket[kBuckets] = {0};
+    int64_t niw = 0;
     const int64_t span_tp = 64 * (int64_t)per_thread_, span_w = 64;
-    int nmax_tp = 1;
     double hcum[CSIM_MAX_QUBITS + 1];
     int hcum_t = -1;
     for (int64_t i = 0; i < ns; i++) {
@@ -521,12 +543,15 @@ int Engine::launch_round() {
         const int64_t jb = e->kind == 2 ? rs.slots[i].s : 0;
         const int64_t nj = e->chi - jb;
         if (!e->q->exact) {
-            nitp += (nj + span_tp - 1) / span_tp;
-            nmax_tp = std::max(nmax_tp, e->t);
+            nbucket[bucket_of_[e->t]] += (nj + span_tp - 1) / span_tp;
         } else {
             niw += (nj + span_w - 1) / span_w;
         }
     }
+    int64_t bstart[kBuckets + 1];
+    bstart[0] = 0;
+    for (int b = 0; b < kBuckets; b++) bstart[b + 1] = bstart[b] + nbucket[b];
+    const int64_t nitp = bstart[kBuckets];
     const int64_t nitems = nitp + niw;
     // upload block: desc | proj | words | items | ranges
     const size_t o_desc = 0;
@@ -569,7 +594,9 @@ int Engine::launch_round() {
     int64_t* hrange = (int64_t*)(hb + o_range);
     const double* dcum = (const double*)cum_.p;
     const csim::GState* dstates = (const csim::GState*)(wb + w_states);
-    int64_t itp = 0, iw = nitp;
+    int64_t cur[kBuckets];
+    for (int b = 0; b < kBuckets; b++) cur[b] = bstart[b];
+    int64_t iw = nitp;
     for (int64_t i = 0; i < ns; i++) {
         Eval* e = rs.slots[i].e;
         const int64_t s = rs.slots[i].s;
@@ -599,10 +626,11 @@ int Engine::launch_round() {
         const int64_t jb = e->kind == 2 ? s : 0;
         const int64_t diag = e->kind == 2 ? s : -1;
         if (!r->exact) {
-            hrange[2 * i] = itp;
+            int64_t& c = cur[bucket_of_[e->t]];
+            hrange[2 * i] = c;
             for (int64_t j = jb; j < e->chi; j += span_tp)
-                hitems[itp++] = csim::PairItem{i, j, std::min(span_tp, e->chi - j), diag, r->dec->cw, nullptr};
-            hrange[2 * i + 1] = itp;
+                hitems[c++] = csim::PairItem{i, j, std::min(span_tp, e->chi - j), diag, r->dec->cw, nullptr};
+            hrange[2 * i + 1] = c;
         } else {
             hrange[2 * i] = iw;
             for (int64_t j = jb; j < e->chi; j += span_w)
@@ -623,8 +651,11 @@ int Engine::launch_round() {
         return fail(ctx_, CSIM_ERR_CUDA, "draw/project launch failed");
     CK(cudaEventRecord(rs.ev[1], ctx_->stream));
     const csim::PairItem* ditems = (const csim::PairItem*)(db + o_items);
-    if (csim::launch_items_tp(L, ditems, nitp, dstates, dcode, per_thread_, nmax_tp, part, partd) ||
-        csim::launch_items_warp(L, ditems + nitp, niw, dstates, dcode, part + 4 * nitp, partd + 4 * nitp))
+    for (int b = 0; b < kBuckets; b++)
+        if (nbucket[b] && csim::launch_items_tp(L, ditems + bstart[b], nbucket[b], dstates, dcode, per_thread_,
+                                                bucket_hi_[b], part + 4 * bstart[b], partd + 4 * bstart[b]))
+            return fail(ctx_, CSIM_ERR_CUDA, "pair launch failed");
+    if (csim::launch_items_warp(L, ditems + nitp, niw, dstates, dcode, part + 4 * nitp, partd + 4 * nitp))
         return fail(ctx_, CSIM_ERR_CUDA, "pair launch failed");
     CK(cudaEventRecord(rs.ev[2], ctx_->stream));
     const int64_t* drange = (const int64_t*)(db + o_range);
@@ -820,39 +851,63 @@ extern "C" int csim_run_queries(csim_ctx* ctx, int64_t nq, const csim_query* q, 
         return first_err;
     }
     stats_begin(ctx);
-    Engine eng(ctx, (int64_t)1 << 28, (int64_t)1 << 16, ctx->per_thread, 0);
-    CKR(eng.init());
+    if (!ctx->engine || ctx->engine->per_thread() != ctx->per_thread) {
+        if (ctx->engine) engine_free(ctx->engine);
+        ctx->engine = new Engine(ctx, (int64_t)1 << 28, (int64_t)1 << 16, ctx->per_thread, 0);
+        const int rc = ctx->engine->init();
+        if (rc) {
+            engine_free(ctx->engine);
+            ctx->engine = nullptr;
+            return rc;
+        }
+    }
+    Engine& eng = *ctx->engine;
+    const int64_t rounds0 = eng.rounds, pairs0 = eng.pairs, states0 = eng.states, live0 = eng.states_live;
+    const double dev0 = eng.device_ms, pair0 = eng.pair_ms;
+    eng.finished.clear();
     std::vector<std::unique_ptr<QueryRec>> recs(nq);
+    // on a failure the engine may still point at this call's queries: drop it
+    auto abandon = [&](int rc) {
+        cudaStreamSynchronize(ctx->stream);
+        engine_free(ctx->engine);
+        ctx->engine = nullptr;
+        return rc;
+    };
     for (int64_t i = 0; i < nq; i++) {
         recs[i] = std::make_unique<QueryRec>();
         recs[i]->ticket = i;
         copy_query(q[i], recs[i].get());
         eng.plan(recs[i].get());
         bool ok = false;
-        CKR(eng.admit(recs[i].get(), true, &ok));
+        if (const int rc = eng.admit(recs[i].get(), true, &ok)) return abandon(rc);
     }
     while (!eng.idle()) {
         bool launched = false;
         if (eng.inflight() < 2 && eng.schedulable()) {
-            CKR(eng.launch_round());
+            if (const int rc = eng.launch_round()) return abandon(rc);
             launched = true;
         }
-        if (eng.inflight() == 2 || (!launched && eng.inflight() > 0)) CKR(eng.complete_round());
+        if (eng.inflight() == 2 || (!launched && eng.inflight() > 0))
+            if (const int rc = eng.complete_round()) return abandon(rc);
     }
-    CK(cudaStreamSynchronize(ctx->stream));
-    CK(cudaGetLastError());
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess)
+        return abandon(fail(ctx, CSIM_ERR_CUDA, "stream failed after the last round"));
     for (int64_t i = 0; i < nq; i++) {
         r[i] = recs[i]->res;
         if (r[i].status && !first_err) first_err = r[i].status;
     }
-    ctx->stats.device_ms = eng.device_ms;
-    ctx->stats.pair_kernel_ms = eng.pair_ms;
-    ctx->stats.states = eng.states;
-    ctx->stats.states_live = eng.states_live;
-    ctx->stats.pairs = eng.pairs;
+    eng.finished.clear();
+    (void)rounds0;
+    ctx->stats.device_ms = eng.device_ms - dev0;
+    ctx->stats.pair_kernel_ms = eng.pair_ms - pair0;
+    ctx->stats.states = eng.states - states0;
+    ctx->stats.states_live = eng.states_live - live0;
+    ctx->stats.pairs = eng.pairs - pairs0;
     stats_end(ctx);
     return first_err;
 }
+
+void engine_free(Engine* engine) { delete engine; }
 
 // ---------------------------------------------------------------- server
 struct csim_server {

@@ -47,6 +47,12 @@ extern "C" int csim_ctx_create(int device, csim_ctx** out) {
 
 extern "C" void csim_ctx_destroy(csim_ctx* ctx) {
     if (!ctx) return;
+    if (ctx->engine) {
+        cudaSetDevice(ctx->device);
+        engine_free(ctx->engine);
+        ctx->engine = nullptr;
+    }
+    if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (int i = 0; i < kNumBufs + 32; i++)

@@ -170,6 +170,9 @@ enum BufId {
     kBufL, kBufParts, kBufPartsDiag, kNumBufs
 };
 
+class Engine;                     // csim_engine.cpp: the batched query engine
+void engine_free(Engine* engine);  // releases it and its device memory
+
 struct csim_ctx {
     int device = 0;
     int num_sms = 0;
@@ -187,6 +190,7 @@ struct csim_ctx {
     int pair_kernel = 0;  // CSIM_OPT_PAIR_KERNEL
     int per_thread = 16;  // CSIM_OPT_PER_THREAD
     cudaEvent_t ev[4] = {};
+    Engine* engine = nullptr;  // created by the first batched csim_run_queries
 };
 
 namespace csim_host {
