@@ -12,6 +12,10 @@ protocol file tests/golden/workload_c2.txt.
   e2e    pairs per second of wall time through the C ABI with host buffers and
          the reference's own rand() draws (host word generation, uploads and
          result reads inside the timed region)
+  batch  batched vs plain queries/s on the light queries of the c3 workload
+         (tests/golden/workload_c3.json.gz): the same queries and draws through
+         csim_run_queries in shared launches and one at a time, results checked
+         bit-identical
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 Under torchrun each rank draws its own states (weak scaling); rank 0 prints.
@@ -247,7 +251,7 @@ def run_ours(args, rank, world, local_rank):
     kernel_rate = (pairs / world) / (pair_ms / 1e3)  # pairs/s of the pair kernel alone (rank 0 share)
     achieved = kernel_rate * per_pair / 1e9 if per_pair else None
     peak = alu_peak_gops(props.multi_processor_count, clk.get("sm_max_mhz") or 2070.0)
-    roofline = {"bound": "alu", "kernel": "k_terms<2,0> (theta x prepL term pairs)",
+    roofline = {"bound": "alu", "kernel": "k_terms_tp (theta x prepL term pairs, thread per pair)",
                 "achieved": achieved, "peak": peak, "unit": "G packed row-ops/s",
                 "frac": (achieved / peak) if achieved else None,
                 "traffic": dram_bytes_per_launch(samples, k),
@@ -272,12 +276,71 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clk,
         "gpu_launches": launches,
     }
+    if world == 1 and not args.no_batch:
+        out["batch"] = batch_compare(gpu)
     if world == 1 and not args.no_cpu_baseline:
         try:
             out["cpu_baseline"] = cpu_baseline(cfg, projs, k, L)
         except Exception as e:  # the baseline never decides the run
             out["cpu_baseline"] = {"value": None, "unit": UNIT, "error": str(e)}
     return out
+
+
+C3_WORKLOAD = os.path.join(ROOT, "tests", "golden", "workload_c3.json.gz")
+C3_LIGHT_PAIRS = 1 << 26
+
+
+def c3_queries(light=True):
+    """The batched-query workload (tests/golden/workload_c3.json.gz, 256 queries,
+    t ~ U[8, 60], relative error 0.05).  light=True keeps the queries of at most
+    2^26 inner products, the ones too small to fill the GPU on their own."""
+    import gzip
+
+    from circuitsimulator_gb300 import backend
+
+    with gzip.open(C3_WORKLOAD, "rt") as f:
+        recs = json.load(f)
+    out = []
+    for q in recs:
+        cfg, projs = backend.parse_protocol(q["input"])
+        t, k, ex = cfg["t"], cfg["k"], cfg["exact"]
+        chi = 2 ** ((t + 1) // 2) if ex else 2 ** k
+        na = cfg["noapprox"] or (not cfg["forceSample"] and cfg["samples"] * cfg["bins"] * 2 > chi - 1)
+        pairs = sum(chi * (chi + 1) // 2 if na else cfg["samples"] * cfg["bins"] * chi
+                    for p in projs if len(p[0]) > 0)
+        if light and pairs > C3_LIGHT_PAIRS:
+            continue
+        out.append({"cfg": cfg, "projs": projs, "seed": q["seed"], "rng": backend.RNG_PHILOX})
+    return out, len(recs)
+
+
+def batch_compare(gpu, reps=3):
+    """Batched vs plain queries/s on the light c3 queries: the same queries, the
+    same draws, results checked identical.  Plain = one query after another
+    through the single-query entry points; batched = csim_run_queries."""
+    qs, total = c3_queries(light=True)
+    gpu.run_queries(qs[:4], batched=True)
+    gpu.run_queries(qs[:4], batched=False)
+    tp, tb = [], []
+    same = True
+    pairs = 0
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        rp = gpu.run_queries(qs, batched=False)
+        t1 = time.perf_counter()
+        rb = gpu.run_queries(qs, batched=True)
+        t2 = time.perf_counter()
+        tp.append(t1 - t0)
+        tb.append(t2 - t1)
+        same = same and all((a["numerator"], a["denominator"]) == (b["numerator"], b["denominator"])
+                            for a, b in zip(rp, rb))
+        pairs = sum(b["pairs"] for b in rb)
+    p, b = float(np.median(tp)), float(np.median(tb))
+    return {"workload": "c3 light: the %d of %d c3 queries with <= 2^26 inner products (t 8..23, relative "
+                        "error 0.05, Philox draws)" % (len(qs), total),
+            "metric": "queries/s", "plain": len(qs) / p, "batched": len(qs) / b, "speedup": p / b,
+            "identical_results": bool(same), "pairs": pairs, "reps": reps,
+            "timing": "wall clock around the ABI call, host work included, median of reps"}
 
 
 def run_reference(args, rank, world):
@@ -347,6 +410,7 @@ def main():
                     help="states per projector per step (default: the workload's L = 4096); smaller values are "
                          "profiling cases, not bench lines")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-plain queries/s leg")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
