@@ -144,6 +144,8 @@ def load_library(path=LIB_PATH):
         "csim_multi_sampled_projector": ([vp, vp, vp, i32, i32, C.c_double, i32, i32, i32, u64, vp], C.c_int),
         "csim_exact_projector": ([vp, vp, vp, i32, i32, C.c_double, vp], C.c_int),
         "csim_decompose": ([i32, C.c_double, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp], C.c_int),
+        "csim_decompose_on": ([vp, i32, C.c_double, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp], C.c_int),
+        "csim_fidelity_sum": ([vp, i32, vp, i32, vp], C.c_int),
         "csim_run_queries": ([vp, i64, vp, vp, i32], C.c_int),
         "csim_server_create": ([vp, vp], C.c_int),
         "csim_submit": ([vp, vp, vp], C.c_int),
@@ -355,6 +357,23 @@ class Backend:
         out = C.c_double(0)
         self._check(self.lib.csim_exact_projector(self.ctx, C.byref(P), _p(Lp), int(k), int(bool(exact)),
                                                   float(norm), C.byref(out)))
+        return out.value
+
+    def decompose(self, t, fidbound=1e-5, rank=False, fidelity=False, forceL=False, exact=False, k=0, rng=None):
+        """decompose() with the fidelity sum on this GPU (csim_decompose_on)."""
+        rng = rng or LibcRand(1)
+        e, kk, norm = C.c_int32(int(bool(exact))), C.c_int32(int(k or 0)), C.c_double(0)
+        L = np.zeros(64, dtype=np.uint64)
+        self._check(self.lib.csim_decompose_on(self.ctx, int(t), float(fidbound), int(bool(rank)),
+                                               int(bool(fidelity)), int(bool(forceL)), 0, 1, C.byref(e),
+                                               C.byref(kk), C.byref(norm), _p(L), rng._buf, None))
+        return bool(e.value), kk.value, norm.value, (None if e.value else L[: kk.value].copy())
+
+    def fidelity_sum(self, t, L):
+        """Z(L) = sum over codewords x of 2^(-|x|/2) (probability.c:391-398) on the GPU."""
+        Lp = np.ascontiguousarray(np.asarray([int(x) for x in L] or [0], dtype=np.uint64))
+        out = C.c_double(0)
+        self._check(self.lib.csim_fidelity_sum(self.ctx, int(t), _p(Lp), len(L), C.byref(out)))
         return out.value
 
     def run_queries(self, queries, batched=True, check=True):

@@ -106,11 +106,18 @@ extern "C" int csim_backend_run(FILE* in, FILE* out, int device) {
         csim_libc_rand_seed(dstate.data(), 1);
         double norm = 0;
         uint64_t L[CSIM_MAX_QUBITS] = {0};
-        const int rc = csim_decompose(t, fidbound, rank, fidelity, forceL, verbose, quiet, &exact, &k, &norm, L,
-                                      dstate.data(), out);
+        // the fidelity sum runs on the GPU; without one the lines up to the L
+        // matrix still print, and the run stops below with the device error
+        csim_ctx* ctx = nullptr;
+        const int ctx_rc = csim_ctx_create(device, &ctx);
+        const int rc = ctx ? csim_decompose_on(ctx, t, fidbound, rank, fidelity, forceL, verbose, quiet, &exact, &k,
+                                               &norm, L, dstate.data(), out)
+                           : csim_decompose(t, fidbound, rank, fidelity, forceL, verbose, quiet, &exact, &k, &norm,
+                                            L, dstate.data(), out);
         if (rc != CSIM_OK) {
             fprintf(out, "csim: decompose failed (%d)\n", rc);
             fflush(out);
+            csim_ctx_destroy(ctx);
             return rc;
         }
         fprintf(out, "World Size: %d\n", 1);
@@ -146,8 +153,7 @@ extern "C" int csim_backend_run(FILE* in, FILE* out, int device) {
         const int rng = (r_env && strcmp(r_env, "philox") == 0) ? CSIM_RNG_PHILOX : CSIM_RNG_LIBC;
         const uint64_t sd = rng == CSIM_RNG_LIBC ? (uint64_t)(uint32_t)seed : seed;
 
-        csim_ctx* ctx = nullptr;
-        int r = csim_ctx_create(device, &ctx);
+        int r = ctx_rc;
         if (r != CSIM_OK) {
             fprintf(out, "csim: no usable GB300 device (%d)\n", r);
             fflush(out);

@@ -287,8 +287,8 @@ void Engine::plan(QueryRec* r) {
     ds.seed(1);
     r->exact = Q.exact;
     r->k = Q.k;
-    const int rc = csim_decompose(Q.t, Q.fidbound, Q.rank, Q.fidelity, Q.force_l, Q.verbose, Q.quiet, &r->exact,
-                                  &r->k, &r->norm, r->L, &ds, nullptr);
+    const int rc = csim_decompose_on(ctx_, Q.t, Q.fidbound, Q.rank, Q.fidelity, Q.force_l, Q.verbose, Q.quiet,
+                                     &r->exact, &r->k, &r->norm, r->L, &ds, nullptr);
     if (rc != CSIM_OK) {
         fail_query(r, rc);
         return;

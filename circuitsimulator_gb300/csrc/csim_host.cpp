@@ -726,11 +726,33 @@ int gf2_rank(const uint64_t* rows, int nrows) {
     return rank;
 }
 
-}  // namespace
+// Z(L) on the device, exactly: valid while every partial sum of the reference's
+// double loop is exact, k + floor(t/2) <= 53 (terms are multiples of 2^-floor(t/2), sums < 2^k)
+int fidelity_sum_gpu(csim_ctx* ctx, int t, const uint64_t* L, int k, double* Z) {
+    const int S = t / 2;
+    if (k < 0 || k > 40 || t < 1 || t > CSIM_MAX_QUBITS || k + S > 53)
+        return fail(ctx, CSIM_ERR_ARG, "fidelity sum: k=%d t=%d beyond the exact range k + t/2 <= 53", k, t);
+    uint64_t rows[CSIM_MAX_QUBITS] = {0};
+    for (int i = 0; i < k; i++) rows[i] = L[i];
+    uint64_t* dL;
+    CKR(dput(ctx, kBufL, rows, (size_t)CSIM_MAX_QUBITS, &dL));
+    void* v;
+    CKR(dbuf(ctx, kBufParts, (size_t)ctx->num_sms * 8 * 16 + 16, &v));
+    int nb = 0;
+    if (csim::launch_fidelity_sum(launch_of(ctx), dL, k, S, (unsigned __int128*)v, &nb))
+        return fail(ctx, CSIM_ERR_CUDA, "fidelity sum launch failed");
+    std::vector<unsigned __int128> part(nb);
+    CKR(dget(ctx, part.data(), (const unsigned __int128*)v, (size_t)nb));
+    CKR(finish(ctx));
+    unsigned __int128 sum = 0;
+    for (int i = 0; i < nb; i++) sum += part[i];
+    *Z = std::ldexp((double)(uint64_t)sum, -S);  // sum <= 2^53: exact
+    return 0;
+}
 
-extern "C" int csim_decompose(int32_t t, double fidbound, int32_t rank, int32_t fidelity, int32_t force_l,
-                              int32_t verbose, int32_t quiet, int32_t* exact, int32_t* k, double* norm,
-                              uint64_t* L_out, void* rng_state, FILE* log) {
+int decompose_impl(csim_ctx* gpu, int32_t t, double fidbound, int32_t rank, int32_t fidelity, int32_t force_l,
+                   int32_t verbose, int32_t quiet, int32_t* exact, int32_t* k, double* norm, uint64_t* L_out,
+                   void* rng_state, FILE* log) {
     if (!exact || !k || !norm || !L_out || !rng_state || t < 0 || t > CSIM_MAX_QUBITS) return CSIM_ERR_ARG;
     LibcRand& lr = *(LibcRand*)rng_state;
     if (t == 0) {
@@ -759,7 +781,17 @@ extern "C" int csim_decompose(int32_t t, double fidbound, int32_t rank, int32_t 
     }
     if (*k > 40) return CSIM_ERR_ARG;
     double inner = 0, Z_L = 0;
+    // The reference draws L until the fidelity bound holds (probability.c:355).
+    // With its integer-division Z(L) the bound is out of reach for an
+    // autopicked k at moderate t, and that loop never ends; here it stops after
+    // kMaxCodeDraws draws with CSIM_ERR_ARG.
+    constexpr int kMaxCodeDraws = 256;
+    int draws = 0;
     while (inner < 1 - fidbound || forceK) {
+        if (++draws > kMaxCodeDraws) {
+            if (log) fprintf(log, "csim: no L reached delta = %f in %d draws\n", fidbound, kMaxCodeDraws);
+            return CSIM_ERR_ARG;
+        }
         const int kk = *k, bytes = (kk * t + 7) / 8;
         for (int i = 0; i < kk; i++) L_out[i] = 0;
         for (int b = 0; b < bytes; b++) {  // BitMatrixSetRandom over the row-major bit array
@@ -774,8 +806,16 @@ extern "C" int csim_decompose(int32_t t, double fidbound, int32_t rank, int32_t 
             continue;
         }
         if (fidelity) {
-            Z_L = 0;  // Z(L) = sum_x 2^{-|x|/2}, with the reference's integer division
-            for (int64_t i = 0; i < ((int64_t)1 << kk); i++) Z_L += pow(2, -popc(codeword(i, L_out, kk)) / 2);
+            // Z(L) = sum_x 2^{-|x|/2}, with the reference's integer division.  On the
+            // device where that double loop is exact; beyond that its rounding is
+            // reproduced by the same loop in codeword order
+            if (gpu && kk + t / 2 <= 53) {
+                const int rc = fidelity_sum_gpu(gpu, t, L_out, kk, &Z_L);
+                if (rc) return rc;
+            } else {
+                Z_L = 0;
+                for (int64_t i = 0; i < ((int64_t)1 << kk); i++) Z_L += pow(2, -popc(codeword(i, L_out, kk)) / 2);
+            }
             inner = pow(2, kk) * pow(v, 2 * t) / Z_L;
             if (forceK) {
                 if (log) fprintf(log, "delta = 1 - <H^t|L>: %lf\n", 1 - inner);
@@ -791,4 +831,28 @@ extern "C" int csim_decompose(int32_t t, double fidbound, int32_t rank, int32_t 
     }
     if (fidelity) *norm = sqrt(pow(2, *k) * Z_L);
     return CSIM_OK;
+}
+
+}  // namespace
+
+extern "C" int csim_decompose(int32_t t, double fidbound, int32_t rank, int32_t fidelity, int32_t force_l,
+                              int32_t verbose, int32_t quiet, int32_t* exact, int32_t* k, double* norm,
+                              uint64_t* L_out, void* rng_state, FILE* log) {
+    return decompose_impl(nullptr, t, fidbound, rank, fidelity, force_l, verbose, quiet, exact, k, norm, L_out,
+                          rng_state, log);
+}
+
+extern "C" int csim_decompose_on(csim_ctx* ctx, int32_t t, double fidbound, int32_t rank, int32_t fidelity,
+                                 int32_t force_l, int32_t verbose, int32_t quiet, int32_t* exact, int32_t* k,
+                                 double* norm, uint64_t* L_out, void* rng_state, FILE* log) {
+    if (!ctx) return CSIM_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    return decompose_impl(ctx, t, fidbound, rank, fidelity, force_l, verbose, quiet, exact, k, norm, L_out,
+                          rng_state, log);
+}
+
+extern "C" int csim_fidelity_sum(csim_ctx* ctx, int32_t t, const uint64_t* L, int32_t k, double* Z_L) {
+    if (!ctx || !Z_L || (k > 0 && !L)) return fail(ctx, CSIM_ERR_ARG, "bad argument");
+    cudaSetDevice(ctx->device);
+    return fidelity_sum_gpu(ctx, t, L, k, Z_L);
 }

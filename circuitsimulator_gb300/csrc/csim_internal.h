@@ -31,6 +31,9 @@ int launch_random_states(const Launch& L, int n, int64_t count, int mode, uint64
 int launch_project(const Launch& L, int nr, GState* s, int64_t count, int nstabs, const int* m, const uint64_t* zeta,
                    const uint64_t* xi, int* code);
 int launch_codewords(const Launch& L, const uint64_t* Ld, int k, int64_t j0, int64_t count, uint64_t* out);
+// decompose()'s fidelity sum as the integer sum of 2^(S - |x|/2) over the 2^k
+// codewords: one partial per block (*nblocks of them, at most SMs * 8)
+int launch_fidelity_sum(const Launch& L, const uint64_t* Ld, int k, int S, unsigned __int128* part, int* nblocks);
 int launch_prep(const Launch& L, int t, int exact, const uint64_t* codewords, const int64_t* idx, int64_t count,
                 GState* out);
 // part / part_diag: 4 int128 per work item (ntheta * ceil(nj/chunk) items), zeroed by the caller

@@ -225,6 +225,48 @@ __global__ void __launch_bounds__(256) k_prep(int t, int exact, const uint64_t* 
     }
 }
 
+// decompose()'s fidelity sum (probability.c:391-398): Z(L) = sum over the 2^k
+// codewords x of 2^(-|x|/2), |x|/2 in integer division.  Terms are powers of
+// two, so the sum is taken exactly as the integer sum of 2^(S - |x|/2),
+// S = floor(t/2), in 128 bits; the order of the codewords does not matter.
+// Each thread walks a contiguous range of Gray-code indices, so consecutive
+// codewords differ by one row of L.  One 128-bit partial per block.
+__global__ void __launch_bounds__(256) k_fidelity_sum(const uint64_t* L, int k, int S, int64_t per_thread,
+                                                      unsigned __int128* part) {
+    __shared__ uint64_t sL[64];
+    __shared__ unsigned __int128 red[8];
+    if (threadIdx.x < 64) sL[threadIdx.x] = threadIdx.x < (unsigned)k ? L[threadIdx.x] : 0ull;
+    __syncthreads();
+    const int64_t total = (int64_t)1 << k;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t i0 = tid * per_thread;
+    unsigned __int128 acc = 0;
+    if (i0 < total) {
+        const int64_t i1 = i0 + per_thread < total ? i0 + per_thread : total;
+        // codeword of Gray index g = i0 ^ (i0 >> 1): bit b of g selects row k-1-b
+        const uint64_t g = (uint64_t)(i0 ^ (i0 >> 1));
+        uint64_t x = 0;
+        for (int b = 0; b < k; b++)
+            if ((g >> b) & 1) x ^= sL[k - 1 - b];
+        for (int64_t i = i0; i < i1; i++) {
+            acc += (unsigned __int128)1 << (S - __popcll(x) / 2);
+            const int b = __ffsll((long long)(i + 1)) - 1;  // Gray code i -> i+1 flips bit ctz(i+1)
+            if (b < k) x ^= sL[k - 1 - b];
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint64_t lo = (uint64_t)acc, hi = (uint64_t)(acc >> 64);
+        acc += ((unsigned __int128)__shfl_xor_sync(kFull, hi, o) << 64) | __shfl_xor_sync(kFull, lo, o);
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned __int128 s = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[w];
+        part[blockIdx.x] = s;
+    }
+}
+
 // ------------------------------------------------------------ the hot loop
 // Adds eps 2^{p/2} w^m, scaled by 2^{P/2}, to z = z0 + z1 w + z2 w^2 + z3 w^3
 // (w = e^{i pi/4}); sqrt 2 = w - w^3.  The reference's p lies in [-2n, n]
@@ -441,6 +483,19 @@ int launch_prep(const Launch& L, int t, int exact, const uint64_t* codewords, co
     const int g = grid_for(L, count);
     if (t <= 32) k_prep<1><<<g, 256, 0, L.stream>>>(t, exact, codewords, idx, count, out);
     else k_prep<2><<<g, 256, 0, L.stream>>>(t, exact, codewords, idx, count, out);
+    return post(L);
+}
+
+int launch_fidelity_sum(const Launch& L, const uint64_t* Ld, int k, int S, unsigned __int128* part, int* nblocks) {
+    if (k < 0 || k > 40 || S < 0 || S > 32) return -1;
+    const int64_t total = (int64_t)1 << k;
+    const int64_t threads = (int64_t)L.num_sms * 2048;
+    int64_t per_thread = (total + threads - 1) / threads;
+    if (per_thread < 1) per_thread = 1;
+    const int64_t nthreads = (total + per_thread - 1) / per_thread;
+    const int64_t blocks = (nthreads + 255) / 256;
+    *nblocks = (int)blocks;
+    k_fidelity_sum<<<(int)blocks, 256, 0, L.stream>>>(Ld, k, S, per_thread, part);
     return post(L);
 }
 

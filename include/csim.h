@@ -306,6 +306,18 @@ int csim_decompose(int32_t t, double fidbound, int32_t rank, int32_t fidelity, i
                    int32_t verbose, int32_t quiet, int32_t *exact, int32_t *k, double *norm, uint64_t *L_out,
                    void *rng_state, FILE *log);
 
+/* csim_decompose with the fidelity sum Z(L) = sum_x 2^(-|x|/2) over the 2^k
+ * codewords (probability.c:391-398) taken on ctx's GPU, exactly, where the
+ * reference's double loop is exact (k + floor(t/2) <= 53); beyond that the
+ * host loop reproduces its rounding.  Same outputs as csim_decompose. */
+int csim_decompose_on(csim_ctx *ctx, int32_t t, double fidbound, int32_t rank, int32_t fidelity,
+                      int32_t force_l, int32_t verbose, int32_t quiet, int32_t *exact, int32_t *k, double *norm,
+                      uint64_t *L_out, void *rng_state, FILE *log);
+
+/* Z(L) of the k-row code L on t qubits, on the GPU.  CSIM_ERR_ARG unless
+ * k + floor(t/2) <= 53, where the value equals the reference's double sum. */
+int csim_fidelity_sum(csim_ctx *ctx, int32_t t, const uint64_t *L, int32_t k, double *Z_L);
+
 /* The C library's srand()/rand() sequence, reproduced as a value type so that
  * each context owns one.  Use csim_libc_rand_size() bytes of storage. */
 int64_t csim_libc_rand_size(void);

@@ -357,3 +357,41 @@ def test_philox_blocks_compose(gpu):
         gpu.rng_position(123, lo)
         parts.append(gpu.singleProjectorSample(P, L, False, hi - lo, backend.RNG_PHILOX, backend.SEED_CONTINUE))
     assert (np.concatenate(parts) == whole).all()
+
+
+def _zl_reference_loop(t, L):
+    """The reference's Z(L) loop (probability.c:391-398) in codeword order, in double."""
+    k = len(L)
+    j = np.arange(1 << k, dtype=np.uint64)
+    x = np.zeros(1 << k, dtype=np.uint64)
+    for r in range(k):
+        x ^= np.where((j >> np.uint64(k - 1 - r)) & np.uint64(1), np.uint64(int(L[r])), np.uint64(0))
+    w = np.array([bin(int(v)).count("1") // 2 for v in x], dtype=np.int64)
+    return float(np.cumsum(2.0 ** (-w.astype(np.float64)))[-1])
+
+
+@pytest.mark.gpu
+def test_fidelity_sum_matches_reference_loop(gpu):
+    rs = np.random.RandomState(41)
+    for t, k in ((5, 3), (12, 6), (24, 11), (40, 16), (64, 12), (17, 17)):
+        L = [rand_word(rs, t) for _ in range(k)]
+        assert gpu.fidelity_sum(t, L) == _zl_reference_loop(t, L), (t, k)
+
+
+@pytest.mark.gpu
+def test_decompose_with_fidelity_on_gpu_equals_host(gpu):
+    # k given (one draw of L) or small t with a loose bound: with the reference's
+    # integer-division Z(L), an autopicked k at large t never reaches the bound
+    for t, fb, kk, force_l in ((8, 0.3, 0, True), (9, 0.35, 0, True), (31, 0.02, 14, False), (40, 0.01, 16, False),
+                               (48, 0.02, 12, False)):
+        host = backend.decompose(t, fb, False, True, force_l, False, kk)
+        dev = gpu.decompose(t, fb, False, True, force_l, False, kk)
+        assert host[:3] == dev[:3], t
+        assert (host[3] is None and dev[3] is None) or list(host[3]) == list(dev[3])
+
+
+def test_decompose_fidelity_loop_is_bounded():
+    """An autopicked k whose fidelity bound is out of reach fails after a bounded
+    number of draws of L (the reference's loop, probability.c:355, never ends)."""
+    with pytest.raises(backend.CsimError):
+        backend.decompose(31, 0.02, False, True, False, False, 0)
