@@ -782,10 +782,12 @@ int decompose_impl(csim_ctx* gpu, int32_t t, double fidbound, int32_t rank, int3
     if (*k > 40) return CSIM_ERR_ARG;
     double inner = 0, Z_L = 0;
     // The reference draws L until the fidelity bound holds (probability.c:355).
-    // With its integer-division Z(L) the bound is out of reach for an
-    // autopicked k at moderate t, and that loop never ends; here it stops after
-    // kMaxCodeDraws draws with CSIM_ERR_ARG.
-    constexpr int kMaxCodeDraws = 256;
+    // With its integer-division Z(L) the bound can be out of reach (an
+    // autopicked k at larger t), and then that loop never ends; here it stops
+    // after kMaxCodeDraws draws with CSIM_ERR_ARG.  Bounds that can be met take
+    // hundreds to thousands of draws (411 and 2437 in the reference's seeded
+    // decompose vectors).
+    constexpr int kMaxCodeDraws = 1 << 16;
     int draws = 0;
     while (inner < 1 - fidbound || forceK) {
         if (++draws > kMaxCodeDraws) {

@@ -390,8 +390,9 @@ def test_decompose_with_fidelity_on_gpu_equals_host(gpu):
         assert (host[3] is None and dev[3] is None) or list(host[3]) == list(dev[3])
 
 
-def test_decompose_fidelity_loop_is_bounded():
+@pytest.mark.gpu
+def test_decompose_fidelity_loop_is_bounded(gpu):
     """An autopicked k whose fidelity bound is out of reach fails after a bounded
     number of draws of L (the reference's loop, probability.c:355, never ends)."""
     with pytest.raises(backend.CsimError):
-        backend.decompose(31, 0.02, False, True, False, False, 0)
+        gpu.decompose(31, 0.02, False, True, False, False, 0)
