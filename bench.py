@@ -343,6 +343,40 @@ def batch_compare(gpu, reps=3):
             "timing": "wall clock around the ABI call, host work included, median of reps"}
 
 
+C4_WORKLOAD = os.path.join(ROOT, "tests", "golden", "workload_c4.json")
+
+
+def chain_compare(shots, nbits, samples=None):
+    """sampleQubits chains on the c4 circuit (tests/golden/workload_c4.json:
+    n=32, t=64, k=14 code, L=2048 states per conditional): `shots` chains of
+    `nbits` sampled qubits, plain (one shot after another, one query at a
+    time) vs batched (all shots in lockstep, one csim_run_queries call per
+    step).  Same numpy seeds and backend seed; outputs checked equal."""
+    from circuitsimulator_gb300 import backend, sample
+
+    w = json.load(open(C4_WORKLOAD))
+    cfg = dict(w["config"], seed=4242)
+    if samples:
+        cfg["samples"] = samples
+    bits = w["sample"][:nbits]
+    seeds = list(range(1000, 1000 + shots))
+    gpu = backend.Backend(0)
+    sample.sample_qubits_batch(w["circ"], {}, bits[:1], dict(cfg), seeds[:2], backend=gpu)  # warm-up
+    t0 = time.perf_counter()
+    plain = [sample.sampleQubits(w["circ"], {}, list(bits), dict(cfg), rng=np.random.RandomState(s), backend=gpu)
+             for s in seeds]
+    t1 = time.perf_counter()
+    st = {}
+    batched = sample.sample_qubits_batch(w["circ"], {}, list(bits), dict(cfg), seeds, backend=gpu, stats=st)
+    t2 = time.perf_counter()
+    queries = sum(st["queries_per_step"])
+    return {"workload": "c4 chain: %d shots x %d sampled qubits, n=32, t=64, k=%d, L=%d per conditional"
+                        % (shots, nbits, cfg["k"], cfg["samples"]),
+            "metric": "queries/s", "queries": queries, "plain": queries / (t1 - t0), "batched": queries / (t2 - t1),
+            "speedup": (t1 - t0) / (t2 - t1), "identical_outputs": plain == batched, "steps": st["steps"],
+            "plain_s": t1 - t0, "batched_s": t2 - t1}
+
+
 def run_reference(args, rank, world):
     """The reference's algorithm on the host cores (the oracle port of
     libcirc/stabilizer.c + stateprep.c + innerprod.c: the reference's own C
@@ -411,7 +445,14 @@ def main():
                          "profiling cases, not bench lines")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-plain queries/s leg")
+    ap.add_argument("--chain", default=None, metavar="SHOTSxBITS",
+                    help="only time sampleQubits chains on the c4 circuit, plain vs batched (e.g. 16x4)")
+    ap.add_argument("--chain-samples", type=int, default=None, help="L per conditional for --chain")
     args = ap.parse_args()
+    if args.chain:
+        shots, nbits = (int(v) for v in args.chain.lower().split("x"))
+        print(json.dumps(chain_compare(shots, nbits, args.chain_samples)))
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

@@ -392,7 +392,9 @@ def test_decompose_with_fidelity_on_gpu_equals_host(gpu):
 
 @pytest.mark.gpu
 def test_decompose_fidelity_loop_is_bounded(gpu):
-    """An autopicked k whose fidelity bound is out of reach fails after a bounded
-    number of draws of L (the reference's loop, probability.c:355, never ends)."""
+    """A fidelity bound out of reach fails after a bounded number of draws of L
+    (the reference's loop, probability.c:355, never ends).  With delta = 1e-300
+    the loop needs 2^k v^2t / Z(L) >= 1.0, and the integer-division Z(L) is at
+    least the true one, whose fidelity is below 1; forceL keeps k = t = 12."""
     with pytest.raises(backend.CsimError):
-        gpu.decompose(31, 0.02, False, True, False, False, 0)
+        gpu.decompose(12, 1e-300, False, True, True, False, 0)
