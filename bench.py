@@ -16,6 +16,8 @@ protocol file tests/golden/workload_c2.txt.
          (tests/golden/workload_c3.json.gz): the same queries and draws through
          csim_run_queries in shared launches and one at a time, results checked
          bit-identical
+  serve  p50/p99 latency and queries/s of the continuous-batching server vs
+         plain one-at-a-time service, Poisson arrivals of light c3 queries
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 Under torchrun each rank draws its own states (weak scaling); rank 0 prints.
@@ -278,6 +280,7 @@ def run_ours(args, rank, world, local_rank):
     }
     if world == 1 and not args.no_batch:
         out["batch"] = batch_compare(gpu)
+        out["serve"] = serve_compare(100.0, 150)
     if world == 1 and not args.no_cpu_baseline:
         try:
             out["cpu_baseline"] = cpu_baseline(cfg, projs, k, L)
@@ -341,6 +344,59 @@ def batch_compare(gpu, reps=3):
             "metric": "queries/s", "plain": len(qs) / p, "batched": len(qs) / b, "speedup": p / b,
             "identical_results": bool(same), "pairs": pairs, "reps": reps,
             "timing": "wall clock around the ABI call, host work included, median of reps"}
+
+
+def serve_compare(rate, count, seed=5):
+    """Serving on the light c3 queries under Poisson arrivals at `rate`
+    queries/s: the continuous-batching server (csim_submit as each query
+    arrives) vs plain one-at-a-time service (first come first served through
+    the single-query entry points).  Latency = result time - arrival time."""
+    from circuitsimulator_gb300 import backend
+
+    light, _ = c3_queries(light=True)
+    rs = np.random.RandomState(seed)
+    qs = [light[i] for i in rs.randint(len(light), size=count)]
+    arrivals = np.cumsum(rs.exponential(1.0 / rate, size=count))
+
+    def pct(v):
+        v = np.sort(np.asarray(v))
+        return {"p50_ms": 1e3 * float(np.percentile(v, 50)), "p99_ms": 1e3 * float(np.percentile(v, 99)),
+                "max_ms": 1e3 * float(v[-1])}
+
+    srv = backend.Server(0)
+    for t in [srv.submit(q) for q in qs[:8]]:  # warm-up: decompositions resident, buffers sized
+        srv.wait(t)
+        srv.release(t)
+    t0 = time.perf_counter()
+    tickets = []
+    for q, a in zip(qs, arrivals):
+        d = t0 + a - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        tickets.append(srv.submit(q))
+    res = [srv.wait(t) for t in tickets]
+    t_end = time.perf_counter()
+    st = srv.stats()
+    srv.close()
+    server = dict(pct([r["latency_s"] for r in res]), queries_per_s=count / (t_end - t0),
+                  rounds=st["rounds"], failed=sum(1 for r in res if r["status"]))
+
+    gpu = backend.Backend(0)
+    gpu.run_queries(qs[:8], batched=False)
+    lat = []
+    t0 = time.perf_counter()
+    for q, a in zip(qs, arrivals):
+        d = t0 + a - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        gpu.run_queries([q], batched=False)
+        lat.append(time.perf_counter() - t0 - a)
+    t_end = time.perf_counter()
+    plain = dict(pct(lat), queries_per_s=count / (t_end - t0))
+    return {"workload": "c5 (scaled): %d light c3 queries (t 8..23, relative error 0.05), Poisson arrivals at "
+                        "%g queries/s" % (count, rate),
+            "rate": rate, "server": server, "plain": plain,
+            "throughput_ratio": server["queries_per_s"] / plain["queries_per_s"]}
 
 
 C4_WORKLOAD = os.path.join(ROOT, "tests", "golden", "workload_c4.json")
@@ -448,7 +504,14 @@ def main():
     ap.add_argument("--chain", default=None, metavar="SHOTSxBITS",
                     help="only time sampleQubits chains on the c4 circuit, plain vs batched (e.g. 16x4)")
     ap.add_argument("--chain-samples", type=int, default=None, help="L per conditional for --chain")
+    ap.add_argument("--serve", default=None, metavar="RATES",
+                    help="only time serving under Poisson arrivals at these rates (queries/s, comma separated)")
+    ap.add_argument("--serve-count", type=int, default=300, help="queries per rate for --serve")
     args = ap.parse_args()
+    if args.serve:
+        rates = [float(r) for r in args.serve.split(",")]
+        print(json.dumps([serve_compare(r, args.serve_count) for r in rates]))
+        return
     if args.chain:
         shots, nbits = (int(v) for v in args.chain.lower().split("x"))
         print(json.dumps(chain_compare(shots, nbits, args.chain_samples)))

@@ -492,6 +492,23 @@ class Server:
         return _result_dict(st)
 
 
+def serve_backend(protocol_texts, seed, rng=None, timeout=None, exe=EXE_PATH):
+    """Runs `gpubackend serve` on back-to-back protocol inputs; returns one
+    (status, numerator, denominator) per input, in input order.  Query i is
+    seeded with seed + i."""
+    env = dict(os.environ, CSIM_SEED=str(int(seed)))
+    if rng is not None:
+        env["CSIM_RNG"] = rng
+    r = subprocess.run([exe, "serve"], input="".join(t if t.endswith("\n") else t + "\n" for t in protocol_texts)
+                       .encode(), stdout=subprocess.PIPE, stderr=subprocess.PIPE, env=env, timeout=timeout)
+    out = []
+    for ln in r.stdout.decode().splitlines():
+        f = ln.split()
+        if len(f) == 4 and f[0].isdigit():
+            out.append((int(f[1]), float(f[2]), float(f[3])))
+    return r.returncode, out
+
+
 def run_backend(protocol_text, seed=None, rng=None, timeout=None, exe=EXE_PATH):
     """Runs the gpubackend executable on one stdin-protocol input; returns its
     stdout lines (the last two are numerator and denominator)."""

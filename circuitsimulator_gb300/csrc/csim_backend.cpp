@@ -12,6 +12,7 @@
 // set; CSIM_RNG=philox switches to the counter-based generator.
 #include <unistd.h>
 
+#include <cctype>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -190,4 +191,137 @@ bad:
     fprintf(out, "csim: malformed backend input\n");
     fflush(out);
     return CSIM_ERR_PROTOCOL;
+}
+
+// ---------------------------------------------------------------- serving daemon
+// One process for a stream of queries instead of one process per query
+// (libcirc/probability.py:237-244).  Reads back-to-back protocol inputs (13
+// scalars, G', H') until end of input and submits each to a csim_server as
+// soon as it is read, so queries that arrive while others run share rounds.
+// Writes one line per query, in input order:
+//     <index> <status> <numerator %.17e> <denominator %.17e>
+// Seeds: CSIM_SEED + index when CSIM_SEED is set, else process id + index.
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <thread>
+
+namespace {
+
+struct OwnedQuery {
+    csim_query q{};
+    Proj G, H;
+};
+
+bool read_query(FILE* in, OwnedQuery& oq) {
+    int v[8];
+    for (int i = 0; i < 8; i++)
+        if (fscanf(in, "%d", &v[i]) != 1) return false;
+    double fb;
+    if (fscanf(in, "%lf", &fb) != 1) return false;
+    int w[4];
+    for (int i = 0; i < 4; i++)
+        if (fscanf(in, "%d", &w[i]) != 1) return false;
+    if (!read_projector(in, oq.G) || !read_projector(in, oq.H)) return false;
+    csim_query& q = oq.q;
+    q.quiet = v[0];
+    q.verbose = v[1];
+    q.noapprox = v[2];
+    q.samples = v[3];
+    q.bins = v[4];
+    q.t = v[5];
+    q.k = v[6];
+    q.exact = v[7];
+    q.fidbound = fb;
+    q.fidelity = w[0];
+    q.rank = w[1];
+    q.force_l = w[2];
+    q.force_sample = w[3];
+    q.G = oq.G.view();
+    q.H = oq.H.view();
+    return true;
+}
+
+}  // namespace
+
+extern "C" int csim_backend_serve(FILE* in, FILE* out, int device) {
+    csim_server_config cfg{};
+    cfg.device = device;
+    const char* b_env = getenv("CSIM_HBM_BUDGET");
+    cfg.hbm_budget_bytes = (b_env && *b_env) ? (int64_t)strtoll(b_env, nullptr, 10) : 0;
+    csim_server* srv = nullptr;
+    int rc = csim_server_create(&cfg, &srv);
+    if (rc != CSIM_OK) {
+        fprintf(out, "csim: no usable GB300 device (%d)\n", rc);
+        fflush(out);
+        return rc;
+    }
+    const char* s_env = getenv("CSIM_SEED");
+    const uint64_t seed0 = (s_env && *s_env) ? (uint64_t)strtoull(s_env, nullptr, 10) : (uint64_t)getpid();
+    const char* r_env = getenv("CSIM_RNG");
+    const int rng = (r_env && strcmp(r_env, "philox") == 0) ? CSIM_RNG_PHILOX : CSIM_RNG_LIBC;
+
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<int64_t> tickets;  // in input order
+    bool eof = false;
+    std::thread writer([&] {
+        int64_t index = 0;
+        while (true) {
+            int64_t tk;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv.wait(lk, [&] { return eof || !tickets.empty(); });
+                if (tickets.empty()) return;
+                tk = tickets.front();
+                tickets.pop_front();
+            }
+            csim_query_result r{};
+            int w = csim_wait(srv, tk, -1.0, &r);
+            if (w != CSIM_OK) r.status = w;
+            fprintf(out, "%lld %d %.17e %.17e\n", (long long)index++, r.status, r.numerator, r.denominator);
+            fflush(out);
+            csim_release(srv, tk);
+        }
+    });
+    int64_t index = 0;
+    int status = CSIM_OK;
+    while (true) {
+        OwnedQuery* oq = new OwnedQuery();
+        if (!read_query(in, *oq)) {
+            delete oq;
+            int c;
+            while ((c = fgetc(in)) != EOF && isspace(c)) {
+            }
+            if (c != EOF) status = CSIM_ERR_PROTOCOL;  // trailing garbage
+            break;
+        }
+        oq->q.rng = rng;
+        oq->q.seed = rng == CSIM_RNG_LIBC ? (uint64_t)(uint32_t)(seed0 + (uint64_t)index) : seed0 + (uint64_t)index;
+        int64_t tk = 0;
+        const int s = csim_submit(srv, &oq->q, &tk);  // copies the query
+        delete oq;
+        if (s != CSIM_OK) {
+            status = s;
+            break;
+        }
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            tickets.push_back(tk);
+        }
+        cv.notify_one();
+        index++;
+    }
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        eof = true;
+    }
+    cv.notify_one();
+    writer.join();
+    csim_server_destroy(srv);
+    if (status == CSIM_ERR_PROTOCOL) {
+        fprintf(out, "csim: malformed backend input after query %lld\n", (long long)index);
+        fflush(out);
+    }
+    return status;
 }

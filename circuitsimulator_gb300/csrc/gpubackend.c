@@ -6,6 +6,9 @@
  * "stdin"; with none, a file name is read from stdin.  libcirc/probability.py
  * runs it with config["cpath"] = path of this executable and
  * config["mpirun"] = "" (one process drives the whole GPU).
+ *
+ * "gpubackend serve" keeps one process for a stream of back-to-back protocol
+ * inputs and answers each with one line (csim_backend_serve).
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -15,6 +18,10 @@
 
 int main(int argc, char *argv[]) {
     char file[256] = "";
+    if (argc == 2 && strcmp(argv[1], "serve") == 0) {  /* one process, a stream of queries */
+        const char *dev = getenv("CSIM_DEVICE");
+        return csim_backend_serve(stdin, stdout, dev ? atoi(dev) : 0) == CSIM_OK ? 0 : 1;
+    }
     printf("C backend print mode is on.\n");
     if (argc == 1) {
         if (scanf("%255s", file) != 1) file[0] = '\0';

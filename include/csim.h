@@ -232,6 +232,12 @@ typedef struct csim_query_result {
  * per-query status is in r[i].status. */
 int csim_run_queries(csim_ctx *ctx, int64_t nq, const csim_query *q, csim_query_result *r, int32_t batched);
 
+/* The backend as a long-lived process: reads back-to-back stdin-protocol
+ * inputs until end of input, runs them on a csim_server as they arrive, and
+ * writes "<index> <status> <numerator> <denominator>" per query in input
+ * order (%.17e).  Seeds are CSIM_SEED + index (process id + index if unset). */
+int csim_backend_serve(FILE *in, FILE *out, int device);
+
 /* ------------------------------------------------------------- serving */
 
 /* A query server on one GPU, replacing one backend process per query

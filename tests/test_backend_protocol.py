@@ -81,3 +81,16 @@ def test_backend_output_matches_reference(exe, case):
     assert _l_block(lines) == _l_block(ref)
     for a, b in zip(lines[-2:], ref[-2:]):
         assert close(float(a), float(b), 1e-12, 1e-12), (a, b)
+
+
+def test_serving_daemon_without_gpu_fails_loudly(exe):
+    import subprocess
+
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    r = subprocess.run([exe, "serve"], input=cases()[0]["input"].encode(), stdout=subprocess.PIPE,
+                       stderr=subprocess.PIPE, timeout=60)
+    assert r.returncode != 0
+    assert b"no usable GB300 device" in r.stdout

@@ -206,3 +206,15 @@ def test_server_bad_query_fails_alone():
         srv.close()
     assert res[1]["status"] == -1
     assert res[0]["status"] == 0 and res[2]["status"] == 0
+
+
+def test_serving_daemon_equals_run_queries(be):
+    """`gpubackend serve`: a stream of protocol inputs in one process gives,
+    query by query, what csim_run_queries gives with the same seeds."""
+    cases = e2e_cases()
+    rc, out = backend.serve_backend([c["input"] for c in cases], seed=5000, timeout=300)
+    assert rc == 0 and len(out) == len(cases)
+    ref = be.run_queries([{"input": c["input"], "seed": 5000 + i} for i, c in enumerate(cases)], batched=True)
+    for (st, num, den), r in zip(out, ref):
+        assert st == 0
+        assert (num, den) == (r["numerator"], r["denominator"])
