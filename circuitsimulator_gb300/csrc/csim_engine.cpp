@@ -100,7 +100,8 @@ struct Decomp {
     int t = 0, exact = 0, k = 0;
     int64_t chi = 0;
     std::vector<uint64_t> L;
-    uint64_t* cw = nullptr;      // codewords (exact == 0)
+    uint64_t* cw = nullptr;      // codewords (exact == 0), term order
+    uint64_t* cws = nullptr;     // the same in ordered_codewords' order, for sampled estimators
     csim_state* phis = nullptr;  // term states: prepH (exact == 1), prepL (exact projector on |L>)
     uint64_t* dL = nullptr;
     size_t bytes = 0;
@@ -108,9 +109,11 @@ struct Decomp {
     int64_t last_use = 0;
     void release() {
         if (cw) cudaFree(cw);
+        if (cws) cudaFree(cws);
         if (phis) cudaFree(phis);
         if (dL) cudaFree(dL);
         cw = nullptr;
+        cws = nullptr;
         phis = nullptr;
         dL = nullptr;
     }
@@ -346,7 +349,7 @@ int Engine::ensure_decomp(QueryRec* r, bool need_phis, bool force, Decomp** out)
     const int64_t chi = r->chi;
     const bool want_cw = !r->exact, want_phis = r->exact || need_phis;
     size_t add = 0;
-    if (!d && want_cw) add += align_up((size_t)chi * 8) + kAlign;
+    if (!d && want_cw) add += 2 * align_up((size_t)chi * 8) + kAlign;
     if (want_phis && !(d && d->phis)) add += align_up((size_t)chi * sizeof(csim_state));
     if (add && resident_ + (int64_t)add > budget_) {  // evict unused decompositions, least recently used first
         std::vector<std::pair<int64_t, std::vector<uint64_t>>> lru;
@@ -374,12 +377,16 @@ int Engine::ensure_decomp(QueryRec* r, bool need_phis, bool force, Decomp** out)
         decomps_[key] = std::move(nd);
         if (want_cw) {
             if (cudaMalloc(&d->cw, (size_t)chi * 8) != cudaSuccess ||
+                cudaMalloc(&d->cws, (size_t)chi * 8) != cudaSuccess ||
                 cudaMalloc(&d->dL, 8 * (size_t)CSIM_MAX_QUBITS) != cudaSuccess) {
                 d->release();
                 decomps_.erase(key);
                 return fail(ctx_, CSIM_ERR_NOMEM, "codeword table of 2^%d terms", r->k);
             }
-            d->bytes += align_up((size_t)chi * 8) + kAlign;
+            d->bytes += 2 * align_up((size_t)chi * 8) + kAlign;
+            std::vector<uint64_t> ordered;
+            ordered_codewords(d->L.data(), d->k, ordered);
+            CK(cudaMemcpy(d->cws, ordered.data(), (size_t)chi * 8, cudaMemcpyHostToDevice));
             uint64_t rows[CSIM_MAX_QUBITS] = {0};
             for (int i = 0; i < d->k; i++) rows[i] = d->L[i];
             CK(cudaMemcpy(d->dL, rows, sizeof(rows), cudaMemcpyHostToDevice));
@@ -629,7 +636,8 @@ int Engine::launch_round() {
             int64_t& c = cur[bucket_of_[e->t]];
             hrange[2 * i] = c;
             for (int64_t j = jb; j < e->chi; j += span_tp)
-                hitems[c++] = csim::PairItem{i, j, std::min(span_tp, e->chi - j), diag, r->dec->cw, nullptr};
+                hitems[c++] = csim::PairItem{i, j, std::min(span_tp, e->chi - j), diag,
+                                             e->kind == 1 ? r->dec->cws : r->dec->cw, nullptr};
             hrange[2 * i + 1] = c;
         } else {
             hrange[2 * i] = iw;

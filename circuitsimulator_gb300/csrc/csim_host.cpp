@@ -345,12 +345,26 @@ extern "C" int csim_prep_l(csim_ctx* ctx, int32_t t, const uint64_t* L, int32_t 
 // ---------------------------------------------------------------- hot path
 namespace {
 
-// the terms |phi_j>, j in [j0, j0+nj): codewords (|L>) or prepared states (|H^t>)
+// the terms |phi_j>, j in [j0, j0+nj): codewords (|L>) or prepared states (|H^t>).
+// ordered: all 2^k codewords in ordered_codewords' order (sums over all terms only)
 int stage_terms(csim_ctx* ctx, int t, int exact, const uint64_t* L, int k, int64_t j0, int64_t nj,
-                uint64_t** dcw, csim_state** dphis) {
+                uint64_t** dcw, csim_state** dphis, bool ordered = false) {
     *dcw = nullptr;
     *dphis = nullptr;
     void* v;
+    if (!exact && ordered && j0 == 0 && nj == ((int64_t)1 << k)) {
+        std::vector<uint64_t> key(L, L + k);
+        key.push_back((uint64_t)k);
+        if (key != ctx->cw_key || !ctx->buf[kBufCwOrdered]) {
+            std::vector<uint64_t> cw;
+            ordered_codewords(L, k, cw);
+            uint64_t* d;
+            CKR(dput(ctx, kBufCwOrdered, cw.data(), cw.size(), &d));
+            ctx->cw_key = key;
+        }
+        *dcw = (uint64_t*)ctx->buf[kBufCwOrdered];
+        return 0;
+    }
     if (!exact) {
         uint64_t* dL;
         CKR(dput(ctx, kBufL, L, (size_t)k, &dL));
@@ -461,7 +475,7 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
     cum_table(t, hcum);
     uint64_t* dcw;
     csim_state* dphis;
-    CKR(stage_terms(ctx, t, exact, L, k, 0, chi, &dcw, &dphis));
+    CKR(stage_terms(ctx, t, exact, L, k, 0, chi, &dcw, &dphis, /*ordered=*/true));
 
     const int64_t batch = 1 << 14;
     std::vector<uint32_t> words;

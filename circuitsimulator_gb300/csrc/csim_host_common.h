@@ -142,6 +142,26 @@ inline void draw_state_words(LibcRand& lr, int n, const double* cum, std::vector
     for (int64_t i = 0; i < rest; i++) words.push_back((uint32_t)lr.next());
 }
 
+// The 2^k codewords of L in the order the thread-per-pair kernel walks them in
+// a sampled estimator: by weight, then by value (high positions first).  The
+// 32 pairs of a warp then have the same number of shrinks, and mostly the
+// same leading zero pattern, so the warp's predicated loops waste few lanes.
+// A state's sum over all terms is exact, so it does not depend on the order.
+inline void ordered_codewords(const uint64_t* L, int k, std::vector<uint64_t>& out) {
+    const int64_t chi = (int64_t)1 << k;
+    out.resize((size_t)chi);
+    uint64_t x = 0;
+    out[0] = 0;
+    for (int64_t i = 1; i < chi; i++) {  // Gray code: one row of L per step
+        x ^= L[k - 1 - __builtin_ctzll((unsigned long long)i)];
+        out[(size_t)i] = x;
+    }
+    std::sort(out.begin(), out.end(), [](uint64_t a, uint64_t b) {
+        const int pa = __builtin_popcountll(a), pb = __builtin_popcountll(b);
+        return pa != pb ? pa < pb : a < b;
+    });
+}
+
 // z0 + z1 w + z2 w^2 + z3 w^3 (w = e^{i pi/4}) times 2^{-P/2}, P even
 inline void zomega_to_complex(const __int128* z, int P, double* re, double* im) {
     const double s = 0.70710678118654752440;
@@ -167,7 +187,7 @@ inline double sqrt_half_power(int c) {  // projfactor of innerprod.c:104-111: c 
 enum BufId {
     kBufA, kBufB, kBufEps, kBufP, kBufM, kBufXi, kBufZeta, kBufAlpha, kBufCode, kBufWords, kBufOffsets,
     kBufCum, kBufCodewords, kBufAcc, kBufAccDiag, kBufPhis, kBufIdx, kBufConsumed, kBufPm, kBufPz, kBufPx,
-    kBufL, kBufParts, kBufPartsDiag, kNumBufs
+    kBufL, kBufParts, kBufPartsDiag, kBufCwOrdered, kNumBufs
 };
 
 class Engine;                     // csim_engine.cpp: the batched query engine
@@ -191,6 +211,7 @@ struct csim_ctx {
     int per_thread = 16;  // CSIM_OPT_PER_THREAD
     cudaEvent_t ev[4] = {};
     Engine* engine = nullptr;  // created by the first batched csim_run_queries
+    std::vector<uint64_t> cw_key;  // (k, rows of L) of the ordered codeword table in kBufCwOrdered
 };
 
 namespace csim_host {
