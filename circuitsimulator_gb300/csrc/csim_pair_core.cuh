@@ -153,10 +153,30 @@ template <class W>
 CSIM_HD inline W wmask(bool b) {  // all ones if b
     return (W)0 - (W)(b ? 1 : 0);
 }
+// bit reversal, so that a row loop can walk a mask from its top bit down
+CSIM_HD inline uint32_t wbrev(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+    return __brev(x);
+#else
+    uint32_t r = 0;
+    for (int i = 0; i < 32; i++) r |= ((x >> i) & 1u) << (31 - i);
+    return r;
+#endif
+}
+CSIM_HD inline uint64_t wbrev(uint64_t x) {
+#if defined(__CUDA_ARCH__)
+    return __brevll(x);
+#else
+    return ((uint64_t)wbrev((uint32_t)x) << 32) | wbrev((uint32_t)(x >> 32));
+#endif
+}
+// all ones if the top bit of x is set (an arithmetic shift)
+CSIM_HD inline uint32_t topmask(uint32_t x) { return (uint32_t)((int32_t)x >> 31); }
+CSIM_HD inline uint64_t topmask(uint64_t x) { return (uint64_t)((int64_t)x >> 63); }
 
 struct PairRegs {
     int k, Q;
-    uint64_t h;       // position space (n bits)
+    uint64_t h;       // h at the codeword's zero positions, compact (bit j = j-th zero, descending)
     uint64_t D1, D2;  // row space (k bits)
 };
 
@@ -190,8 +210,12 @@ CSIM_HD inline W shrink_row(W r, W Ji, W U, W mi, W bu, W bc, W bj) {
 }
 
 // Shrink by e_q (alpha = 0), stabilizer.c:500-585, for a symmetric J.
-// `act`: this lane has a shrink to do.  Returns 0 EMPTY, 1 SAME, 2 SUCCESS
-// (1 when inactive).  All lanes must call it together.
+// The zero columns of the pair's codeword are kept compact, in the order they
+// are shrunk by (descending q): slot j of sGT holds column q_j of G as a row
+// mask and bit j of s.h holds h's bit q_j; no other column or bit of h is
+// read again.  This shrinks by slot `q`; slots q+1..nz-1 are the columns of
+// the later shrinks.  `act`: this lane has a shrink to do.  Returns 0 EMPTY,
+// 1 SAME, 2 SUCCESS (1 when inactive).  All lanes must call it together.
 //
 // With R = I + U e_i^T (U = S \ {i}, i = max S) and J symmetric,
 //   R J R^T = J + U Ji^T + Ji U^T + J_ii U U^T,
@@ -201,7 +225,7 @@ CSIM_HD inline W shrink_row(W r, W Ji, W U, W mi, W bu, W bc, W bj) {
 // corrections of updateDJ are U & Ji, and updateQD's J.y is column kk of the
 // result, i.e. C with bit i taken from bit kk of C.
 template <class W>
-CSIM_HD inline int tp_shrink(PairRegs& s, uint64_t* sJ, uint64_t* sGT, int st, int q, uint64_t zrem, bool act) {
+CSIM_HD inline int tp_shrink(PairRegs& s, uint64_t* sJ, uint64_t* sGT, int st, int q, int nz, bool act) {
     using T = WordTraits<W>;
     const int k = s.k;
     const W km = wlow<W>(k);
@@ -215,20 +239,18 @@ CSIM_HD inline int tp_shrink(PairRegs& s, uint64_t* sJ, uint64_t* sGT, int st, i
 
     // G, column form: rows in U get the pivot row, row kk moves to slot i;
     // h gets the pivot row when beta = 1 (stabilizer.c:530-533, 557, 569-573)
-    const int nz = upd ? hd_popc64(zrem) : 0;
-    const int NZ = uniform_max(nz);
-    uint64_t z = zrem, hflip = 0ull;
-    for (int t = 0; t < NZ; t++) {
-        if (t < nz) {
-            const int c = hd_ffs64(z) - 1;
-            const uint64_t mc = z & (0ull - z);  // lowest remaining zero column, as a mask
-            z ^= mc;
+    const int nrem = upd ? nz - 1 - q : 0;
+    const int NR = uniform_max(nrem);
+    uint64_t hflip = 0ull;
+    for (int t = 0; t < NR; t++) {
+        if (t < nrem) {
+            const int c = q + 1 + t;
             W g = (W)RG(c);
             const bool gi = (g & mi) != (W)0;
             g ^= U & wmask<W>(gi);
             g = (g & ~mi) | (mi & wmask<W>((g & mk) != (W)0));
             RG(c) = (uint64_t)g;
-            if (gi) hflip |= mc;
+            if (gi) hflip |= bit1(c);
         }
     }
     if (beta) s.h ^= hflip;
@@ -242,21 +264,24 @@ CSIM_HD inline int tp_shrink(PairRegs& s, uint64_t* sJ, uint64_t* sGT, int st, i
     // beyond k are outside the block and never read again
     const int KX = uniform_max(upd ? k : 0);
     if (upd) {
-        // two rows per 16-byte access (the pair buffer holds an even number of rows)
-        W cu = U, cc = C, cj = Jk;
+        // two rows per 16-byte access (the pair buffer holds an even number of rows);
+        // the coefficient masks walk bit-reversed copies from the top bit down
+        W cu = wbrev(U), cc = wbrev(C), cj = wbrev(Jk);
 #if defined(__CUDA_ARCH__)
 #pragma unroll 2
 #endif
         for (int x = 0; x < KX; x += 2) {
             U64x2* pr = reinterpret_cast<U64x2*>(&RJ(x));
             U64x2 v = *pr;
-            v.a = (uint64_t)shrink_row<W>((W)v.a, Ji, U, mi, wmask<W>(cu & 1), wmask<W>(cc & 1), wmask<W>(cj & 1));
-            v.b = (uint64_t)shrink_row<W>((W)v.b, Ji, U, mi, wmask<W>((cu >> 1) & 1), wmask<W>((cc >> 1) & 1),
-                                          wmask<W>((cj >> 1) & 1));
+            v.a = (uint64_t)shrink_row<W>((W)v.a, Ji, U, mi, topmask(cu), topmask(cc), topmask(cj));
+            cu <<= 1;
+            cc <<= 1;
+            cj <<= 1;
+            v.b = (uint64_t)shrink_row<W>((W)v.b, Ji, U, mi, topmask(cu), topmask(cc), topmask(cj));
+            cu <<= 1;
+            cc <<= 1;
+            cj <<= 1;
             *pr = v;
-            cu >>= 2;
-            cc >>= 2;
-            cj >>= 2;
         }
     }
     if (upd && i != kk) RJ(i) = (uint64_t)((Jk & ~mi) | (mi & wmask<W>(wget<W>(Jk, kk))));
@@ -324,17 +349,18 @@ CSIM_HD inline void tp_exp_sum(PairRegs& s, uint64_t* sJ, int st, bool act, int&
         if (upd) {
             // rows a and kk are rewritten below; the pass itself is branch-free
             const W ma = wbit<W>(a), mk = wbit<W>(kk & (T::bits - 1));
-            W cu = U, cc = C, cj = Jk;
+            W cu = wbrev(U), cc = wbrev(C), cj = wbrev(Jk);
             for (int x = 0; x < KX; x++) {
                 W r = (W)RJ(x);
-                r ^= Ja & wmask<W>(cu & 1);
-                r ^= U & wmask<W>(cc & 1);
+                const W bc = topmask(cc);
+                r ^= Ja & topmask(cu);
+                r ^= U & bc;
                 // swap bits a and kk: bit a <- J'[x][kk] = bit x of Jk, bit kk <- J'[x][a] = bit x of C
-                r = (r & ~(ma | mk)) | (ma & wmask<W>(cj & 1)) | (mk & wmask<W>(cc & 1));
+                r = (r & ~(ma | mk)) | (ma & topmask(cj)) | (mk & bc);
                 RJ(x) = (uint64_t)r;
-                cu >>= 1;
-                cc >>= 1;
-                cj >>= 1;
+                cu <<= 1;
+                cc <<= 1;
+                cj <<= 1;
             }
         }
         if (upd && a != kk) {
@@ -486,23 +512,26 @@ CSIM_HD inline void pair_l(bool valid, int n, int k1, int Q, uint64_t h, uint64_
             v.b = pJ[r + 1];
             *reinterpret_cast<U64x2*>(&RJ(r)) = v;
         }
-    uint64_t zeros = valid ? (~x & lowmask(n)) : 0ull;
-    for (uint64_t zz = zeros; zz; zz &= zz - 1) {
-        const int c = hd_ffs64(zz) - 1;
-        RG(c) = pGT[c];
+    // the zero columns of x, descending (the order of the shrinks), compact
+    int nz = 0;
+    uint64_t hz = 0ull;
+    for (uint64_t zz = valid ? (~x & lowmask(n)) : 0ull; zz; nz++) {
+        const int c = 63 - hd_clz64(zz);
+        zz &= ~bit1(c);
+        RG(nz) = pGT[c];
+        hz |= (uint64_t)getbit(h, c) << nz;
     }
+    s.h = hz;
     eps = 0;
     p = 0;
     m = 0;
     bool alive = valid;
-    const int NZ = uniform_max(hd_popc64(zeros));
+    const int NZ = uniform_max(nz);
     for (int it = 0; it < NZ; it++) {
-        const bool act = alive && zeros != 0ull;
-        const int q = act ? 63 - hd_clz64(zeros) : 0;
-        if (act) zeros &= ~bit1(q);
+        const bool act = alive && it < nz;
         const bool wide = uniform_max(alive ? s.k : 0) > 32;
-        const int r = wide ? tp_shrink<uint64_t>(s, sJ, sGT, st, q, zeros, act)
-                           : tp_shrink<uint32_t>(s, sJ, sGT, st, q, zeros, act);
+        const int r = wide ? tp_shrink<uint64_t>(s, sJ, sGT, st, it, nz, act)
+                           : tp_shrink<uint32_t>(s, sJ, sGT, st, it, nz, act);
         if (act && r == 0) alive = false;
     }
     if (uniform_max(alive ? s.k : 0) > 32) tp_exp_sum<uint64_t>(s, sJ, st, alive, eps, p, m, err);
