@@ -355,12 +355,14 @@ int stage_terms(csim_ctx* ctx, int t, int exact, const uint64_t* L, int k, int64
     if (!exact && ordered && j0 == 0 && nj == ((int64_t)1 << k)) {
         std::vector<uint64_t> key(L, L + k);
         key.push_back((uint64_t)k);
+        key.push_back((uint64_t)t);
         if (key != ctx->cw_key || !ctx->buf[kBufCwOrdered]) {
             std::vector<uint64_t> cw;
             ordered_codewords(L, k, cw);
             uint64_t* d;
             CKR(dput(ctx, kBufCwOrdered, cw.data(), cw.size(), &d));
             ctx->cw_key = key;
+            ctx->cw_split = light_split(cw, t);
         }
         *dcw = (uint64_t*)ctx->buf[kBufCwOrdered];
         return 0;
@@ -425,8 +427,8 @@ extern "C" int csim_term_products(csim_ctx* ctx, int32_t t, int32_t exact, const
         CKR(dbuf(ctx, kBufM, c * nj * 4, &v));
         int* dm = (int*)v;
         const int rc = (!exact && ctx->pair_kernel == 0 && sym)
-                           ? csim::launch_terms_tp(launch_of(ctx), t, dcw, (const csim::GState*)dth, nullptr, c, j0, nj,
-                                                   ctx->per_thread, 2 * t, nullptr, de, dp, dm)
+                           ? csim::launch_terms_tp(launch_of(ctx), t, t, dcw, (const csim::GState*)dth, nullptr, c, j0,
+                                                   nj, ctx->per_thread, 2 * t, nullptr, 0, 0, de, dp, dm)
                            : csim::launch_terms(launch_of(ctx), nr, exact ? 1 : 0, dcw, (const csim::GState*)dphis,
                                                 (const csim::GState*)dth, nullptr, c, j0, nj, 64, 2 * t, nullptr,
                                                 nullptr, de, dp, dm);
@@ -517,11 +519,21 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
         __int128* dpart = (__int128*)v;
         CK(cudaMemsetAsync(dpart, 0, nparts * sizeof(__int128), ctx->stream));
         CK(cudaEventRecord(ctx->ev[1], ctx->stream));
-        const int rc = tp ? csim::launch_terms_tp(launch_of(ctx), t, dcw, dth, dcode, c, 0, chi, ctx->per_thread, P2,
-                                                  dpart, nullptr, nullptr, nullptr)
-                          : csim::launch_terms(launch_of(ctx), nr, exact ? 1 : 0, dcw, (const csim::GState*)dphis, dth,
-                                               dcode, c, 0, chi, (int)chunk, P2, dpart, nullptr, nullptr, nullptr,
-                                               nullptr);
+        int rc = 0;
+        if (tp) {
+            // terms [0, jb): every zero count; terms [jb, chi): at most light_zeros(t) zeros
+            const int64_t span = 64 * (int64_t)ctx->per_thread;
+            const int64_t jb = std::min(chi, (ctx->cw_split + span - 1) / span * span);
+            if (jb > 0)
+                rc |= csim::launch_terms_tp(launch_of(ctx), t, t, dcw, dth, dcode, c, 0, jb, ctx->per_thread, P2,
+                                            dpart, nchunks, 0, nullptr, nullptr, nullptr);
+            if (jb < chi)
+                rc |= csim::launch_terms_tp(launch_of(ctx), t, light_zeros(t), dcw + jb, dth, dcode, c, jb, chi - jb,
+                                            ctx->per_thread, P2, dpart, nchunks, jb / span, nullptr, nullptr, nullptr);
+        } else {
+            rc = csim::launch_terms(launch_of(ctx), nr, exact ? 1 : 0, dcw, (const csim::GState*)dphis, dth, dcode, c,
+                                    0, chi, (int)chunk, P2, dpart, nullptr, nullptr, nullptr, nullptr);
+        }
         if (rc) return fail(ctx, CSIM_ERR_CUDA, "term launch failed");
         CK(cudaEventRecord(ctx->ev[2], ctx->stream));
         CKR(dbuf(ctx, kBufAcc, (size_t)c * 4 * sizeof(__int128), &v));

@@ -162,6 +162,21 @@ inline void ordered_codewords(const uint64_t* L, int k, std::vector<uint64_t>& o
     });
 }
 
+// Zero bound of the "light" part of an ordered codeword table: codewords with
+// at most this many zeros run in a launch whose G-column slots are sized for
+// it, which leaves shared memory for more resident blocks.  Weights of a
+// random code's codewords cluster at t/2, so most terms fall in this part.
+inline int light_zeros(int t) { return std::min(t, (3 * t + 4) / 5); }
+
+// First index of an ordered table (ascending weight) from which every codeword
+// has at most light_zeros(t) zeros.
+inline int64_t light_split(const std::vector<uint64_t>& cw, int t) {
+    const int wmin = t - light_zeros(t);
+    int64_t j = 0;
+    while (j < (int64_t)cw.size() && __builtin_popcountll(cw[(size_t)j]) < wmin) j++;
+    return j;
+}
+
 // z0 + z1 w + z2 w^2 + z3 w^3 (w = e^{i pi/4}) times 2^{-P/2}, P even
 inline void zomega_to_complex(const __int128* z, int P, double* re, double* im) {
     const double s = 0.70710678118654752440;
@@ -212,6 +227,7 @@ struct csim_ctx {
     cudaEvent_t ev[4] = {};
     Engine* engine = nullptr;  // created by the first batched csim_run_queries
     std::vector<uint64_t> cw_key;  // (k, rows of L) of the ordered codeword table in kBufCwOrdered
+    int64_t cw_split = 0;          // first index of that table whose codewords have <= light_zeros(t) zeros
 };
 
 namespace csim_host {

@@ -42,11 +42,14 @@ int launch_terms(const Launch& L, int nr, int mode, const uint64_t* codewords, c
                  __int128* part, __int128* part_diag, int* eps_o, int* p_o, int* m_o);
 int launch_reduce_parts(const Launch& L, const __int128* part, int64_t ntheta, int64_t nchunks, __int128* acc);
 
-// thread-per-pair kernel for terms of |L> (csim_terms_tp.cu); nmax >= every theta's n.
-// Work item = (theta, block of 64 * per_thread terms): part holds 4 int128 per item.
-int launch_terms_tp(const Launch& L, int nmax, const uint64_t* codewords, const GState* theta, const int* code,
-                    int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P, __int128* part, int* eps_o,
-                    int* p_o, int* m_o);
+// thread-per-pair kernel for terms of |L> (csim_terms_tp.cu); nmax >= every theta's n,
+// gmax >= the zeros of every codeword in [j0, j0 + nj) (gmax = nmax always holds).
+// codewords[0] is term j0's codeword.
+// Work item = (theta a, block cb of 64 * per_thread terms): 4 int128 partial sums at
+// part[4 * (a * part_stride + part_base + cb)].
+int launch_terms_tp(const Launch& L, int nmax, int gmax, const uint64_t* codewords, const GState* theta,
+                    const int* code, int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P, __int128* part,
+                    int64_t part_stride, int64_t part_base, int* eps_o, int* p_o, int* m_o);
 int64_t terms_tp_blocks(int64_t nj, int per_thread);
 
 }  // namespace csim

@@ -498,7 +498,13 @@ CSIM_HD inline void zacc(__int128 (&z)[4], int eps, int p, int m, int P, int& er
 // exceeds 32 and 32-bit after that.
 CSIM_HD inline void pair_l(bool valid, int n, int k1, int Q, uint64_t h, uint64_t D1, uint64_t D2, const uint64_t* pJ,
                            const uint64_t* pGT, uint64_t x, uint64_t* sJ, uint64_t* sGT, int st, int& eps, int& p,
-                           int& m, int& err) {
+                           int& m, int& err, int gmax = 64) {
+    // sGT has gmax slots: a codeword with more zeros is refused (the caller
+    // bounds the zeros of the codewords it passes)
+    if (valid && hd_popc64(~x & lowmask(n)) > gmax) {
+        err |= kErrRange;
+        valid = false;
+    }
     PairRegs s;
     s.k = k1;
     s.Q = Q;

@@ -140,8 +140,8 @@ extern "C" int csim_single_projector_samples_static(int32_t device, const csim_p
                                    states, nullptr) ||
         csim::launch_project(Lh, nr, states, count, nstabs, (const int*)(base + kOffPm),
                              (const uint64_t*)(base + kOffPz), (const uint64_t*)(base + kOffPx), code) ||
-        csim::launch_terms_tp(Lh, t, cw, states, code, count, 0, chi, kPerThread, 2 * t, part, nullptr, nullptr,
-                              nullptr) ||
+        csim::launch_terms_tp(Lh, t, t, cw, states, code, count, 0, chi, kPerThread, 2 * t, part, nblk, 0, nullptr,
+                              nullptr, nullptr) ||
         csim::launch_reduce_parts(Lh, part, count, nblk, acc))
         return CSIM_ERR_CUDA;
 

@@ -45,12 +45,14 @@ __device__ __forceinline__ __int128 shfl_xor_i128(__int128 v, int m) {
     return (__int128)(((unsigned __int128)hi << 64) | lo);
 }
 
-// Work item = (theta a, block of kTP * per_thread consecutive terms).  Thread t
-// takes terms jb + t + kTP * r, r < per_thread.  Partial sums: 4 int128 per item.
+// Work item = (theta a, block cb of kTP * per_thread consecutive terms).  Thread t
+// takes terms jb + t + kTP * r, r < per_thread.  Partial sums: 4 int128 per item,
+// at part[4 * (a * part_stride + part_base + cb)].  gmax bounds the zeros of
+// every codeword in [j0, j0 + nj) and sizes the G-column slots.
 __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, const GState* theta, const int* code,
                                                   int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P,
-                                                  int nmax, __int128* part, int* eps_o, int* p_o, int* m_o,
-                                                  int* err) {
+                                                  int nmax, int gmax, __int128* part, int64_t part_stride,
+                                                  int64_t part_base, int* eps_o, int* p_o, int* m_o, int* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TPShared& sh = *reinterpret_cast<TPShared*>(smem_raw);
     const int tid = threadIdx.x;
@@ -102,7 +104,7 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
                 const uint64_t x = valid ? codewords[j - j0] : 0ull;
                 int eps, pp, mm;
                 pc::pair_l(valid, n, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ, sh.pGT, x, sJ + 2 * tid, sGT + tid, kTP,
-                           eps, pp, mm, e);
+                           eps, pp, mm, e, gmax);
                 if (!valid) continue;
                 pc::zacc(z, eps, pp, mm, P, e);
                 if (eps_o) {
@@ -122,7 +124,7 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
             if (tid < 4) {
                 __int128 acc = 0;
                 for (int w = 0; w < kTP / 32; w++) acc += sh.red[w][tid];
-                part[4 * item + tid] = acc;
+                part[4 * (a * part_stride + part_base + cb) + tid] = acc;
             }
         }
     }
@@ -130,19 +132,20 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
     if (e && (tid & 31) == 0) atomicOr(err, e);
 }
 
-size_t terms_tp_smem(int nmax) {
-    return sizeof(TPShared) + (size_t)(((nmax + 1) & ~1) + nmax) * kTP * sizeof(uint64_t);
+size_t terms_tp_smem(int nmax, int gmax) {
+    return sizeof(TPShared) + (size_t)(((nmax + 1) & ~1) + gmax) * kTP * sizeof(uint64_t);
 }
 
-int launch_terms_tp(const Launch& L, int nmax, const uint64_t* codewords, const GState* theta, const int* code,
-                    int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P, __int128* part, int* eps_o,
-                    int* p_o, int* m_o) {
+int launch_terms_tp(const Launch& L, int nmax, int gmax, const uint64_t* codewords, const GState* theta,
+                    const int* code, int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P, __int128* part,
+                    int64_t part_stride, int64_t part_base, int* eps_o, int* p_o, int* m_o) {
     if (ntheta <= 0 || nj <= 0) return 0;
-    if (nmax < 1 || nmax > 64) return -1;
+    if (nmax < 1 || nmax > 64 || gmax < 0 || gmax > nmax) return -1;
     const int64_t span = (int64_t)kTP * per_thread;
     const int64_t nblk = (nj + span - 1) / span;
-    const size_t smem = terms_tp_smem(nmax);
-    if (cudaFuncSetAttribute(k_terms_tp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)terms_tp_smem(64)) !=
+    if (part && part_stride < part_base + nblk) return -1;
+    const size_t smem = terms_tp_smem(nmax, gmax);
+    if (cudaFuncSetAttribute(k_terms_tp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)terms_tp_smem(64, 64)) !=
         cudaSuccess)
         return -1;
     int per_sm = 0;
@@ -151,8 +154,8 @@ int launch_terms_tp(const Launch& L, int nmax, const uint64_t* codewords, const 
     const int64_t items = ntheta * nblk;
     int64_t grid = (int64_t)L.num_sms * per_sm;
     if (grid > items) grid = items;
-    k_terms_tp<<<(int)grid, kTP, smem, L.stream>>>(codewords, theta, code, ntheta, j0, nj, per_thread, P, nmax, part,
-                                                    eps_o, p_o, m_o, L.d_err);
+    k_terms_tp<<<(int)grid, kTP, smem, L.stream>>>(codewords, theta, code, ntheta, j0, nj, per_thread, P, nmax, gmax,
+                                                    part, part_stride, part_base, eps_o, p_o, m_o, L.d_err);
     (*L.launches)++;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
