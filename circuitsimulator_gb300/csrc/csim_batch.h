@@ -45,13 +45,16 @@ struct CodeDesc {
 
 int launch_draw_project(const Launch& L, const DrawDesc* desc, int64_t count, GState* out, int* code);
 // resident blocks per SM of k_items_tp launched for states of up to nmax qubits
-int items_tp_occupancy(int nmax);
+// and codewords of up to gmax zeros
+int items_tp_occupancy(int nmax, int gmax);
 int launch_items_tp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,
-                    int per_thread, int nmax, __int128* part, __int128* part_diag);
+                    int per_thread, int nmax, int gmax, __int128* part, __int128* part_diag);
 int launch_items_warp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,
                       __int128* part, __int128* part_diag);
-// per-slot sums of item partials; slot s owns items [range[2s], range[2s+1])
-int launch_reduce_slots(const Launch& L, const __int128* part, const int64_t* range, int64_t nslots, __int128* out);
+// per-slot sums of item partials; slot s owns items [range[2s], range[2s+1]) and,
+// if range2 is not null, [range2[2s], range2[2s+1])
+int launch_reduce_slots(const Launch& L, const __int128* part, const int64_t* range, const int64_t* range2,
+                        int64_t nslots, __int128* out);
 int launch_codewords_multi(const Launch& L, const CodeDesc* codes, int ncodes, int64_t maxchi, uint64_t* out);
 
 }  // namespace csim

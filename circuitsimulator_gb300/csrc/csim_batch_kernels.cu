@@ -101,8 +101,8 @@ __device__ __forceinline__ __int128 shfl_xor_128(__int128 v, int m) {
 // One block per item: up to kTPB * per_thread terms of one state.  part[4w..]:
 // the item's sum; part_diag[4w..]: the term j == item.diag (exactProjector).
 __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_t nitems, const GState* states,
-                                                   const int* codes, int per_thread, int nmax, __int128* part,
-                                                   __int128* part_diag, int* err) {
+                                                   const int* codes, int per_thread, int nmax, int gmax,
+                                                   __int128* part, __int128* part_diag, int* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ItemShared& sh = *reinterpret_cast<ItemShared*>(smem_raw);
     const int tid = threadIdx.x;
@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_
                 const uint64_t x = valid ? it.cw[j] : 0ull;
                 int eps, pp, mm;
                 pc::pair_l(valid, n, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ, sh.pGT, x, sJ + 2 * tid, sGT + tid, kTPB,
-                           eps, pp, mm, e);
+                           eps, pp, mm, e, gmax);
                 if (!valid) continue;
                 pc::zacc(z, eps, pp, mm, P, e);
                 if (j == it.diag) {
@@ -224,13 +224,16 @@ __global__ void __launch_bounds__(256) k_items_warp(const PairItem* items, int64
     flush(e, err);
 }
 
-// slot s sums the items [range[2s], range[2s+1])
-__global__ void k_reduce_slots(const __int128* part, const int64_t* range, int64_t nslots, __int128* out) {
+// slot s sums the items [range[2s], range[2s+1]) and [range2[2s], range2[2s+1])
+__global__ void k_reduce_slots(const __int128* part, const int64_t* range, const int64_t* range2, int64_t nslots,
+                               __int128* out) {
     for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nslots * 4;
          w += (int64_t)gridDim.x * blockDim.x) {
         const int64_t s = w / 4, q = w % 4;
         __int128 acc = 0;
         for (int64_t i = range[2 * s]; i < range[2 * s + 1]; i++) acc += part[4 * i + q];
+        if (range2)
+            for (int64_t i = range2[2 * s]; i < range2[2 * s + 1]; i++) acc += part[4 * i + q];
         out[w] = acc;
     }
 }
@@ -251,8 +254,8 @@ __global__ void k_codewords_multi(const CodeDesc* codes, int ncodes, uint64_t* o
 }
 
 // ------------------------------------------------------------ launchers
-size_t items_tp_smem(int nmax) {
-    return sizeof(ItemShared) + (size_t)(((nmax + 1) & ~1) + nmax) * kTPB * sizeof(uint64_t);
+size_t items_tp_smem(int nmax, int gmax) {
+    return sizeof(ItemShared) + (size_t)(((nmax + 1) & ~1) + gmax) * kTPB * sizeof(uint64_t);
 }
 
 int launch_draw_project(const Launch& L, const DrawDesc* desc, int64_t count, GState* out, int* code) {
@@ -264,23 +267,24 @@ int launch_draw_project(const Launch& L, const DrawDesc* desc, int64_t count, GS
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-int items_tp_occupancy(int nmax) {
-    if (nmax < 1 || nmax > 64) return -1;
-    if (cudaFuncSetAttribute(k_items_tp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)items_tp_smem(64)) !=
+int items_tp_occupancy(int nmax, int gmax) {
+    if (nmax < 1 || nmax > 64 || gmax < 0 || gmax > nmax) return -1;
+    if (cudaFuncSetAttribute(k_items_tp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)items_tp_smem(64, 64)) !=
         cudaSuccess)
         return -1;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_items_tp, kTPB, items_tp_smem(nmax)) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_items_tp, kTPB, items_tp_smem(nmax, gmax)) !=
+        cudaSuccess)
         return -1;
     return per_sm;
 }
 
 int launch_items_tp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,
-                    int per_thread, int nmax, __int128* part, __int128* part_diag) {
+                    int per_thread, int nmax, int gmax, __int128* part, __int128* part_diag) {
     if (nitems <= 0) return 0;
-    if (nmax < 1 || nmax > 64) return -1;
-    const size_t smem = items_tp_smem(nmax);
-    if (cudaFuncSetAttribute(k_items_tp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)items_tp_smem(64)) !=
+    if (nmax < 1 || nmax > 64 || gmax < 0 || gmax > nmax) return -1;
+    const size_t smem = items_tp_smem(nmax, gmax);
+    if (cudaFuncSetAttribute(k_items_tp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)items_tp_smem(64, 64)) !=
         cudaSuccess)
         return -1;
     int per_sm = 0;
@@ -288,8 +292,8 @@ int launch_items_tp(const Launch& L, const PairItem* items, int64_t nitems, cons
         per_sm = 1;
     int64_t grid = (int64_t)L.num_sms * per_sm;
     if (grid > nitems) grid = nitems;
-    k_items_tp<<<(int)grid, kTPB, smem, L.stream>>>(items, nitems, states, codes, per_thread, nmax, part, part_diag,
-                                                    L.d_err);
+    k_items_tp<<<(int)grid, kTPB, smem, L.stream>>>(items, nitems, states, codes, per_thread, nmax, gmax, part,
+                                                    part_diag, L.d_err);
     (*L.launches)++;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
@@ -304,11 +308,12 @@ int launch_items_warp(const Launch& L, const PairItem* items, int64_t nitems, co
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-int launch_reduce_slots(const Launch& L, const __int128* part, const int64_t* range, int64_t nslots, __int128* out) {
+int launch_reduce_slots(const Launch& L, const __int128* part, const int64_t* range, const int64_t* range2,
+                        int64_t nslots, __int128* out) {
     if (nslots <= 0) return 0;
     int64_t blocks = (nslots * 4 + 255) / 256;
     if (blocks > (int64_t)L.num_sms * 16) blocks = (int64_t)L.num_sms * 16;
-    k_reduce_slots<<<(int)blocks, 256, 0, L.stream>>>(part, range, nslots, out);
+    k_reduce_slots<<<(int)blocks, 256, 0, L.stream>>>(part, range, range2, nslots, out);
     (*L.launches)++;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -44,8 +44,9 @@ using Clock = std::chrono::steady_clock;
 constexpr size_t kAlign = 256;
 inline size_t align_up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
 
-// at most one thread-per-pair launch per t
-constexpr int kBuckets = CSIM_MAX_QUBITS;
+// thread-per-pair launches: one per (occupancy class of t, light or not); a
+// light launch takes codewords of at most light_zeros(t) zeros
+constexpr int kBuckets = 2 * CSIM_MAX_QUBITS;
 
 // device memory that grows on demand (contents are not kept)
 struct DevBuf {
@@ -102,6 +103,7 @@ struct Decomp {
     std::vector<uint64_t> L;
     uint64_t* cw = nullptr;      // codewords (exact == 0), term order
     uint64_t* cws = nullptr;     // the same in ordered_codewords' order, for sampled estimators
+    int64_t light = 0;           // first index of cws with at most light_zeros(t) zeros
     csim_state* phis = nullptr;  // term states: prepH (exact == 1), prepL (exact projector on |L>)
     uint64_t* dL = nullptr;
     size_t bytes = 0;
@@ -220,7 +222,7 @@ class Engine {
         int occ_prev = -1;
         nbuckets_ = 0;
         for (int t = 1; t <= CSIM_MAX_QUBITS; t++) {
-            const int occ = csim::items_tp_occupancy(t);
+            const int occ = csim::items_tp_occupancy(t, t);
             if (occ <= 0) return fail(ctx_, CSIM_ERR_CUDA, "occupancy query failed");
             if (occ != occ_prev) nbuckets_++;
             occ_prev = occ;
@@ -386,6 +388,7 @@ int Engine::ensure_decomp(QueryRec* r, bool need_phis, bool force, Decomp** out)
             d->bytes += 2 * align_up((size_t)chi * 8) + kAlign;
             std::vector<uint64_t> ordered;
             ordered_codewords(d->L.data(), d->k, ordered);
+            d->light = light_split(ordered, d->t);
             CK(cudaMemcpy(d->cws, ordered.data(), (size_t)chi * 8, cudaMemcpyHostToDevice));
             uint64_t rows[CSIM_MAX_QUBITS] = {0};
             for (int i = 0; i < d->k; i++) rows[i] = d->L[i];
@@ -477,6 +480,12 @@ int Engine::admit(QueryRec* r, bool force, bool* admitted) {
     return 0;
 }
 
+// first item (of span terms, from term 0) of a sampled evaluation whose codewords all
+// have at most light_zeros(t) zeros in the ordered table
+static int64_t light_first_item(const Eval* e, int64_t span) {
+    return std::min((e->chi + span - 1) / span, (e->q->dec->light + span - 1) / span);
+}
+
 bool Engine::eval_ready(const Eval* e) const {
     if (e->next >= e->ns) return false;
     // rand() draws: H' continues G''s stream, so its states are drawn after all of G''s
@@ -550,7 +559,11 @@ int Engine::launch_round() {
         const int64_t jb = e->kind == 2 ? rs.slots[i].s : 0;
         const int64_t nj = e->chi - jb;
         if (!e->q->exact) {
-            nbucket[bucket_of_[e->t]] += (nj + span_tp - 1) / span_tp;
+            const int b = 2 * bucket_of_[e->t];
+            const int64_t nall = (nj + span_tp - 1) / span_tp;
+            const int64_t nlight = e->kind == 1 ? nall - light_first_item(e, span_tp) : 0;
+            nbucket[b] += nall - nlight;
+            nbucket[b + 1] += nlight;
         } else {
             niw += (nj + span_w - 1) / span_w;
         }
@@ -566,7 +579,8 @@ int Engine::launch_round() {
     const size_t o_words = align_up(o_proj + evix.size() * 192 * 8);
     const size_t o_items = align_up(o_words + words.size() * 4);
     const size_t o_range = align_up(o_items + (size_t)nitems * sizeof(csim::PairItem));
-    const size_t up_bytes = align_up(o_range + (size_t)ns * 16);
+    const size_t o_range2 = align_up(o_range + (size_t)ns * 16);
+    const size_t up_bytes = align_up(o_range2 + (size_t)ns * 16);
     // work block: states | parts | parts diag
     const size_t w_states = 0;
     const size_t w_part = align_up((size_t)ns * sizeof(csim_state));
@@ -598,7 +612,8 @@ int Engine::launch_round() {
     const uint32_t* dwords = (const uint32_t*)(db + o_words);
     csim::DrawDesc* hdesc = (csim::DrawDesc*)(hb + o_desc);
     csim::PairItem* hitems = (csim::PairItem*)(hb + o_items);
-    int64_t* hrange = (int64_t*)(hb + o_range);
+    int64_t* hrange = (int64_t*)(hb + o_range);    // a slot's items in its heavy or warp launch
+    int64_t* hrange2 = (int64_t*)(hb + o_range2);  // and in its light launch
     const double* dcum = (const double*)cum_.p;
     const csim::GState* dstates = (const csim::GState*)(wb + w_states);
     int64_t cur[kBuckets];
@@ -633,13 +648,23 @@ int Engine::launch_round() {
         const int64_t jb = e->kind == 2 ? s : 0;
         const int64_t diag = e->kind == 2 ? s : -1;
         if (!r->exact) {
-            int64_t& c = cur[bucket_of_[e->t]];
-            hrange[2 * i] = c;
-            for (int64_t j = jb; j < e->chi; j += span_tp)
-                hitems[c++] = csim::PairItem{i, j, std::min(span_tp, e->chi - j), diag,
-                                             e->kind == 1 ? r->dec->cws : r->dec->cw, nullptr};
-            hrange[2 * i + 1] = c;
+            // heavy items first, then light ones; a slot's items may sit in two
+            // launches, so its range is kept per slot in each (see below)
+            const int b = 2 * bucket_of_[e->t];
+            const int64_t jl = e->kind == 1 ? light_first_item(e, span_tp) * span_tp : e->chi;
+            int64_t& ch = cur[b];
+            int64_t& cl = cur[b + 1];
+            hrange[2 * i] = ch;
+            for (int64_t j = jb; j < std::min(jl, e->chi); j += span_tp)
+                hitems[ch++] = csim::PairItem{i, j, std::min(span_tp, e->chi - j), diag,
+                                              e->kind == 1 ? r->dec->cws : r->dec->cw, nullptr};
+            hrange[2 * i + 1] = ch;
+            hrange2[2 * i] = cl;
+            for (int64_t j = std::max(jl, jb); j < e->chi; j += span_tp)
+                hitems[cl++] = csim::PairItem{i, j, std::min(span_tp, e->chi - j), diag, r->dec->cws, nullptr};
+            hrange2[2 * i + 1] = cl;
         } else {
+            hrange2[2 * i] = hrange2[2 * i + 1] = 0;
             hrange[2 * i] = iw;
             for (int64_t j = jb; j < e->chi; j += span_w)
                 hitems[iw++] = csim::PairItem{i, j, std::min(span_w, e->chi - j), diag, nullptr,
@@ -659,16 +684,19 @@ int Engine::launch_round() {
         return fail(ctx_, CSIM_ERR_CUDA, "draw/project launch failed");
     CK(cudaEventRecord(rs.ev[1], ctx_->stream));
     const csim::PairItem* ditems = (const csim::PairItem*)(db + o_items);
-    for (int b = 0; b < kBuckets; b++)
-        if (nbucket[b] && csim::launch_items_tp(L, ditems + bstart[b], nbucket[b], dstates, dcode, per_thread_,
-                                                bucket_hi_[b], part + 4 * bstart[b], partd + 4 * bstart[b]))
+    for (int b = 0; b < 2 * nbuckets_; b++) {
+        const int nmax = bucket_hi_[b / 2], gmax = (b & 1) ? light_zeros(nmax) : nmax;
+        if (nbucket[b] && csim::launch_items_tp(L, ditems + bstart[b], nbucket[b], dstates, dcode, per_thread_, nmax,
+                                                gmax, part + 4 * bstart[b], partd + 4 * bstart[b]))
             return fail(ctx_, CSIM_ERR_CUDA, "pair launch failed");
+    }
     if (csim::launch_items_warp(L, ditems + nitp, niw, dstates, dcode, part + 4 * nitp, partd + 4 * nitp))
         return fail(ctx_, CSIM_ERR_CUDA, "pair launch failed");
     CK(cudaEventRecord(rs.ev[2], ctx_->stream));
     const int64_t* drange = (const int64_t*)(db + o_range);
-    if (csim::launch_reduce_slots(L, part, drange, ns, (__int128*)(dd + rs.off_sum)) ||
-        csim::launch_reduce_slots(L, partd, drange, ns, (__int128*)(dd + rs.off_sumd)))
+    const int64_t* drange2 = (const int64_t*)(db + o_range2);
+    if (csim::launch_reduce_slots(L, part, drange, drange2, ns, (__int128*)(dd + rs.off_sum)) ||
+        csim::launch_reduce_slots(L, partd, drange, drange2, ns, (__int128*)(dd + rs.off_sumd)))
         return fail(ctx_, CSIM_ERR_CUDA, "reduce launch failed");
     CK(cudaMemcpyAsync(rs.hdown.p, dd, down_bytes, cudaMemcpyDeviceToHost, ctx_->stream));
     CK(cudaEventRecord(rs.ev[3], ctx_->stream));
@@ -918,14 +946,19 @@ extern "C" int csim_run_queries(csim_ctx* ctx, int64_t nq, const csim_query* q, 
 void engine_free(Engine* engine) { delete engine; }
 
 // ---------------------------------------------------------------- server
+// Ownership and visibility: a query belongs to `tickets` from csim_submit to
+// csim_release.  Clients see a result only once the worker has published it
+// under the mutex (published = true); the engine's own `done` flag is the
+// worker's business.
 struct csim_server {
     csim_ctx* ctx = nullptr;
     std::unique_ptr<Engine> eng;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
-    std::deque<std::unique_ptr<QueryRec>> incoming;        // submitted, not yet planned
+    std::deque<QueryRec*> incoming;                        // submitted, not yet planned
     std::deque<QueryRec*> waiting;                         // planned, waiting for memory (worker only)
     std::map<int64_t, std::unique_ptr<QueryRec>> tickets;  // every unreleased query
+    std::map<int64_t, bool> published;                     // ticket -> result visible to clients
     int64_t next_ticket = 1;
     int64_t submitted = 0, completed = 0, failed = 0;
     csim_server_stats snap{};  // engine counters as of the worker's last step
@@ -941,19 +974,13 @@ void csim_server::run() {
     std::unique_lock<std::mutex> lk(mu);
     while (true) {
         // admit new queries (planning runs outside the lock)
-        std::deque<std::unique_ptr<QueryRec>> fresh;
+        std::deque<QueryRec*> fresh;
         fresh.swap(incoming);
         lk.unlock();
-        std::vector<QueryRec*> planned;
-        for (auto& r : fresh) {
-            eng->plan(r.get());
-            planned.push_back(r.get());
-        }
-        lk.lock();
-        for (auto& r : fresh) tickets[r->ticket] = std::move(r);
-        for (QueryRec* r : planned)
+        for (QueryRec* r : fresh) {
+            eng->plan(r);
             if (!r->done) waiting.push_back(r);
-        lk.unlock();
+        }
         int rc = 0;
         while (!waiting.empty()) {  // first come first served while memory allows
             QueryRec* r = waiting.front();
@@ -981,6 +1008,7 @@ void csim_server::run() {
             r->res.latency_s = std::chrono::duration<double>(now - r->t_submit).count();
             if (r->res.status) failed++;
             else completed++;
+            published[r->ticket] = true;
         }
         if (!eng->finished.empty()) cv_done.notify_all();
         eng->finished.clear();
@@ -992,22 +1020,18 @@ void csim_server::run() {
         if (eng->idle() && incoming.empty() && waiting.empty())
             cv_work.wait(lk, [&] { return stop || !incoming.empty(); });
     }
-    // fail what is left
+    // fail what is left, once nothing is on the device
     lk.unlock();
     cudaStreamSynchronize(ctx->stream);
     lk.lock();
     for (auto& kv : tickets)
-        if (!kv.second->done) {
+        if (!published[kv.first]) {
             kv.second->res.status = worker_error ? worker_error : CSIM_ERR_ARG;
             kv.second->done = true;
+            kv.second->inflight = 0;
+            published[kv.first] = true;
             failed++;
         }
-    for (auto& r : incoming) {
-        r->res.status = worker_error ? worker_error : CSIM_ERR_ARG;
-        r->done = true;
-        failed++;
-        tickets[r->ticket] = std::move(r);
-    }
     incoming.clear();
     cv_done.notify_all();
 }
@@ -1042,54 +1066,32 @@ extern "C" int csim_submit(csim_server* s, const csim_query* q, int64_t* ticket)
     if (s->stop) return s->worker_error ? s->worker_error : CSIM_ERR_ARG;
     r->ticket = s->next_ticket++;
     *ticket = r->ticket;
-    s->incoming.push_back(std::move(r));
+    s->incoming.push_back(r.get());
+    s->published[r->ticket] = false;
+    s->tickets[r->ticket] = std::move(r);
     s->submitted++;
     s->cv_work.notify_one();
     return CSIM_OK;
 }
 
-namespace {
-
-// caller holds s->mu
-int lookup(csim_server* s, int64_t ticket, QueryRec** out) {
-    auto it = s->tickets.find(ticket);
-    if (it != s->tickets.end()) {
-        *out = it->second.get();
-        return CSIM_OK;
-    }
-    for (auto& r : s->incoming)
-        if (r->ticket == ticket) {
-            *out = r.get();
-            return CSIM_OK;
-        }
-    return CSIM_ERR_ARG;
-}
-
-}  // namespace
-
 extern "C" int csim_poll(csim_server* s, int64_t ticket, csim_query_result* out) {
     if (!s || !out) return CSIM_ERR_ARG;
     std::lock_guard<std::mutex> lk(s->mu);
-    QueryRec* r = nullptr;
-    if (lookup(s, ticket, &r)) return CSIM_ERR_ARG;
-    if (!r->done) return CSIM_PENDING;
-    *out = r->res;
+    auto it = s->tickets.find(ticket);
+    if (it == s->tickets.end()) return CSIM_ERR_ARG;
+    if (!s->published[ticket]) return CSIM_PENDING;
+    *out = it->second->res;
     return CSIM_OK;
 }
 
 extern "C" int csim_wait(csim_server* s, int64_t ticket, double timeout_s, csim_query_result* out) {
     if (!s || !out) return CSIM_ERR_ARG;
     std::unique_lock<std::mutex> lk(s->mu);
-    QueryRec* r = nullptr;
-    if (lookup(s, ticket, &r)) return CSIM_ERR_ARG;
-    auto ready = [&] {
-        QueryRec* x = nullptr;
-        return lookup(s, ticket, &x) == CSIM_OK && x->done;
-    };
+    if (!s->tickets.count(ticket)) return CSIM_ERR_ARG;
+    auto ready = [&] { return s->published[ticket]; };
     if (timeout_s < 0) s->cv_done.wait(lk, ready);
     else if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), ready)) return CSIM_PENDING;
-    lookup(s, ticket, &r);
-    *out = r->res;
+    *out = s->tickets[ticket]->res;
     return CSIM_OK;
 }
 
@@ -1097,9 +1099,10 @@ extern "C" int csim_release(csim_server* s, int64_t ticket) {
     if (!s) return CSIM_ERR_ARG;
     std::lock_guard<std::mutex> lk(s->mu);
     auto it = s->tickets.find(ticket);
-    if (it == s->tickets.end() || !it->second->done) return CSIM_ERR_ARG;
+    if (it == s->tickets.end() || !s->published[ticket]) return CSIM_ERR_ARG;
     if (it->second->inflight > 0) return CSIM_PENDING;  // a failed query's states are still being read back
     s->tickets.erase(it);
+    s->published.erase(ticket);
     return CSIM_OK;
 }
 
