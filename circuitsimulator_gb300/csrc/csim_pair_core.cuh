@@ -96,6 +96,13 @@ CSIM_HD inline void gamma_ab(int A, int B, int& e, int& p, int& m, int& err) {
 // and only the low halves of the slots are read (the high halves are left
 // as they are and never read again).
 #define RJ(r) sJ[(size_t)((r) >> 1) * 2 * st + ((r) & 1)]
+
+// 64-bit row arithmetic while the warp's largest k exceeds this.  Builds of
+// the host checker set it to 0 to run the 64-bit code on every pair, as a
+// lane with k <= 32 does in a warp that still has a larger k.
+#ifndef CSIM_TP_WIDE_FROM
+#define CSIM_TP_WIDE_FROM 32
+#endif
 #define RG(c) sGT[(size_t)(c) * st]
 
 struct alignas(16) U64x2 {
@@ -255,8 +262,16 @@ CSIM_HD inline int tp_shrink(PairRegs& s, uint64_t* sJ, uint64_t* sGT, int st, i
     }
     if (beta) s.h ^= hflip;
 
-    // J: rank-two update, then the i <-> kk swap and drop of kk
-    const W Ji = upd ? (W)RJ(i) : (W)0;
+    // J: rank-two update, then the i <-> kk swap and drop of kk.  In 64-bit
+    // mode rows below 32 keep only their low halves current: bit y >= 32 of
+    // row x < 32 is bit x of row y (J is symmetric), which rows >= 32 carry in
+    // full, so row i's high half is gathered from them when i < 32.
+    W Ji = upd ? (W)RJ(i) : (W)0;
+    if (sizeof(W) == 8 && upd && i < 32) {
+        uint64_t hi = 0ull;
+        for (int y = 32; y < k; y++) hi |= (uint64_t)((RJ(y) >> i) & 1ull) << (y - 32);
+        Ji = (W)(((uint64_t)(uint32_t)Ji) | (hi << 32));
+    }
     const W C = Ji ^ (wget<W>(Ji, i) ? U : (W)0);  // new row (and column) i
     const W Jk = upd ? (W)((W)RJ(kk) ^ (wget<W>(C, kk) ? U : (W)0)) : (W)0;  // new row kk (kk not in U)
     // every row of the lane's block is rewritten (rows i and kk get values that are
@@ -266,11 +281,38 @@ CSIM_HD inline int tp_shrink(PairRegs& s, uint64_t* sJ, uint64_t* sGT, int st, i
     if (upd) {
         // two rows per 16-byte access (the pair buffer holds an even number of rows);
         // the coefficient masks walk bit-reversed copies from the top bit down
-        W cu = wbrev(U), cc = wbrev(C), cj = wbrev(Jk);
+        const W ru = wbrev(U), rc = wbrev(C), rj = wbrev(Jk);
+        int x0 = 0;
+        if (sizeof(W) == 8) {
+            // rows below 32: 32-bit arithmetic on the low halves; bit i moves only
+            // when i < 32 (a high bit of such a row is stale and never read)
+            const uint32_t Ji32 = (uint32_t)Ji, U32 = (uint32_t)U, mi32 = i < 32 ? (uint32_t)mi : 0u;
+            uint32_t cu = (uint32_t)((uint64_t)ru >> 32), cc = (uint32_t)((uint64_t)rc >> 32),
+                     cj = (uint32_t)((uint64_t)rj >> 32);
+            const int K32 = KX < 32 ? KX : 32;
 #if defined(__CUDA_ARCH__)
 #pragma unroll 2
 #endif
-        for (int x = 0; x < KX; x += 2) {
+            for (int x = 0; x < K32; x += 2) {
+                U64x2* pr = reinterpret_cast<U64x2*>(&RJ(x));
+                U64x2 v = *pr;
+                v.a = shrink_row<uint32_t>((uint32_t)v.a, Ji32, U32, mi32, topmask(cu), topmask(cc), topmask(cj));
+                cu <<= 1;
+                cc <<= 1;
+                cj <<= 1;
+                v.b = shrink_row<uint32_t>((uint32_t)v.b, Ji32, U32, mi32, topmask(cu), topmask(cc), topmask(cj));
+                cu <<= 1;
+                cc <<= 1;
+                cj <<= 1;
+                *pr = v;
+            }
+            x0 = 32;
+        }
+        W cu = ru << (x0 & (T::bits - 1)), cc = rc << (x0 & (T::bits - 1)), cj = rj << (x0 & (T::bits - 1));
+#if defined(__CUDA_ARCH__)
+#pragma unroll 2
+#endif
+        for (int x = x0; x < KX; x += 2) {
             U64x2* pr = reinterpret_cast<U64x2*>(&RJ(x));
             U64x2 v = *pr;
             v.a = (uint64_t)shrink_row<W>((W)v.a, Ji, U, mi, topmask(cu), topmask(cc), topmask(cj));
@@ -535,13 +577,24 @@ CSIM_HD inline void pair_l(bool valid, int n, int k1, int Q, uint64_t h, uint64_
     const int NZ = uniform_max(nz);
     for (int it = 0; it < NZ; it++) {
         const bool act = alive && it < nz;
-        const bool wide = uniform_max(alive ? s.k : 0) > 32;
+        const bool wide = uniform_max(alive ? s.k : 0) > CSIM_TP_WIDE_FROM;
         const int r = wide ? tp_shrink<uint64_t>(s, sJ, sGT, st, it, nz, act)
                            : tp_shrink<uint32_t>(s, sJ, sGT, st, it, nz, act);
         if (act && r == 0) alive = false;
     }
-    if (uniform_max(alive ? s.k : 0) > 32) tp_exp_sum<uint64_t>(s, sJ, st, alive, eps, p, m, err);
-    else tp_exp_sum<uint32_t>(s, sJ, st, alive, eps, p, m, err);
+    if (uniform_max(alive ? s.k : 0) > CSIM_TP_WIDE_FROM) {
+        // the 64-bit exponential sum reads whole rows: rebuild the high halves
+        // of rows below 32 from the rows >= 32 (J symmetric)
+        if (alive && s.k > 32)
+            for (int x = 0; x < 32; x++) {
+                uint64_t hi = 0ull;
+                for (int y = 32; y < s.k; y++) hi |= (uint64_t)((RJ(y) >> x) & 1ull) << (y - 32);
+                RJ(x) = (uint64_t)(uint32_t)RJ(x) | (hi << 32);
+            }
+        tp_exp_sum<uint64_t>(s, sJ, st, alive, eps, p, m, err);
+    } else {
+        tp_exp_sum<uint32_t>(s, sJ, st, alive, eps, p, m, err);
+    }
     if (alive) p -= k1 + hd_popc64(x);
     else {
         eps = 0;

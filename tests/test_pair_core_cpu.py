@@ -17,12 +17,16 @@ SO = os.path.join(HERE, "native", "_build", "libtphost.so")
 CORE = os.path.join(os.path.dirname(HERE), "circuitsimulator_gb300", "csrc", "csim_pair_core.cuh")
 
 
-@pytest.fixture(scope="module")
-def tp():
-    os.makedirs(os.path.dirname(SO), exist_ok=True)
-    if not os.path.exists(SO) or os.path.getmtime(SO) < max(os.path.getmtime(SRC), os.path.getmtime(CORE)):
-        subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", SRC, "-o", SO])
-    lib = C.CDLL(SO)
+@pytest.fixture(scope="module", params=["32", "0"], ids=["wide_above_32", "always_wide"])
+def tp(request):
+    """The host build of the pair routine; "always_wide" runs the 64-bit code
+    for every k, as a lane with a small k does in a warp that holds a larger one."""
+    so = SO.replace(".so", "_w%s.so" % request.param)
+    os.makedirs(os.path.dirname(so), exist_ok=True)
+    if not os.path.exists(so) or os.path.getmtime(so) < max(os.path.getmtime(SRC), os.path.getmtime(CORE)):
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-DCSIM_TP_WIDE_FROM=" + request.param,
+                               SRC, "-o", so])
+    lib = C.CDLL(so)
     lib.tp_host_pairs.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
     lib.tp_host_pairs.restype = C.c_int
 
