@@ -138,9 +138,7 @@ __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_
         const int n = sh.n;
         if (n > nmax || asym) e |= kErrArg;
         if (sh.live && !asym && n >= 1 && n <= nmax) {
-            const int nrow2 = (nmax + 1) & ~1;
-            uint64_t* sJ = reinterpret_cast<uint64_t*>(smem_raw + sizeof(ItemShared));
-            uint64_t* sGT = sJ + (size_t)nrow2 * kTPB;
+            const pc::PairMem mem = pc::pair_mem(smem_raw + sizeof(ItemShared), nmax, kTPB, tid);
             const int P = 2 * n;
             for (int r = 0; r < per_thread; r++) {
                 const int64_t j = it.j0 + tid + (int64_t)kTPB * r;
@@ -148,7 +146,7 @@ __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_
                 if (__all_sync(kFull, !valid)) break;
                 const uint64_t x = valid ? it.cw[j] : 0ull;
                 int eps, pp, mm;
-                pc::pair_l(valid, n, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ, sh.pGT, x, sJ + 2 * tid, sGT + tid, kTPB,
+                pc::pair_l(valid, n, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ, sh.pGT, x, mem,
                            eps, pp, mm, e, gmax);
                 if (!valid) continue;
                 pc::zacc(z, eps, pp, mm, P, e);
@@ -254,9 +252,7 @@ __global__ void k_codewords_multi(const CodeDesc* codes, int ncodes, uint64_t* o
 }
 
 // ------------------------------------------------------------ launchers
-size_t items_tp_smem(int nmax, int gmax) {
-    return sizeof(ItemShared) + (size_t)(((nmax + 1) & ~1) + gmax) * kTPB * sizeof(uint64_t);
-}
+size_t items_tp_smem(int nmax, int gmax) { return sizeof(ItemShared) + pc::pair_mem_bytes(nmax, gmax, kTPB); }
 
 int launch_draw_project(const Launch& L, const DrawDesc* desc, int64_t count, GState* out, int* code) {
     if (count <= 0) return 0;

@@ -1,11 +1,12 @@
 // csim_pair_core.cuh — one (theta, prepL term) pair, the body of the
-// thread-per-pair kernel (csim_terms_tp.cu), written once for the device and
-// the host: the same functions are compiled into a host-side checker
-// (tests/native/tp_host_check.cu) that the CPU tests compare with the oracle.
+// thread-per-pair kernels (csim_terms_tp.cu, csim_batch_kernels.cu), written
+// once for the device and the host: the same functions are compiled into a
+// host-side checker (tests/native/tp_host_check.cpp) that the CPU tests
+// compare with the oracle.
 //
-// The pair's J rows and G columns live in caller-provided memory with stride
-// `st` words between consecutive indices (the kernel's shared-memory
-// [index][thread] layout; 1 on the host).
+// The pair's J rows and G columns live in caller-provided memory (PairMem)
+// with stride `st` 16-byte units between consecutive indices (the kernels'
+// shared-memory [index][thread] layout; 1 on the host).
 #pragma once
 
 #include <cstdint>
@@ -89,13 +90,40 @@ CSIM_HD inline void gamma_ab(int A, int B, int& e, int& p, int& m, int& err) {
     else err |= kErrGamma;
 }
 
-// J rows are stored in pairs: rows 2p and 2p+1 are adjacent 64-bit slots, so
-// one 16-byte access moves both; pair p of a lane is 2*st slots after pair
-// p-1.  G columns are single slots st apart.  While every row-space index
-// of a pair is below 32 (k <= 32) the arithmetic runs on 32-bit words W
-// and only the low halves of the slots are read (the high halves are left
-// as they are and never read again).
-#define RJ(r) sJ[(size_t)((r) >> 1) * 2 * st + ((r) & 1)]
+// Per-pair working memory, laid out [index][thread] (consecutive indices of
+// one lane are `st` 16-byte units apart, so every access is conflict-free for
+// whole units):
+//   j32  rows 0..31 of J, low 32 bits, four rows per 16-byte unit;
+//   j64  rows 32.. of J, all 64 bits, two rows per 16-byte unit;
+//   g    the G columns of the codeword's zero positions, one 64-bit slot each.
+// Rows below 32 keep only their low halves: bit y >= 32 of such a row is bit
+// r of row y (J is symmetric), which the rows >= 32 carry in full; read_row
+// gathers it when a whole row is needed.  While k <= 32 (the narrow mode)
+// only j32 is used.
+struct PairMem {
+    uint32_t* j32;
+    uint64_t* j64;
+    uint64_t* g;
+    int st;
+};
+// Bytes of a block's working memory for `threads` lanes, and lane `lane`'s
+// view of it: j32 (32 rows), then j64 (rows 32..nmax-1, an even count), then
+// gmax G-column slots, each [index][thread].
+inline size_t pair_mem_bytes(int nmax, int gmax, int threads) {
+    const int n64 = nmax > 32 ? (((nmax + 1) & ~1) - 32) : 0;
+    return (size_t)threads * (32 * 4 + (size_t)n64 * 8 + (size_t)gmax * 8);
+}
+CSIM_HD inline PairMem pair_mem(unsigned char* base, int nmax, int threads, int lane) {
+    const int n64 = nmax > 32 ? (((nmax + 1) & ~1) - 32) : 0;
+    uint32_t* j32 = reinterpret_cast<uint32_t*>(base);
+    uint64_t* j64 = reinterpret_cast<uint64_t*>(base + (size_t)threads * 32 * 4);
+    uint64_t* g = j64 + (size_t)n64 * threads;
+    return PairMem{j32 + 4 * lane, j64 + 2 * lane, g + lane, threads};
+}
+
+#define R32(r) M.j32[(size_t)((r) >> 2) * 4 * M.st + ((r) & 3)]
+#define R64(r) M.j64[(size_t)(((r) - 32) >> 1) * 2 * M.st + (((r) - 32) & 1)]
+#define RG(c) M.g[(size_t)(c) * M.st]
 
 // 64-bit row arithmetic while the warp's largest k exceeds this.  Builds of
 // the host checker set it to 0 to run the 64-bit code on every pair, as a
@@ -103,10 +131,12 @@ CSIM_HD inline void gamma_ab(int A, int B, int& e, int& p, int& m, int& err) {
 #ifndef CSIM_TP_WIDE_FROM
 #define CSIM_TP_WIDE_FROM 32
 #endif
-#define RG(c) sGT[(size_t)(c) * st]
 
 struct alignas(16) U64x2 {
     uint64_t a, b;
+};
+struct alignas(16) U32x4 {
+    uint32_t a, b, c, d;
 };
 
 template <class W>
@@ -208,6 +238,28 @@ CSIM_HD inline void tp_add_D(PairRegs& s, uint64_t u, int d1, int d2) {
 
 CSIM_HD inline int tp_getD(const PairRegs& s, int i) { return 2 * (2 * getbit(s.D2, i) + getbit(s.D1, i)); }
 
+// bits 32..k-1 of row r < 32, i.e. bit r of rows 32..k-1
+CSIM_HD inline uint64_t gather_hi(const PairMem& M, int r, int k) {
+    uint64_t hi = 0ull;
+    for (int y = 32; y < k; y++) hi |= ((R64(y) >> r) & 1ull) << (y - 32);
+    return hi;
+}
+
+// whole row r of J (narrow mode: r < 32 and k <= 32)
+template <class W>
+CSIM_HD inline W read_row(const PairMem& M, int r, int k) {
+    if (sizeof(W) == 4) return (W)R32(r);
+    if (r >= 32) return (W)R64(r);
+    return (W)((uint64_t)R32(r) | (gather_hi(M, r, k) << 32));
+}
+
+// stores row r (a row below 32 keeps its low half)
+template <class W>
+CSIM_HD inline void write_row(const PairMem& M, int r, W v) {
+    if (r >= 32) R64(r) = (uint64_t)v;
+    else R32(r) = (uint32_t)v;
+}
+
 // one row of the shrink's rank-two update + bit move (see tp_shrink)
 template <class W>
 CSIM_HD inline W shrink_row(W r, W Ji, W U, W mi, W bu, W bc, W bj) {
@@ -232,7 +284,7 @@ CSIM_HD inline W shrink_row(W r, W Ji, W U, W mi, W bu, W bc, W bj) {
 // corrections of updateDJ are U & Ji, and updateQD's J.y is column kk of the
 // result, i.e. C with bit i taken from bit kk of C.
 template <class W>
-CSIM_HD inline int tp_shrink(PairRegs& s, uint64_t* sJ, uint64_t* sGT, int st, int q, int nz, bool act) {
+CSIM_HD inline int tp_shrink(PairRegs& s, const PairMem& M, int q, int nz, bool act) {
     using T = WordTraits<W>;
     const int k = s.k;
     const W km = wlow<W>(k);
@@ -262,71 +314,54 @@ CSIM_HD inline int tp_shrink(PairRegs& s, uint64_t* sJ, uint64_t* sGT, int st, i
     }
     if (beta) s.h ^= hflip;
 
-    // J: rank-two update, then the i <-> kk swap and drop of kk.  In 64-bit
-    // mode rows below 32 keep only their low halves current: bit y >= 32 of
-    // row x < 32 is bit x of row y (J is symmetric), which rows >= 32 carry in
-    // full, so row i's high half is gathered from them when i < 32.
-    W Ji = upd ? (W)RJ(i) : (W)0;
-    if (sizeof(W) == 8 && upd && i < 32) {
-        uint64_t hi = 0ull;
-        for (int y = 32; y < k; y++) hi |= (uint64_t)((RJ(y) >> i) & 1ull) << (y - 32);
-        Ji = (W)(((uint64_t)(uint32_t)Ji) | (hi << 32));
-    }
+    // J: rank-two update, then the i <-> kk swap and drop of kk
+    const W Ji = upd ? read_row<W>(M, i, k) : (W)0;
     const W C = Ji ^ (wget<W>(Ji, i) ? U : (W)0);  // new row (and column) i
-    const W Jk = upd ? (W)((W)RJ(kk) ^ (wget<W>(C, kk) ? U : (W)0)) : (W)0;  // new row kk (kk not in U)
+    const W Jk = upd ? (W)(read_row<W>(M, kk, k) ^ (wget<W>(C, kk) ? U : (W)0)) : (W)0;  // new row kk (kk not in U)
     // every row of the lane's block is rewritten (rows i and kk get values that are
     // replaced or dropped just below), so the pass is branch-free; rows at or
-    // beyond k are outside the block and never read again
+    // beyond k are outside the block and never read again.  The coefficient
+    // masks walk bit-reversed copies from the top bit down.
     const int KX = uniform_max(upd ? k : 0);
     if (upd) {
-        // two rows per 16-byte access (the pair buffer holds an even number of rows);
-        // the coefficient masks walk bit-reversed copies from the top bit down
         const W ru = wbrev(U), rc = wbrev(C), rj = wbrev(Jk);
-        int x0 = 0;
-        if (sizeof(W) == 8) {
-            // rows below 32: 32-bit arithmetic on the low halves; bit i moves only
-            // when i < 32 (a high bit of such a row is stale and never read)
+        // rows below 32, four per 16-byte unit, 32-bit; bit i moves only when
+        // i < 32 (a high bit of such a row is not stored)
+        {
             const uint32_t Ji32 = (uint32_t)Ji, U32 = (uint32_t)U, mi32 = i < 32 ? (uint32_t)mi : 0u;
-            uint32_t cu = (uint32_t)((uint64_t)ru >> 32), cc = (uint32_t)((uint64_t)rc >> 32),
-                     cj = (uint32_t)((uint64_t)rj >> 32);
+            const int sh = T::bits - 32;
+            uint32_t cu = (uint32_t)(ru >> sh), cc = (uint32_t)(rc >> sh), cj = (uint32_t)(rj >> sh);
             const int K32 = KX < 32 ? KX : 32;
-#if defined(__CUDA_ARCH__)
-#pragma unroll 2
-#endif
-            for (int x = 0; x < K32; x += 2) {
-                U64x2* pr = reinterpret_cast<U64x2*>(&RJ(x));
-                U64x2 v = *pr;
-                v.a = shrink_row<uint32_t>((uint32_t)v.a, Ji32, U32, mi32, topmask(cu), topmask(cc), topmask(cj));
-                cu <<= 1;
-                cc <<= 1;
-                cj <<= 1;
-                v.b = shrink_row<uint32_t>((uint32_t)v.b, Ji32, U32, mi32, topmask(cu), topmask(cc), topmask(cj));
-                cu <<= 1;
-                cc <<= 1;
-                cj <<= 1;
+            for (int x = 0; x < K32; x += 4) {
+                U32x4* pr = reinterpret_cast<U32x4*>(&R32(x));
+                U32x4 v = *pr;
+                v.a = shrink_row<uint32_t>(v.a, Ji32, U32, mi32, topmask(cu), topmask(cc), topmask(cj));
+                v.b = shrink_row<uint32_t>(v.b, Ji32, U32, mi32, topmask(cu << 1), topmask(cc << 1), topmask(cj << 1));
+                v.c = shrink_row<uint32_t>(v.c, Ji32, U32, mi32, topmask(cu << 2), topmask(cc << 2), topmask(cj << 2));
+                v.d = shrink_row<uint32_t>(v.d, Ji32, U32, mi32, topmask(cu << 3), topmask(cc << 3), topmask(cj << 3));
+                cu <<= 4;
+                cc <<= 4;
+                cj <<= 4;
                 *pr = v;
             }
-            x0 = 32;
         }
-        W cu = ru << (x0 & (T::bits - 1)), cc = rc << (x0 & (T::bits - 1)), cj = rj << (x0 & (T::bits - 1));
-#if defined(__CUDA_ARCH__)
-#pragma unroll 2
-#endif
-        for (int x = x0; x < KX; x += 2) {
-            U64x2* pr = reinterpret_cast<U64x2*>(&RJ(x));
-            U64x2 v = *pr;
-            v.a = (uint64_t)shrink_row<W>((W)v.a, Ji, U, mi, topmask(cu), topmask(cc), topmask(cj));
-            cu <<= 1;
-            cc <<= 1;
-            cj <<= 1;
-            v.b = (uint64_t)shrink_row<W>((W)v.b, Ji, U, mi, topmask(cu), topmask(cc), topmask(cj));
-            cu <<= 1;
-            cc <<= 1;
-            cj <<= 1;
-            *pr = v;
+        // rows 32.. (64-bit mode only), two per 16-byte unit
+        if (sizeof(W) == 8) {
+            W cu = (W)((uint64_t)ru << 32), cc = (W)((uint64_t)rc << 32), cj = (W)((uint64_t)rj << 32);
+            for (int x = 32; x < KX; x += 2) {
+                U64x2* pr = reinterpret_cast<U64x2*>(&R64(x));
+                U64x2 v = *pr;
+                v.a = (uint64_t)shrink_row<W>((W)v.a, Ji, U, mi, topmask(cu), topmask(cc), topmask(cj));
+                v.b = (uint64_t)shrink_row<W>((W)v.b, Ji, U, mi, topmask((W)(cu << 1)), topmask((W)(cc << 1)),
+                                              topmask((W)(cj << 1)));
+                cu <<= 2;
+                cc <<= 2;
+                cj <<= 2;
+                *pr = v;
+            }
         }
     }
-    if (upd && i != kk) RJ(i) = (uint64_t)((Jk & ~mi) | (mi & wmask<W>(wget<W>(Jk, kk))));
+    if (upd && i != kk) write_row<W>(M, i, (Jk & ~mi) | (mi & wmask<W>(wget<W>(Jk, kk))));
     if (upd) {
         // D: eq. 49 and the lower-triangle parities (J[max][min] = Ji by symmetry)
         tp_add_D(s, (uint64_t)U, getbit(s.D1, i), getbit(s.D2, i));
@@ -372,7 +407,7 @@ CSIM_HD inline void tp_factor_dimer(WAcc& w, int A, int B, int& err) {
 
 // exponentialSumExact (stabilizer.c:300-481), symmetric J; `act` as for tp_shrink.
 template <class W>
-CSIM_HD inline void tp_exp_sum(PairRegs& s, uint64_t* sJ, int st, bool act, int& eps, int& p, int& m, int& err) {
+CSIM_HD inline void tp_exp_sum(PairRegs& s, const PairMem& M, bool act, int& eps, int& p, int& m, int& err) {
     using T = WordTraits<W>;
     const int k = act ? s.k : 0;
     const W km = wlow<W>(k);
@@ -384,32 +419,54 @@ CSIM_HD inline void tp_exp_sum(PairRegs& s, uint64_t* sJ, int st, bool act, int&
         const int a = upd ? T::ffs(Sm) - 1 : 0;
         const W U = Sm & ~wbit<W>(a);
         const int kk = k - 1;
-        const W Ja = upd ? (W)RJ(a) : (W)0;
+        const W Ja = upd ? read_row<W>(M, a, k) : (W)0;
         const W C = Ja ^ (wget<W>(Ja, a) ? U : (W)0);  // new row/column a
-        const W Jk = upd ? (W)((W)RJ(kk) ^ (wget<W>(U, kk) ? Ja : (W)0) ^ (wget<W>(C, kk) ? U : (W)0)) : (W)0;
+        const W Jk =
+            upd ? (W)(read_row<W>(M, kk, k) ^ (wget<W>(U, kk) ? Ja : (W)0) ^ (wget<W>(C, kk) ? U : (W)0)) : (W)0;
         const int KX = uniform_max(upd ? k : 0);
         if (upd) {
-            // rows a and kk are rewritten below; the pass itself is branch-free
+            // every row: rank-two update, then bit a <- J'[x][kk] = bit x of Jk and
+            // bit kk <- J'[x][a] = bit x of C (rows a and kk are rewritten below)
             const W ma = wbit<W>(a), mk = wbit<W>(kk & (T::bits - 1));
-            W cu = wbrev(U), cc = wbrev(C), cj = wbrev(Jk);
-            for (int x = 0; x < KX; x++) {
-                W r = (W)RJ(x);
-                const W bc = topmask(cc);
-                r ^= Ja & topmask(cu);
-                r ^= U & bc;
-                // swap bits a and kk: bit a <- J'[x][kk] = bit x of Jk, bit kk <- J'[x][a] = bit x of C
-                r = (r & ~(ma | mk)) | (ma & topmask(cj)) | (mk & bc);
-                RJ(x) = (uint64_t)r;
-                cu <<= 1;
-                cc <<= 1;
-                cj <<= 1;
+            const W ru = wbrev(U), rc = wbrev(C), rj = wbrev(Jk);
+            {
+                const uint32_t Ja32 = (uint32_t)Ja, U32 = (uint32_t)U;
+                const uint32_t ma32 = a < 32 ? (uint32_t)ma : 0u, mk32 = kk < 32 ? (uint32_t)mk : 0u;
+                const int sh = T::bits - 32;
+                uint32_t cu = (uint32_t)(ru >> sh), cc = (uint32_t)(rc >> sh), cj = (uint32_t)(rj >> sh);
+                const int K32 = KX < 32 ? KX : 32;
+                for (int x = 0; x < K32; x++) {
+                    uint32_t r = R32(x);
+                    const uint32_t bc = topmask(cc);
+                    r ^= Ja32 & topmask(cu);
+                    r ^= U32 & bc;
+                    r = (r & ~(ma32 | mk32)) | (ma32 & topmask(cj)) | (mk32 & bc);
+                    R32(x) = r;
+                    cu <<= 1;
+                    cc <<= 1;
+                    cj <<= 1;
+                }
+            }
+            if (sizeof(W) == 8) {
+                W cu = (W)((uint64_t)ru << 32), cc = (W)((uint64_t)rc << 32), cj = (W)((uint64_t)rj << 32);
+                for (int x = 32; x < KX; x++) {
+                    W r = (W)R64(x);
+                    const W bc = topmask(cc);
+                    r ^= Ja & topmask(cu);
+                    r ^= U & bc;
+                    r = (r & ~(ma | mk)) | (ma & topmask(cj)) | (mk & bc);
+                    R64(x) = (uint64_t)r;
+                    cu <<= 1;
+                    cc <<= 1;
+                    cj <<= 1;
+                }
             }
         }
         if (upd && a != kk) {
-            RJ(a) = (uint64_t)(W)swapbits((uint64_t)Jk, a, kk);
-            RJ(kk) = (uint64_t)(W)swapbits((uint64_t)C, a, kk);
+            write_row<W>(M, a, (W)swapbits((uint64_t)Jk, a, kk));
+            write_row<W>(M, kk, (W)swapbits((uint64_t)C, a, kk));
         } else if (upd) {
-            RJ(a) = (uint64_t)C;
+            write_row<W>(M, a, C);
         }
         if (upd) {
             tp_add_D(s, (uint64_t)U, getbit(s.D1, a), getbit(s.D2, a));
@@ -420,17 +477,20 @@ CSIM_HD inline void tp_exp_sum(PairRegs& s, uint64_t* sJ, int st, bool act, int&
         }
     }
     W E = km & ~(sidx >= 0 ? wbit<W>(sidx) : (W)0);
+    // rows updated in each pass besides those still in play: in 64-bit mode
+    // the row sidx >= 32, whose bits give the bit sidx of rows below 32
+    const W keep = (sizeof(W) == 8 && sidx >= 32) ? wbit<W>(sidx) : (W)0;
     WAcc w0 = {0, 0, 0}, w1 = {0, 0, 0};
     const bool any = E != (W)0;
     const int NE = uniform_max(T::popc(E));
     for (int it = 0; it < NE; it++) {
         const bool live = E != (W)0;
         const int a = live ? T::ffs(E) - 1 : 0;
-        const W ra = live ? (W)RJ(a) : (W)0;
+        const W ra = live ? read_row<W>(M, a, k) : (W)0;
         const W K = ra & E & ~wbit<W>(a);
         const bool dimer = K != (W)0;
         const int b = dimer ? T::ffs(K) - 1 : 0;
-        const W rb = dimer ? (W)RJ(b) : (W)0;
+        const W rb = dimer ? read_row<W>(M, b, k) : (W)0;
         if (live && !dimer) {  // monomer {a}: row a is final
             const int Da = tp_getD(s, a);
             tp_factor_mono(w0, Da, err);
@@ -450,19 +510,19 @@ CSIM_HD inline void tp_exp_sum(PairRegs& s, uint64_t* sJ, int st, bool act, int&
         const int jaa = wget<W>(ra, a), jbb = wget<W>(rb, b), jab = wget<W>(ra, b);
         const W Cb = rb ^ (jbb ? vb : (W)0) ^ (jab ? va : (W)0);
         const W Ca = ra ^ (jab ? vb : (W)0) ^ (jaa ? va : (W)0);
-        const int np = upd ? T::popc(Ep) : 0;
+        W zz = upd ? (Ep | keep) : (W)0;
+        const int np = T::popc(zz);
         const int NP = uniform_max(np);
-        W zz = Ep;
         for (int t = 0; t < NP; t++) {
             if (t < np) {
                 const int x = T::ffs(zz) - 1;
                 zz &= zz - 1;
-                W r = (W)RJ(x);
-                r ^= rb & wmask<W>(wget<W>(vb, x));
-                r ^= ra & wmask<W>(wget<W>(va, x));
-                r ^= vb & wmask<W>(wget<W>(Cb, x));
-                r ^= va & wmask<W>(wget<W>(Ca, x));
-                RJ(x) = (uint64_t)r;
+                W d = rb & wmask<W>(wget<W>(vb, x));
+                d ^= ra & wmask<W>(wget<W>(va, x));
+                d ^= vb & wmask<W>(wget<W>(Cb, x));
+                d ^= va & wmask<W>(wget<W>(Ca, x));
+                if (x >= 32) R64(x) ^= (uint64_t)d;
+                else R32(x) ^= (uint32_t)d;
             }
         }
         if (upd) {
@@ -534,15 +594,15 @@ CSIM_HD inline void zacc(__int128 (&z)[4], int eps, int p, int m, int P, int& er
 }
 
 // One pair: theta's pristine J rows and G columns (as row masks), codeword x;
-// working memory sJ/sGT (stride st), n indices each (sJ an even number).
-// J must be symmetric.  `valid` = this lane has a pair (all lanes of a warp
-// call together).  The row arithmetic is 64-bit while the warp's largest k
-// exceeds 32 and 32-bit after that.
+// working memory M (see PairMem: 32 rows in j32, rows 32..n-1 in j64, gmax
+// G-column slots).  J must be symmetric.  `valid` = this lane has a pair (all
+// lanes of a warp call together).  The row arithmetic is 64-bit while the
+// warp's largest k exceeds 32 and 32-bit after that.
 CSIM_HD inline void pair_l(bool valid, int n, int k1, int Q, uint64_t h, uint64_t D1, uint64_t D2, const uint64_t* pJ,
-                           const uint64_t* pGT, uint64_t x, uint64_t* sJ, uint64_t* sGT, int st, int& eps, int& p,
-                           int& m, int& err, int gmax = 64) {
-    // sGT has gmax slots: a codeword with more zeros is refused (the caller
-    // bounds the zeros of the codewords it passes)
+                           const uint64_t* pGT, uint64_t x, const PairMem& M, int& eps, int& p, int& m, int& err,
+                           int gmax = 64) {
+    // the G-column slots hold gmax columns: a codeword with more zeros is
+    // refused (the caller bounds the zeros of the codewords it passes)
     if (valid && hd_popc64(~x & lowmask(n)) > gmax) {
         err |= kErrRange;
         valid = false;
@@ -553,13 +613,10 @@ CSIM_HD inline void pair_l(bool valid, int n, int k1, int Q, uint64_t h, uint64_
     s.h = h;
     s.D1 = D1;
     s.D2 = D2;
-    if (valid)
-        for (int r = 0; r < k1; r += 2) {
-            U64x2 v;
-            v.a = pJ[r];
-            v.b = pJ[r + 1];
-            *reinterpret_cast<U64x2*>(&RJ(r)) = v;
-        }
+    if (valid) {
+        for (int r = 0; r < k1 && r < 32; r++) R32(r) = (uint32_t)pJ[r];
+        for (int r = 32; r < k1; r++) R64(r) = pJ[r];
+    }
     // the zero columns of x, descending (the order of the shrinks), compact
     int nz = 0;
     uint64_t hz = 0ull;
@@ -578,23 +635,11 @@ CSIM_HD inline void pair_l(bool valid, int n, int k1, int Q, uint64_t h, uint64_
     for (int it = 0; it < NZ; it++) {
         const bool act = alive && it < nz;
         const bool wide = uniform_max(alive ? s.k : 0) > CSIM_TP_WIDE_FROM;
-        const int r = wide ? tp_shrink<uint64_t>(s, sJ, sGT, st, it, nz, act)
-                           : tp_shrink<uint32_t>(s, sJ, sGT, st, it, nz, act);
+        const int r = wide ? tp_shrink<uint64_t>(s, M, it, nz, act) : tp_shrink<uint32_t>(s, M, it, nz, act);
         if (act && r == 0) alive = false;
     }
-    if (uniform_max(alive ? s.k : 0) > CSIM_TP_WIDE_FROM) {
-        // the 64-bit exponential sum reads whole rows: rebuild the high halves
-        // of rows below 32 from the rows >= 32 (J symmetric)
-        if (alive && s.k > 32)
-            for (int x = 0; x < 32; x++) {
-                uint64_t hi = 0ull;
-                for (int y = 32; y < s.k; y++) hi |= (uint64_t)((RJ(y) >> x) & 1ull) << (y - 32);
-                RJ(x) = (uint64_t)(uint32_t)RJ(x) | (hi << 32);
-            }
-        tp_exp_sum<uint64_t>(s, sJ, st, alive, eps, p, m, err);
-    } else {
-        tp_exp_sum<uint32_t>(s, sJ, st, alive, eps, p, m, err);
-    }
+    if (uniform_max(alive ? s.k : 0) > CSIM_TP_WIDE_FROM) tp_exp_sum<uint64_t>(s, M, alive, eps, p, m, err);
+    else tp_exp_sum<uint32_t>(s, M, alive, eps, p, m, err);
     if (alive) p -= k1 + hd_popc64(x);
     else {
         eps = 0;
@@ -603,7 +648,8 @@ CSIM_HD inline void pair_l(bool valid, int n, int k1, int Q, uint64_t h, uint64_
     }
 }
 
-#undef RJ
+#undef R32
+#undef R64
 #undef RG
 
 }  // namespace pc

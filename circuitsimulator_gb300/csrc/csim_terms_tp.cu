@@ -7,11 +7,11 @@
 // Q = D = J = h = 0, so the R stage (stabilizer.c:611-652) changes nothing.
 //
 // Each thread keeps its pair's working state in shared memory with a
-// [index][thread] layout (one 64-bit word per thread per index, so every
-// access is conflict-free whatever the index):
-//   sJ[r]  row r of J                       (r < k)
-//   sGT[c] column c of G as a row mask       (only the zero columns of x,
-//          the only ones a later shrink or h-update of this pair reads)
+// [index][thread] layout (pc::PairMem):
+//   rows 0..31 of J, low 32 bits, four per 16-byte unit
+//   rows 32.. of J, 64 bits, two per 16-byte unit
+//   the G columns of x's zero positions as row masks, in shrink order (the
+//   only ones a later shrink or h-update of this pair reads)
 // and D1, D2, h, Q, k in registers.  Every basis change is the elementary
 // rank-one update of csim_warp.cuh applied row by row, with each row's
 // column bits gathered in the same pass; the exponential sum folds each
@@ -93,9 +93,7 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
         const int n = sh.n;
         if (n > nmax || asym) e |= kErrArg;
         if (sh.live && !asym && n >= 1 && n <= nmax) {
-            const int nrow2 = (nmax + 1) & ~1;  // J rows, an even count (pairs)
-            uint64_t* sJ = reinterpret_cast<uint64_t*>(smem_raw + sizeof(TPShared));
-            uint64_t* sGT = sJ + (size_t)nrow2 * kTP;
+            const pc::PairMem mem = pc::pair_mem(smem_raw + sizeof(TPShared), nmax, kTP, tid);
             const int64_t jb = j0 + cb * span;
             for (int r = 0; r < per_thread; r++) {
                 const int64_t j = jb + tid + (int64_t)kTP * r;
@@ -103,7 +101,7 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
                 if (__all_sync(kFull, !valid)) break;  // warp-uniform exit
                 const uint64_t x = valid ? codewords[j - j0] : 0ull;
                 int eps, pp, mm;
-                pc::pair_l(valid, n, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ, sh.pGT, x, sJ + 2 * tid, sGT + tid, kTP,
+                pc::pair_l(valid, n, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ, sh.pGT, x, mem,
                            eps, pp, mm, e, gmax);
                 if (!valid) continue;
                 pc::zacc(z, eps, pp, mm, P, e);
@@ -132,9 +130,7 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
     if (e && (tid & 31) == 0) atomicOr(err, e);
 }
 
-size_t terms_tp_smem(int nmax, int gmax) {
-    return sizeof(TPShared) + (size_t)(((nmax + 1) & ~1) + gmax) * kTP * sizeof(uint64_t);
-}
+size_t terms_tp_smem(int nmax, int gmax) { return sizeof(TPShared) + pc::pair_mem_bytes(nmax, gmax, kTP); }
 
 int launch_terms_tp(const Launch& L, int nmax, int gmax, const uint64_t* codewords, const GState* theta,
                     const int* code, int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P, __int128* part,

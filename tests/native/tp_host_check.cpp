@@ -10,8 +10,10 @@ extern "C" int tp_host_pairs(const csim_state* theta, int ntheta, const uint64_t
                              int* m) {
     int err = 0;
     uint64_t pGT[64];
-    alignas(16) uint64_t wJ[66];
-    uint64_t wG[64];
+    alignas(16) uint32_t wJ32[32];
+    alignas(16) uint64_t wJ64[34];
+    alignas(16) uint64_t wG[64];
+    const csim::pc::PairMem mem{wJ32, wJ64, wG, 1};
     for (int a = 0; a < ntheta; a++) {
         const csim_state& th = theta[a];
         for (int c = 0; c < 64; c++) {
@@ -22,7 +24,7 @@ extern "C" int tp_host_pairs(const csim_state* theta, int ntheta, const uint64_t
         }
         for (int j = 0; j < nx; j++) {
             const int w = a * nx + j;
-            csim::pc::pair_l(true, th.n, th.k, th.Q, th.h, th.D1, th.D2, th.J, pGT, xs[j], wJ, wG, 1, eps[w], p[w], m[w],
+            csim::pc::pair_l(true, th.n, th.k, th.Q, th.h, th.D1, th.D2, th.J, pGT, xs[j], mem, eps[w], p[w], m[w],
                              err);
         }
     }
