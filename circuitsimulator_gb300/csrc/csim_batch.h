@@ -36,13 +36,6 @@ struct PairItem {
     const GState* phis;
 };
 
-// codeword table of one code: x_j = bits(j) L for j < 2^k, written at out + offset
-struct CodeDesc {
-    const uint64_t* L;
-    int32_t k, pad;
-    int64_t offset;
-};
-
 int launch_draw_project(const Launch& L, const DrawDesc* desc, int64_t count, GState* out, int* code);
 // resident blocks per SM of k_items_tp launched for states of up to nmax qubits
 // and codewords of up to gmax zeros
@@ -55,6 +48,5 @@ int launch_items_warp(const Launch& L, const PairItem* items, int64_t nitems, co
 // if range2 is not null, [range2[2s], range2[2s+1])
 int launch_reduce_slots(const Launch& L, const __int128* part, const int64_t* range, const int64_t* range2,
                         int64_t nslots, __int128* out);
-int launch_codewords_multi(const Launch& L, const CodeDesc* codes, int ncodes, int64_t maxchi, uint64_t* out);
 
 }  // namespace csim

@@ -236,21 +236,6 @@ __global__ void k_reduce_slots(const __int128* part, const int64_t* range, const
     }
 }
 
-// codewords of several codes: descriptor c writes x_j = bits(j) L_c for j < 2^k_c at out + off_c
-__global__ void k_codewords_multi(const CodeDesc* codes, int ncodes, uint64_t* out) {
-    for (int c = 0; c < ncodes; c++) {
-        const CodeDesc d = codes[c];
-        const int64_t chi = (int64_t)1 << d.k;
-        for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < chi;
-             j += (int64_t)gridDim.x * blockDim.x) {
-            uint64_t x = 0ull;
-            for (int r = 0; r < d.k; r++)
-                if ((j >> (d.k - 1 - r)) & 1) x ^= d.L[r];
-            out[d.offset + j] = x;
-        }
-    }
-}
-
 // ------------------------------------------------------------ launchers
 size_t items_tp_smem(int nmax, int gmax) { return sizeof(ItemShared) + pc::pair_mem_bytes(nmax, gmax, kTPB); }
 
@@ -310,16 +295,6 @@ int launch_reduce_slots(const Launch& L, const __int128* part, const int64_t* ra
     int64_t blocks = (nslots * 4 + 255) / 256;
     if (blocks > (int64_t)L.num_sms * 16) blocks = (int64_t)L.num_sms * 16;
     k_reduce_slots<<<(int)blocks, 256, 0, L.stream>>>(part, range, range2, nslots, out);
-    (*L.launches)++;
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
-}
-
-int launch_codewords_multi(const Launch& L, const CodeDesc* codes, int ncodes, int64_t maxchi, uint64_t* out) {
-    if (ncodes <= 0) return 0;
-    int64_t blocks = (maxchi + 255) / 256;
-    if (blocks > (int64_t)L.num_sms * 16) blocks = (int64_t)L.num_sms * 16;
-    if (blocks < 1) blocks = 1;
-    k_codewords_multi<<<(int)blocks, 256, 0, L.stream>>>(codes, ncodes, out);
     (*L.launches)++;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
