@@ -489,52 +489,64 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
         void* v;
         CKR(dbuf(ctx, kBufA, c * sizeof(csim_state), &v));
         csim::GState* dth = (csim::GState*)v;
-        if (rng == CSIM_RNG_LIBC) {
-            words.clear();
-            offs.assign(1, 0);
-            for (int64_t i = 0; i < c; i++) {
-                draw_state_words(ctx->lr, t, hcum, words);
-                offs.push_back((int64_t)words.size());
-            }
-            uint32_t* dw;
-            int64_t* doff;
-            CKR(dput(ctx, kBufWords, words.data(), words.size(), &dw));
-            CKR(dput(ctx, kBufOffsets, offs.data(), offs.size(), &doff));
-            CK(cudaEventRecord(ctx->ev[0], ctx->stream));
-            if (csim::launch_random_states(launch_of(ctx), t, c, 1, 0, 0, dw, doff, dcum, dth, nullptr))
-                return fail(ctx, CSIM_ERR_CUDA, "random state launch failed");
-        } else {
-            CK(cudaEventRecord(ctx->ev[0], ctx->stream));
-            if (csim::launch_random_states(launch_of(ctx), t, c, 0, ctx->philox_seed, ctx->philox_next, nullptr,
-                                           nullptr, dcum, dth, nullptr))
-                return fail(ctx, CSIM_ERR_CUDA, "random state launch failed");
-            ctx->philox_next += c;
-        }
         CKR(dbuf(ctx, kBufCode, c * 4, &v));
         int* dcode = (int*)v;
-        if (csim::launch_project(launch_of(ctx), nr, dth, c, P->nstabs, dpm, dpz, dpx, dcode))
-            return fail(ctx, CSIM_ERR_CUDA, "projection launch failed");
         const size_t nparts = (size_t)c * nchunks * 4;
         CKR(dbuf(ctx, kBufParts, nparts * sizeof(__int128), &v));
         __int128* dpart = (__int128*)v;
+        CK(cudaEventRecord(ctx->ev[0], ctx->stream));
         CK(cudaMemsetAsync(dpart, 0, nparts * sizeof(__int128), ctx->stream));
-        CK(cudaEventRecord(ctx->ev[1], ctx->stream));
-        int rc = 0;
-        if (tp) {
-            // terms [0, jb): every zero count; terms [jb, chi): at most light_zeros(t) zeros
-            const int64_t span = 64 * (int64_t)ctx->per_thread;
-            const int64_t jb = std::min(chi, (ctx->cw_split + span - 1) / span * span);
-            if (jb > 0)
-                rc |= csim::launch_terms_tp(launch_of(ctx), t, t, dcw, dth, dcode, c, 0, jb, ctx->per_thread, P2,
-                                            dpart, nchunks, 0, nullptr, nullptr, nullptr);
-            if (jb < chi)
-                rc |= csim::launch_terms_tp(launch_of(ctx), t, light_zeros(t), dcw + jb, dth, dcode, c, jb, chi - jb,
-                                            ctx->per_thread, P2, dpart, nchunks, jb / span, nullptr, nullptr, nullptr);
-        } else {
-            rc = csim::launch_terms(launch_of(ctx), nr, exact ? 1 : 0, dcw, (const csim::GState*)dphis, dth, dcode, c,
-                                    0, chi, (int)chunk, P2, dpart, nullptr, nullptr, nullptr, nullptr);
+        // With the C library's draws the host makes every state's rand() words.
+        // The batch goes in sub-batches: the host draws sub-batch s+1 while the
+        // GPU works on sub-batch s, all launches queued on the stream.
+        const int64_t sub = rng == CSIM_RNG_LIBC ? std::min<int64_t>(c, 1024) : c;
+        bool first = true;
+        for (int64_t s0 = 0; s0 < c; s0 += sub) {
+            const int64_t cs = std::min(sub, c - s0);
+            csim::GState* sth = (csim::GState*)((csim_state*)dth + s0);
+            int* scode = dcode + s0;
+            if (rng == CSIM_RNG_LIBC) {
+                words.clear();
+                offs.assign(1, 0);
+                for (int64_t i = 0; i < cs; i++) {
+                    draw_state_words(ctx->lr, t, hcum, words);
+                    offs.push_back((int64_t)words.size());
+                }
+                uint32_t* dw;
+                int64_t* doff;
+                CKR(dput(ctx, kBufWords, words.data(), words.size(), &dw));
+                CKR(dput(ctx, kBufOffsets, offs.data(), offs.size(), &doff));
+                if (csim::launch_random_states(launch_of(ctx), t, cs, 1, 0, 0, dw, doff, dcum, sth, nullptr))
+                    return fail(ctx, CSIM_ERR_CUDA, "random state launch failed");
+            } else {
+                if (csim::launch_random_states(launch_of(ctx), t, cs, 0, ctx->philox_seed, ctx->philox_next, nullptr,
+                                               nullptr, dcum, sth, nullptr))
+                    return fail(ctx, CSIM_ERR_CUDA, "random state launch failed");
+                ctx->philox_next += cs;
+            }
+            if (csim::launch_project(launch_of(ctx), nr, sth, cs, P->nstabs, dpm, dpz, dpx, scode))
+                return fail(ctx, CSIM_ERR_CUDA, "projection launch failed");
+            if (first) CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+            first = false;
+            __int128* spart = dpart + (size_t)s0 * nchunks * 4;
+            int rc = 0;
+            if (tp) {
+                // terms [0, jb): every zero count; terms [jb, chi): at most light_zeros(t) zeros
+                const int64_t span = 64 * (int64_t)ctx->per_thread;
+                const int64_t jb = std::min(chi, (ctx->cw_split + span - 1) / span * span);
+                if (jb > 0)
+                    rc |= csim::launch_terms_tp(launch_of(ctx), t, t, dcw, sth, scode, cs, 0, jb, ctx->per_thread, P2,
+                                                spart, nchunks, 0, nullptr, nullptr, nullptr);
+                if (jb < chi)
+                    rc |= csim::launch_terms_tp(launch_of(ctx), t, light_zeros(t), dcw + jb, sth, scode, cs, jb,
+                                                chi - jb, ctx->per_thread, P2, spart, nchunks, jb / span, nullptr,
+                                                nullptr, nullptr);
+            } else {
+                rc = csim::launch_terms(launch_of(ctx), nr, exact ? 1 : 0, dcw, (const csim::GState*)dphis, sth,
+                                        scode, cs, 0, chi, (int)chunk, P2, spart, nullptr, nullptr, nullptr, nullptr);
+            }
+            if (rc) return fail(ctx, CSIM_ERR_CUDA, "term launch failed");
         }
-        if (rc) return fail(ctx, CSIM_ERR_CUDA, "term launch failed");
         CK(cudaEventRecord(ctx->ev[2], ctx->stream));
         CKR(dbuf(ctx, kBufAcc, (size_t)c * 4 * sizeof(__int128), &v));
         __int128* dacc = (__int128*)v;
