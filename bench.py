@@ -317,11 +317,12 @@ def c3_queries(light=True):
     return out, len(recs)
 
 
-def batch_compare(gpu, reps=3):
-    """Batched vs plain queries/s on the light c3 queries: the same queries, the
-    same draws, results checked identical.  Plain = one query after another
-    through the single-query entry points; batched = csim_run_queries."""
-    qs, total = c3_queries(light=True)
+def batch_compare(gpu, reps=3, light=True):
+    """Batched vs plain queries/s on the c3 queries (the light ones by default,
+    all 256 with light=False): the same queries, the same draws, results
+    checked identical.  Plain = one query after another through the
+    single-query entry points; batched = csim_run_queries."""
+    qs, total = c3_queries(light=light)
     gpu.run_queries(qs[:4], batched=True)
     gpu.run_queries(qs[:4], batched=False)
     tp, tb = [], []
@@ -339,8 +340,9 @@ def batch_compare(gpu, reps=3):
                             for a, b in zip(rp, rb))
         pairs = sum(b["pairs"] for b in rb)
     p, b = float(np.median(tp)), float(np.median(tb))
-    return {"workload": "c3 light: the %d of %d c3 queries with <= 2^26 inner products (t 8..23, relative "
-                        "error 0.05, Philox draws)" % (len(qs), total),
+    what = ("c3 light: the %d of %d c3 queries with <= 2^26 inner products (t 8..23" % (len(qs), total) if light
+            else "c3: all %d queries (t 8..60, chi 2^4..2^18" % total)
+    return {"workload": what + ", relative error 0.05, Philox draws)",
             "metric": "queries/s", "plain": len(qs) / p, "batched": len(qs) / b, "speedup": p / b,
             "identical_results": bool(same), "pairs": pairs, "reps": reps,
             "timing": "wall clock around the ABI call, host work included, median of reps"}
@@ -507,7 +509,14 @@ def main():
     ap.add_argument("--serve", default=None, metavar="RATES",
                     help="only time serving under Poisson arrivals at these rates (queries/s, comma separated)")
     ap.add_argument("--serve-count", type=int, default=300, help="queries per rate for --serve")
+    ap.add_argument("--c3-full", action="store_true",
+                    help="only time all 256 c3 queries, plain vs batched (about 10 minutes per arm)")
     args = ap.parse_args()
+    if args.c3_full:
+        from circuitsimulator_gb300 import backend
+
+        print(json.dumps(batch_compare(backend.Backend(0), reps=1, light=False)))
+        return
     if args.serve:
         rates = [float(r) for r in args.serve.split(",")]
         print(json.dumps([serve_compare(r, args.serve_count) for r in rates]))

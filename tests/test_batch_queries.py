@@ -218,3 +218,18 @@ def test_serving_daemon_equals_run_queries(be):
     for (st, num, den), r in zip(out, ref):
         assert st == 0
         assert (num, den) == (r["numerator"], r["denominator"])
+
+
+def test_server_wait_timeout_and_shutdown_with_work_queued():
+    """csim_wait returns PENDING on a timeout; destroying the server with work
+    still queued completes every ticket (as failed) and returns."""
+    qs = [q for q in mixed_queries(seed=41, count=24) if q["cfg"]["t"] >= 24][:4]
+    heavy = []
+    for q in qs:  # make them take a while: more samples
+        h = dict(q)
+        h["cfg"] = dict(q["cfg"], samples=4000, bins=1, noapprox=0, forceSample=1)
+        heavy.append(h)
+    srv = backend.Server(0, round_pairs=1 << 20)
+    tickets = [srv.submit(q) for q in heavy]
+    assert srv.wait(tickets[-1], timeout=0.0) is None
+    srv.close()  # shuts down with work pending: must not hang
