@@ -181,6 +181,8 @@ struct RoundSet {
 }  // namespace
 
 // ---------------------------------------------------------------- engine
+static bool plan_query(csim_ctx* ctx, QueryRec* r);
+
 class Engine {
   public:
     Engine(csim_ctx* ctx, int64_t round_pairs, int64_t round_states, int per_thread, int64_t budget)
@@ -233,7 +235,9 @@ class Engine {
     }
 
     // host plan of one query (decompose, noapprox rule); completes host-only and failed queries
-    void plan(QueryRec* r);
+    void plan(QueryRec* r) {
+        if (plan_query(ctx_, r)) finished.push_back(r);
+    }
     // makes the query's decomposition resident and creates its evaluations;
     // false when it does not fit the memory budget now
     int admit(QueryRec* r, bool force, bool* admitted);
@@ -277,36 +281,41 @@ class Engine {
     bool eval_ready(const Eval* e) const;
 };
 
-void Engine::plan(QueryRec* r) {
+static bool plan_fail(QueryRec* r, int status) {
+    r->res.status = status;
+    r->done = true;
+    return true;
+}
+
+// Host plan of one query: decompose (its fidelity sum on ctx's GPU), the noapprox
+// rule and the answers that need no device work (probability.c:146-174,
+// innerprod.c:47-62, :150).  Returns true when the query is complete already
+// (answered on the host, or failed); its result is in r->res.
+static bool plan_query(csim_ctx* ctx, QueryRec* r) {
     const csim_query& Q = r->q;
     csim_query_result& R = r->res;
     R = csim_query_result{};
     if (Q.t < 0 || Q.t > CSIM_MAX_QUBITS || (Q.rng != CSIM_RNG_LIBC && Q.rng != CSIM_RNG_PHILOX) ||
-        check_projector(ctx_, &Q.G) || check_projector(ctx_, &Q.H) || (Q.G.nstabs && Q.G.nqubits != Q.t) ||
+        check_projector(ctx, &Q.G) || check_projector(ctx, &Q.H) || (Q.G.nstabs && Q.G.nqubits != Q.t) ||
         (Q.H.nstabs && Q.H.nqubits != Q.t) || Q.G.nstabs > 64 || Q.H.nstabs > 64) {
-        fail_query(r, fail(ctx_, CSIM_ERR_ARG, "query %lld: bad t, rng or projectors", (long long)r->ticket));
-        return;
+        return plan_fail(r, fail(ctx, CSIM_ERR_ARG, "query %lld: bad t, rng or projectors", (long long)r->ticket));
     }
     // decompose() runs on rand()'s default stream, before the sampler is seeded (probability.c:146-153)
     LibcRand ds;
     ds.seed(1);
     r->exact = Q.exact;
     r->k = Q.k;
-    const int rc = csim_decompose_on(ctx_, Q.t, Q.fidbound, Q.rank, Q.fidelity, Q.force_l, Q.verbose, Q.quiet,
+    const int rc = csim_decompose_on(ctx, Q.t, Q.fidbound, Q.rank, Q.fidelity, Q.force_l, Q.verbose, Q.quiet,
                                      &r->exact, &r->k, &r->norm, r->L, &ds, nullptr);
-    if (rc != CSIM_OK) {
-        fail_query(r, rc);
-        return;
-    }
+    if (rc != CSIM_OK) return plan_fail(r, rc);
     r->noapprox = Q.noapprox;
     if (Q.noapprox == 0 && Q.force_sample == 0) {  // probability.c:162-174
         const double terms = r->exact ? pow(2, (Q.t + 1) / 2) : pow(2, r->k);
         if (Q.samples * Q.bins * 2 > (terms - 1)) r->noapprox = 1;
     }
     if (r->noapprox == 0 && (Q.bins < 1 || Q.samples < 0)) {
-        fail_query(r, fail(ctx_, CSIM_ERR_ARG, "query %lld: samples=%d bins=%d", (long long)r->ticket, Q.samples,
-                           Q.bins));
-        return;
+        return plan_fail(r, fail(ctx, CSIM_ERR_ARG, "query %lld: samples=%d bins=%d", (long long)r->ticket,
+                                  Q.samples, Q.bins));
     }
     R.exact = r->exact;
     R.k = r->k;
@@ -324,21 +333,16 @@ void Engine::plan(QueryRec* r) {
         }
     }
     if (!(r->host_only[0] && r->host_only[1])) {
-        if (check_code(ctx_, Q.t, r->exact, r->L, r->k)) {
-            fail_query(r, CSIM_ERR_ARG);
-            return;
-        }
-        if (r->noapprox && r->chi > ((int64_t)1 << 20)) {
-            fail_query(r, fail(ctx_, CSIM_ERR_ARG, "query %lld: chi too large for the exact projector",
-                               (long long)r->ticket));
-            return;
-        }
-    } else {
-        r->res.numerator = r->host_value[0];
-        r->res.denominator = r->host_value[1];
-        r->done = true;
-        finished.push_back(r);
+        if (check_code(ctx, Q.t, r->exact, r->L, r->k)) return plan_fail(r, CSIM_ERR_ARG);
+        if (r->noapprox && r->chi > ((int64_t)1 << 20))
+            return plan_fail(r, fail(ctx, CSIM_ERR_ARG, "query %lld: chi too large for the exact projector",
+                                     (long long)r->ticket));
+        return false;
     }
+    r->res.numerator = r->host_value[0];
+    r->res.denominator = r->host_value[1];
+    r->done = true;
+    return true;
 }
 
 int Engine::ensure_decomp(QueryRec* r, bool need_phis, bool force, Decomp** out) {
@@ -854,8 +858,7 @@ extern "C" int csim_run_queries(csim_ctx* ctx, int64_t nq, const csim_query* q, 
             QueryRec rec;
             rec.ticket = i;
             copy_query(q[i], &rec);
-            Engine plan_only(ctx, 0, 0, ctx->per_thread, 0);
-            plan_only.plan(&rec);
+            plan_query(ctx, &rec);
             r[i] = rec.res;
             if (rec.done) {
                 if (r[i].status && !first_err) first_err = r[i].status;
