@@ -1,11 +1,15 @@
-// csim_host.cpp — host side of libcsimgpu.so: the C ABI of include/csim.h.
+// csim_host.cpp — host side of libcsimgpu.so: the single-query C ABI of
+// include/csim.h.
 //
-// Contexts, device buffers, argument checks, the estimator drivers
-// (singleProjectorSample / sampledProjector / multiSampledProjector /
-// exactProjector of libcirc/innerprod.c), decompose (libcirc/probability.c:
-// 307-415) and the C library's rand() sequence.  All stabilizer algebra runs
-// in the kernels of csim_kernels.cu; the host only prepares inputs, converts
-// the kernels' exact Z[w] sums to doubles and does the per-query reductions.
+// Contexts, the batched primitives (innerProduct, exponentialSum, shrink,
+// measurePauli, extend, randomStabilizerState, prepH/prepL), the estimator
+// drivers (singleProjectorSample / sampledProjector / multiSampledProjector /
+// exactProjector of libcirc/innerprod.c) and decompose (libcirc/probability.c:
+// 307-415).  Shared helpers (the C library's rand() sequence, buffers, checks)
+// are in csim_host_common.h; many queries at once go through csim_engine.cpp.
+// All stabilizer algebra runs in the kernels; the host prepares inputs,
+// converts the kernels' exact Z[w] sums to doubles and does the per-query
+// reductions.
 #include "csim_host_common.h"
 
 using namespace csim_host;

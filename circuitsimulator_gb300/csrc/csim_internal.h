@@ -1,5 +1,6 @@
-// csim_internal.h — launch interface between the C ABI host code
-// (csim_host.cpp) and the kernels (csim_kernels.cu).  Not installed.
+// csim_internal.h — launch interface between the host code (csim_host.cpp,
+// csim_engine.cpp, csim_static.cu) and the kernels (csim_kernels.cu,
+// csim_terms_tp.cu).  Not installed.
 #pragma once
 
 #include <cuda_runtime.h>
