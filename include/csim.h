@@ -88,7 +88,10 @@ typedef struct csim_ctx csim_ctx;
 /* ------------------------------------------------------------- context */
 
 /* Opens a context on CUDA device `device`.  Fails with CSIM_ERR_NODEVICE if the
- * device is not an sm_103 part (the kernels are built for sm_103a only). */
+ * device is not an sm_103 part (the kernels are built for sm_103a only).  A
+ * context has its own stream, buffers and generators; use it from one thread
+ * at a time (threads that share a GPU open one context each, or share a
+ * csim_server, which is safe to call from any thread). */
 int csim_ctx_create(int device, csim_ctx **out);
 void csim_ctx_destroy(csim_ctx *ctx);
 /* Message of the last failing call on this context ("" if none). */
