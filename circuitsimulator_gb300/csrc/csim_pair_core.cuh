@@ -389,20 +389,47 @@ struct WAcc {
     int zero, p, m;
 };
 
+// gamma_ab for every A = 2a, B = 2b (a, b mod 4) as one 4-bit code per (a, b)
+// at bits 4(4a + b): bit 3 set = zero, else bits 0..2 = m (and p = 2).  Built
+// at compile time from the same sums as gamma_ab.
+constexpr uint64_t gamma_codes() {
+    uint64_t tab = 0;
+    for (int a = 0; a < 4; a++)
+        for (int b = 0; b < 4; b++) {
+            const int c = (a + b) % 4;
+            const int gr = 1 + ((a == 0) - (a == 2)) + ((b == 0) - (b == 2)) - ((c == 0) - (c == 2));
+            const int gi = ((a == 1) - (a == 3)) + ((b == 1) - (b == 3)) - ((c == 1) - (c == 3));
+            int code = 0;
+            if (gr == 0 && gi == 0) code = 8;
+            else if (gr == 0) code = gi > 0 ? 2 : 6;
+            else if (gr == -2) code = 4;
+            else if (gi == 2) code = 1;
+            else if (gi == 0) code = 0;
+            else code = 7;
+            tab |= (uint64_t)code << (4 * (4 * a + b));
+        }
+    return tab;
+}
+constexpr uint64_t kGammaCodes = gamma_codes();
+
+// one monomer factor partialGamma(A) = 1 + e^{i pi A/4}, A even: r = A mod 8 gives
+// 2^{2/2} w^0 (r = 0), 2^{1/2} w^1 (2), 0 (4), 2^{1/2} w^7 (6)
 CSIM_HD inline void tp_factor_mono(WAcc& w, int A, int& err) {
-    int e, p = 0, m = 0;
-    partial_gamma(A, e, p, m, err);
-    if (!e) w.zero = 1;
-    w.p += p;
-    w.m += m;
+    const int r = A & 7;
+    if (r & 1) err |= kErrGamma;
+    w.zero |= (r == 4);
+    w.p += r == 0 ? 2 : (r == 4 ? 0 : 1);
+    w.m += r == 2 ? 1 : (r == 6 ? 7 : 0);
 }
 
+// one dimer factor Gamma(A, B), A and B even and non-negative (kGammaCodes)
 CSIM_HD inline void tp_factor_dimer(WAcc& w, int A, int B, int& err) {
-    int e, p = 0, m = 0;
-    gamma_ab(A, B, e, p, m, err);
-    if (!e) w.zero = 1;
-    w.p += p;
-    w.m += m;
+    if (((A | B) & 1) || A < 0 || B < 0) err |= kErrGamma;
+    const int code = (int)((kGammaCodes >> (4 * (4 * ((A & 7) >> 1) + ((B & 7) >> 1)))) & 15);
+    const int z = code >> 3;
+    w.zero |= z;
+    w.p += z ? 0 : 2;
+    w.m += z ? 0 : (code & 7);
 }
 
 // exponentialSumExact (stabilizer.c:300-481), symmetric J; `act` as for tp_shrink.
