@@ -256,7 +256,7 @@ CSIM_HD inline W read_row(const PairMem& M, int r, int k) {
 // stores row r (a row below 32 keeps its low half)
 template <class W>
 CSIM_HD inline void write_row(const PairMem& M, int r, W v) {
-    if (r >= 32) R64(r) = (uint64_t)v;
+    if (sizeof(W) == 8 && r >= 32) R64(r) = (uint64_t)v;  // narrow mode: every row is below 32
     else R32(r) = (uint32_t)v;
 }
 
@@ -548,7 +548,7 @@ CSIM_HD inline void tp_exp_sum(PairRegs& s, const PairMem& M, bool act, int& eps
                 d ^= ra & wmask<W>(wget<W>(va, x));
                 d ^= vb & wmask<W>(wget<W>(Cb, x));
                 d ^= va & wmask<W>(wget<W>(Ca, x));
-                if (x >= 32) R64(x) ^= (uint64_t)d;
+                if (sizeof(W) == 8 && x >= 32) R64(x) ^= (uint64_t)d;
                 else R32(x) ^= (uint32_t)d;
             }
         }
