@@ -544,49 +544,59 @@ CSIM_HD inline void tp_exp_sum(PairRegs& s, const PairMem& M, bool act, int& eps
         const int jaa = wget<W>(ra, a), jbb = wget<W>(rb, b), jab = wget<W>(ra, b);
         const W Cb = rb ^ (jbb ? vb : (W)0) ^ (jab ? va : (W)0);
         const W Ca = ra ^ (jab ? vb : (W)0) ^ (jaa ? va : (W)0);
-        if (sizeof(W) == 4) {
-            // narrow mode: every row from the warp's lowest row in play up to its
-            // highest, four per 16-byte unit, coefficient masks by sign shift.
-            // A row outside Ep gets vb_x = va_x = 0, i.e. at most its own
-            // update of the columns in vb and va: such rows (finished rows, a,
-            // b, rows at or beyond k) are never read again.
-            const uint32_t zm = upd ? (uint32_t)Ep : 0u;
-            const int lo = zm ? T::ffs((W)zm) - 1 : 32, hi = zm ? 32 - T::clz((W)zm) : 0;
+        {
+            // every row from the warp's lowest row in play up to its highest: rows
+            // below 32 four per 16-byte unit in 32-bit, rows from 32 up two per unit
+            // in 64-bit; coefficient masks by sign shift.  A row outside Ep gets
+            // vb_x = va_x = 0, i.e. at most its own update of the columns in vb
+            // and va: such rows (finished rows, a, b, rows at or beyond k) are
+            // never read again, and the row sidx kept for 64-bit mode is updated
+            // as it should be.
+            const W zm = upd ? (Ep | keep) : (W)0;
+            const int lo = zm ? T::ffs(zm) - 1 : T::bits, hi = zm ? T::bits - T::clz(zm) : 0;
             const int X0 = uniform_min(lo) & ~3, X1 = uniform_max(hi);
-            const uint32_t rb32 = (uint32_t)rb, ra32 = (uint32_t)ra, vb32 = (uint32_t)vb, va32 = (uint32_t)va;
-            const int sh0 = X0 & 31;  // X0 = 32 only when no lane has a row to update (no iteration)
-            uint32_t cvb = wbrev(vb32) << sh0, cva = wbrev(va32) << sh0, ccb = wbrev((uint32_t)Cb) << sh0,
-                     cca = wbrev((uint32_t)Ca) << sh0;
-            for (int x = X0; x < X1; x += 4) {
-                U32x4* pr = reinterpret_cast<U32x4*>(&R32(x));
-                U32x4 v = *pr;
-                v.a ^= (rb32 & topmask(cvb)) ^ (ra32 & topmask(cva)) ^ (vb32 & topmask(ccb)) ^ (va32 & topmask(cca));
-                v.b ^= (rb32 & topmask(cvb << 1)) ^ (ra32 & topmask(cva << 1)) ^ (vb32 & topmask(ccb << 1)) ^
-                       (va32 & topmask(cca << 1));
-                v.c ^= (rb32 & topmask(cvb << 2)) ^ (ra32 & topmask(cva << 2)) ^ (vb32 & topmask(ccb << 2)) ^
-                       (va32 & topmask(cca << 2));
-                v.d ^= (rb32 & topmask(cvb << 3)) ^ (ra32 & topmask(cva << 3)) ^ (vb32 & topmask(ccb << 3)) ^
-                       (va32 & topmask(cca << 3));
-                cvb <<= 4;
-                cva <<= 4;
-                ccb <<= 4;
-                cca <<= 4;
-                *pr = v;
+            const W rvb = wbrev(vb), rva = wbrev(va), rcb = wbrev(Cb), rca = wbrev(Ca);
+            {
+                const int sh = T::bits - 32;
+                const int s0 = X0 < 32 ? X0 : 0;
+                const uint32_t rb32 = (uint32_t)rb, ra32 = (uint32_t)ra, vb32 = (uint32_t)vb, va32 = (uint32_t)va;
+                uint32_t cvb = (uint32_t)(rvb >> sh) << s0, cva = (uint32_t)(rva >> sh) << s0,
+                         ccb = (uint32_t)(rcb >> sh) << s0, cca = (uint32_t)(rca >> sh) << s0;
+                const int X1a = X1 < 32 ? X1 : 32;
+                for (int x = X0; x < X1a; x += 4) {
+                    U32x4* pr = reinterpret_cast<U32x4*>(&R32(x));
+                    U32x4 v = *pr;
+                    v.a ^= (rb32 & topmask(cvb)) ^ (ra32 & topmask(cva)) ^ (vb32 & topmask(ccb)) ^
+                           (va32 & topmask(cca));
+                    v.b ^= (rb32 & topmask(cvb << 1)) ^ (ra32 & topmask(cva << 1)) ^ (vb32 & topmask(ccb << 1)) ^
+                           (va32 & topmask(cca << 1));
+                    v.c ^= (rb32 & topmask(cvb << 2)) ^ (ra32 & topmask(cva << 2)) ^ (vb32 & topmask(ccb << 2)) ^
+                           (va32 & topmask(cca << 2));
+                    v.d ^= (rb32 & topmask(cvb << 3)) ^ (ra32 & topmask(cva << 3)) ^ (vb32 & topmask(ccb << 3)) ^
+                           (va32 & topmask(cca << 3));
+                    cvb <<= 4;
+                    cva <<= 4;
+                    ccb <<= 4;
+                    cca <<= 4;
+                    *pr = v;
+                }
             }
-        } else {
-            W zz = upd ? (Ep | keep) : (W)0;
-            const int np = T::popc(zz);
-            const int NP = uniform_max(np);
-            for (int t = 0; t < NP; t++) {
-                if (t < np) {
-                    const int x = T::ffs(zz) - 1;
-                    zz &= zz - 1;
-                    W d = rb & wmask<W>(wget<W>(vb, x));
-                    d ^= ra & wmask<W>(wget<W>(va, x));
-                    d ^= vb & wmask<W>(wget<W>(Cb, x));
-                    d ^= va & wmask<W>(wget<W>(Ca, x));
-                    if (sizeof(W) == 8 && x >= 32) R64(x) ^= (uint64_t)d;
-                    else R32(x) ^= (uint32_t)d;
+            if (sizeof(W) == 8) {
+                const int x0 = X0 > 32 ? (X0 & ~1) : 32;
+                const int s1 = x0 & (T::bits - 1);
+                W cvb = rvb << s1, cva = rva << s1, ccb = rcb << s1, cca = rca << s1;
+                for (int x = x0; x < X1; x += 2) {
+                    U64x2* pr = reinterpret_cast<U64x2*>(&R64(x));
+                    U64x2 v = *pr;
+                    v.a ^= (uint64_t)((rb & topmask(cvb)) ^ (ra & topmask(cva)) ^ (vb & topmask(ccb)) ^
+                                      (va & topmask(cca)));
+                    v.b ^= (uint64_t)((rb & topmask((W)(cvb << 1))) ^ (ra & topmask((W)(cva << 1))) ^
+                                      (vb & topmask((W)(ccb << 1))) ^ (va & topmask((W)(cca << 1))));
+                    cvb <<= 2;
+                    cva <<= 2;
+                    ccb <<= 2;
+                    cca <<= 2;
+                    *pr = v;
                 }
             }
         }
