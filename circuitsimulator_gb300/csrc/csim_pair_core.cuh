@@ -45,10 +45,6 @@ CSIM_HD inline int hd_clz64(uint64_t x) {
 CSIM_HD inline uint64_t bit1(int i) { return 1ull << i; }
 CSIM_HD inline uint64_t lowmask(int k) { return k >= 64 ? ~0ull : ((1ull << k) - 1ull); }
 CSIM_HD inline int getbit(uint64_t w, int i) { return (int)((w >> i) & 1ull); }
-CSIM_HD inline uint64_t swapbits(uint64_t w, int i, int j) {
-    const uint64_t t = ((w >> i) ^ (w >> j)) & 1ull;
-    return w ^ ((t << i) | (t << j));
-}
 
 enum : int { kErrRange = 1, kErrExpSum = 4, kErrGamma = 8 };
 
@@ -236,14 +232,24 @@ CSIM_HD inline int uniform_min(int v) {
 #endif
 }
 
-CSIM_HD inline void tp_add_D(PairRegs& s, uint64_t u, int d1, int d2) {
-    const uint64_t a1 = d1 ? u : 0ull, a2 = d2 ? u : 0ull;
-    const uint64_t carry = s.D1 & a1;
-    s.D1 ^= a1;
-    s.D2 ^= a2 ^ carry;
+// D = 2 (2 D2 + D1) per basis vector; adding u to D row-wise (eq. 49), with the carry
+// into D2, on D words of the mode's width (in 32-bit mode k <= 32, so D fits)
+template <class W>
+CSIM_HD inline void add_D(W& D1, W& D2, W u, int d1, int d2) {
+    const W a1 = d1 ? u : (W)0, a2 = d2 ? u : (W)0;
+    const W carry = D1 & a1;
+    D1 ^= a1;
+    D2 ^= a2 ^ carry;
 }
-
-CSIM_HD inline int tp_getD(const PairRegs& s, int i) { return 2 * (2 * getbit(s.D2, i) + getbit(s.D1, i)); }
+template <class W>
+CSIM_HD inline int get_D(W D1, W D2, int i) {
+    return 2 * (2 * wget<W>(D2, i) + wget<W>(D1, i));
+}
+template <class W>
+CSIM_HD inline W wswap(W w, int i, int j) {
+    const W t = ((w >> i) ^ (w >> j)) & (W)1;
+    return w ^ ((t << i) | (t << j));
+}
 
 // bits 32..k-1 of row r < 32, i.e. bit r of rows 32..k-1
 CSIM_HD inline uint64_t gather_hi(const PairMem& M, int r, int k) {
@@ -371,20 +377,23 @@ CSIM_HD inline int tp_shrink(PairRegs& s, const PairMem& M, int q, int nz, bool 
     if (upd && i != kk) write_row<W>(M, i, (Jk & ~mi) | (mi & wmask<W>(wget<W>(Jk, kk))));
     if (upd) {
         // D: eq. 49 and the lower-triangle parities (J[max][min] = Ji by symmetry)
-        tp_add_D(s, (uint64_t)U, getbit(s.D1, i), getbit(s.D2, i));
-        s.D2 ^= (uint64_t)(U & Ji);
+        W D1 = (W)s.D1, D2 = (W)s.D2;
+        add_D<W>(D1, D2, U, wget<W>(D1, i), wget<W>(D2, i));
+        D2 ^= U & Ji;
         if (i != kk) {
-            s.D1 = swapbits(s.D1, i, kk);
-            s.D2 = swapbits(s.D2, i, kk);
+            D1 = wswap<W>(D1, i, kk);
+            D2 = wswap<W>(D2, i, kk);
         }
-        s.D1 &= lowmask(k);
-        s.D2 &= lowmask(k);
+        D1 &= km;
+        D2 &= km;
         if (beta) {
-            s.Q = (s.Q + tp_getD(s, kk)) % 8;
-            s.D2 ^= (uint64_t)(((C & ~mi) | (mi & wmask<W>(wget<W>(C, kk)))) & wlow<W>(kk));
+            s.Q = (s.Q + get_D<W>(D1, D2, kk)) % 8;
+            D2 ^= ((C & ~mi) | (mi & wmask<W>(wget<W>(C, kk)))) & wlow<W>(kk);
         } else {
             s.Q = s.Q % 8;
         }
+        s.D1 = (uint64_t)D1;
+        s.D2 = (uint64_t)D2;
         s.k = kk;
         return 2;
     }
@@ -445,7 +454,8 @@ CSIM_HD inline void tp_exp_sum(PairRegs& s, const PairMem& M, bool act, int& eps
     using T = WordTraits<W>;
     const int k = act ? s.k : 0;
     const W km = wlow<W>(k);
-    const W Sm = (W)s.D1 & km;
+    W D1 = (W)s.D1, D2 = (W)s.D2;
+    const W Sm = D1 & km;
     int sidx = -1;
     {
         // R = I + U e_a^T, then swap a <-> kk (stabilizer.c:317-336); kk may lie in U
@@ -497,16 +507,16 @@ CSIM_HD inline void tp_exp_sum(PairRegs& s, const PairMem& M, bool act, int& eps
             }
         }
         if (upd && a != kk) {
-            write_row<W>(M, a, (W)swapbits((uint64_t)Jk, a, kk));
-            write_row<W>(M, kk, (W)swapbits((uint64_t)C, a, kk));
+            write_row<W>(M, a, wswap<W>(Jk, a, kk));
+            write_row<W>(M, kk, wswap<W>(C, a, kk));
         } else if (upd) {
             write_row<W>(M, a, C);
         }
         if (upd) {
-            tp_add_D(s, (uint64_t)U, getbit(s.D1, a), getbit(s.D2, a));
-            s.D2 ^= (uint64_t)(U & Ja);
-            s.D1 = swapbits(s.D1, a, kk) & lowmask(k);
-            s.D2 = swapbits(s.D2, a, kk) & lowmask(k);
+            add_D<W>(D1, D2, U, wget<W>(D1, a), wget<W>(D2, a));
+            D2 ^= U & Ja;
+            D1 = wswap<W>(D1, a, kk) & km;
+            D2 = wswap<W>(D2, a, kk) & km;
             sidx = kk;
         }
     }
@@ -526,12 +536,12 @@ CSIM_HD inline void tp_exp_sum(PairRegs& s, const PairMem& M, bool act, int& eps
         const int b = dimer ? T::ffs(K) - 1 : 0;
         const W rb = dimer ? read_row<W>(M, b, k) : (W)0;
         if (live && !dimer) {  // monomer {a}: row a is final
-            const int Da = tp_getD(s, a);
+            const int Da = get_D<W>(D1, D2, a);
             tp_factor_mono(w0, Da, err);
             if (sidx >= 0) tp_factor_mono(w1, Da + 4 * wget<W>(ra, sidx), err);
         }
         if (dimer) {  // dimer {a, b}: rows a and b are final
-            const int Da = tp_getD(s, a), Db = tp_getD(s, b);
+            const int Da = get_D<W>(D1, D2, a), Db = get_D<W>(D1, D2, b);
             tp_factor_dimer(w0, Da, Db, err);
             if (sidx >= 0) tp_factor_dimer(w1, Da + 4 * wget<W>(ra, sidx), Db + 4 * wget<W>(rb, sidx), err);
         }
@@ -601,12 +611,12 @@ CSIM_HD inline void tp_exp_sum(PairRegs& s, const PairMem& M, bool act, int& eps
             }
         }
         if (upd) {
-            const int db1 = getbit(s.D1, b), db2 = getbit(s.D2, b), da1 = getbit(s.D1, a), da2 = getbit(s.D2, a);
-            tp_add_D(s, (uint64_t)vb, db1, db2);
-            tp_add_D(s, (uint64_t)va, da1, da2);
+            const int db1 = wget<W>(D1, b), db2 = wget<W>(D2, b), da1 = wget<W>(D1, a), da2 = wget<W>(D2, a);
+            add_D<W>(D1, D2, vb, db1, db2);
+            add_D<W>(D1, D2, va, da1, da2);
             W flip = (vb & rb) ^ (va & ra);
             if (jab) flip ^= vb & va;
-            s.D2 ^= (uint64_t)flip;
+            D2 ^= flip;
         }
         if (live) E = Ep;
     }
@@ -616,7 +626,7 @@ CSIM_HD inline void tp_exp_sum(PairRegs& s, const PairMem& M, bool act, int& eps
         return;
     }
     // W0 = Wsigma(sigma = 0), W1 = Wsigma(sigma = 1) (stabilizer.c:425-479)
-    const int tM0 = s.Q, tM1 = s.Q + (sidx >= 0 ? tp_getD(s, sidx) : 0);
+    const int tM0 = s.Q, tM1 = s.Q + (sidx >= 0 ? get_D<W>(D1, D2, sidx) : 0);
     const int e0 = !w0.zero, p0 = w0.zero ? 0 : w0.p, m0 = w0.zero ? 0 : (any ? (tM0 + w0.m) % 8 : tM0);
     if (sidx < 0) {
         eps = e0; p = p0; m = m0;
