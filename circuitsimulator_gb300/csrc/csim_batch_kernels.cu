@@ -84,10 +84,12 @@ __global__ void __launch_bounds__(256) k_draw_project(const DrawDesc* desc, int6
 constexpr int kTPB = 64;
 
 struct ItemShared {
+    // the item's state, then the state its pairs start from (prefix_shrink)
     uint64_t pJ[64];
     uint64_t pGT[64];
     uint64_t h, D1, D2;
-    int n, k, Q, live;
+    unsigned long long dis;  // bits in which the item's codewords differ
+    int n, k, Q, live, dead;
     __int128 red[kTPB / 32][8];
 };
 
@@ -119,6 +121,8 @@ __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_
             sh.h = g->h;
             sh.D1 = g->D1;
             sh.D2 = g->D2;
+            sh.dis = 0ull;
+            sh.dead = 0;
         }
         {
             sh.pJ[tid] = g->J[tid];
@@ -129,6 +133,18 @@ __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_
             sh.pGT[tid] = col;
         }
         __syncthreads();
+        const uint64_t x0 = it.nj > 0 ? it.cw[it.j0] : 0ull;
+        {  // the bits in which the item's codewords differ
+            uint64_t dis = 0ull;
+            for (int r = 0; r < per_thread; r++) {
+                const int64_t j = it.j0 + tid + (int64_t)kTPB * r;
+                if (j < it.j0 + it.nj) dis |= it.cw[j] ^ x0;
+            }
+            dis = ((uint64_t)__reduce_or_sync(kFull, (unsigned)(dis >> 32)) << 32) |
+                  __reduce_or_sync(kFull, (unsigned)dis);
+            if ((tid & 31) == 0 && dis) atomicOr(&sh.dis, (unsigned long long)dis);
+        }
+        const int k0 = sh.k;  // the state's own (prefix_shrink replaces sh.k after the next barrier)
         bool asym = false;
         if (tid < sh.k)
             for (int r = 0; r < sh.k; r++) asym |= ((sh.pJ[tid] >> r) & 1ull) != ((sh.pJ[r] >> tid) & 1ull);
@@ -138,6 +154,19 @@ __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_
         const int n = sh.n;
         if (n > nmax || asym) e |= kErrArg;
         if (sh.live && !asym && n >= 1 && n <= nmax) {
+            // the shrinks all of the item's pairs share (the zeros of the
+            // codewords' common top bits) run once, on one lane
+            const uint64_t pm = pc::agree_top(sh.dis, n);
+            if (it.nj > 0 && pc::hd_popc64(~x0 & pm & pc::lowmask(n)) > 0) {
+                if (tid < 32) {
+                    const pc::PairMem pmem = pc::pair_mem(smem_raw + sizeof(ItemShared), nmax, 1, 0);
+                    const int ok = pc::prefix_shrink(tid == 0, n, pm, x0, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ,
+                                                     sh.pGT, pmem);
+                    if (tid == 0) sh.dead = !ok;
+                }
+                __syncthreads();
+            }
+            const bool dead = sh.dead != 0;
             const pc::PairMem mem = pc::pair_mem(smem_raw + sizeof(ItemShared), nmax, kTPB, tid);
             const int P = 2 * n;
             for (int r = 0; r < per_thread; r++) {
@@ -145,9 +174,10 @@ __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_
                 const bool valid = j < it.j0 + it.nj;
                 if (__all_sync(kFull, !valid)) break;
                 const uint64_t x = valid ? it.cw[j] : 0ull;
-                int eps, pp, mm;
-                pc::pair_l(valid, n, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ, sh.pGT, x, mem,
-                           eps, pp, mm, e, gmax);
+                int eps = 0, pp = 0, mm = 0;
+                if (!dead)
+                    pc::pair_l(valid, n, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ, sh.pGT, x, mem, eps, pp, mm, e, gmax,
+                               pm, k0);
                 if (!valid) continue;
                 pc::zacc(z, eps, pp, mm, P, e);
                 if (j == it.diag) {

@@ -391,7 +391,7 @@ int Engine::ensure_decomp(QueryRec* r, bool need_phis, bool force, Decomp** out)
             }
             d->bytes += 2 * align_up((size_t)chi * 8) + kAlign;
             std::vector<uint64_t> ordered;
-            ordered_codewords(d->L.data(), d->k, ordered);
+            ordered_codewords(d->L.data(), d->k, d->t, ordered);
             d->light = light_split(ordered, d->t);
             CK(cudaMemcpy(d->cws, ordered.data(), (size_t)chi * 8, cudaMemcpyHostToDevice));
             uint64_t rows[CSIM_MAX_QUBITS] = {0};

@@ -362,7 +362,7 @@ int stage_terms(csim_ctx* ctx, int t, int exact, const uint64_t* L, int k, int64
         key.push_back((uint64_t)t);
         if (key != ctx->cw_key || !ctx->buf[kBufCwOrdered]) {
             std::vector<uint64_t> cw;
-            ordered_codewords(L, k, cw);
+            ordered_codewords(L, k, t, cw);
             uint64_t* d;
             CKR(dput(ctx, kBufCwOrdered, cw.data(), cw.size(), &d));
             ctx->cw_key = key;

@@ -142,12 +142,26 @@ inline void draw_state_words(LibcRand& lr, int n, const double* cum, std::vector
     for (int64_t i = 0; i < rest; i++) words.push_back((uint32_t)lr.next());
 }
 
+// Zero bound of the "light" part of an ordered codeword table: codewords with
+// at most this many zeros run in a launch whose G-column slots are sized for
+// it, which leaves shared memory for more resident blocks.  Weights of a
+// random code's codewords cluster at t/2, so most terms fall in this part.
+inline int light_zeros(int t) { return std::min(t, (3 * t + 4) / 5); }
+
+// Codeword-order parameter: the top-bit groups of ordered_codewords hold
+// about two kernel blocks (2^10 terms each at the default 16 terms per thread)
+inline int ordered_prefix_bits(int k, int t) { return std::max(0, std::min(t, k - 11)); }
+
 // The 2^k codewords of L in the order the thread-per-pair kernel walks them in
-// a sampled estimator: by weight, then by value (high positions first).  The
-// 32 pairs of a warp then have the same number of shrinks, and mostly the
-// same leading zero pattern, so the warp's predicated loops waste few lanes.
-// A state's sum over all terms is exact, so it does not depend on the order.
-inline void ordered_codewords(const uint64_t* L, int k, std::vector<uint64_t>& out) {
+// a sampled estimator.  First those with more than light_zeros(t) zeros (the
+// heavy launch), then the rest (light_split finds the boundary); within each
+// part by the top d = ordered_prefix_bits(k, t) bits, then by weight, then by
+// value.  A block's consecutive codewords then agree on long top bits, whose
+// shrinks the block runs once for all of its pairs (prefix_shrink), and the 32
+// pairs of a warp mostly have the same number of shrinks, so the warp's
+// predicated loops waste few lanes.  A state's sum over all terms is exact,
+// so it does not depend on the order.
+inline void ordered_codewords(const uint64_t* L, int k, int t, std::vector<uint64_t>& out) {
     const int64_t chi = (int64_t)1 << k;
     out.resize((size_t)chi);
     uint64_t x = 0;
@@ -156,19 +170,19 @@ inline void ordered_codewords(const uint64_t* L, int k, std::vector<uint64_t>& o
         x ^= L[k - 1 - __builtin_ctzll((unsigned long long)i)];
         out[(size_t)i] = x;
     }
-    std::sort(out.begin(), out.end(), [](uint64_t a, uint64_t b) {
+    const int wmin = t - light_zeros(t);
+    const int d = ordered_prefix_bits(k, t);
+    std::sort(out.begin(), out.end(), [wmin, d, t](uint64_t a, uint64_t b) {
         const int pa = __builtin_popcountll(a), pb = __builtin_popcountll(b);
+        const bool ha = pa < wmin, hb = pb < wmin;
+        if (ha != hb) return ha;
+        const uint64_t ta = d ? a >> (t - d) : 0, tb = d ? b >> (t - d) : 0;
+        if (ta != tb) return ta < tb;
         return pa != pb ? pa < pb : a < b;
     });
 }
 
-// Zero bound of the "light" part of an ordered codeword table: codewords with
-// at most this many zeros run in a launch whose G-column slots are sized for
-// it, which leaves shared memory for more resident blocks.  Weights of a
-// random code's codewords cluster at t/2, so most terms fall in this part.
-inline int light_zeros(int t) { return std::min(t, (3 * t + 4) / 5); }
-
-// First index of an ordered table (ascending weight) from which every codeword
+// First index of an ordered table (heavy part first) from which every codeword
 // has at most light_zeros(t) zeros.
 inline int64_t light_split(const std::vector<uint64_t>& cw, int t) {
     const int wmin = t - light_zeros(t);

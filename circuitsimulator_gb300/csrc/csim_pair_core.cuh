@@ -678,17 +678,22 @@ CSIM_HD inline void zacc(__int128 (&z)[4], int eps, int p, int m, int P, int& er
     }
 }
 
-// One pair: theta's pristine J rows and G columns (as row masks), codeword x;
-// working memory M (see PairMem: 32 rows in j32, rows 32..n-1 in j64, gmax
-// G-column slots).  J must be symmetric.  `valid` = this lane has a pair (all
-// lanes of a warp call together).  The row arithmetic is 64-bit while the
-// warp's largest k exceeds 32 and 32-bit after that.
+// One pair: theta's J rows and G columns (as row masks), codeword x; working
+// memory M (see PairMem: 32 rows in j32, rows 32..n-1 in j64, gmax G-column
+// slots).  J must be symmetric.  `valid` = this lane has a pair (all lanes of
+// a warp call together).  The row arithmetic is 64-bit while the warp's
+// largest k exceeds 32 and 32-bit after that.
+//
+// `done`: top bits of [0, n) whose shrinks the state passed in has already
+// been through (prefix_shrink); the state's k is then k1 and theta's own is
+// k0.  Without them (done = 0, k0 < 0) the state is theta's.
 CSIM_HD inline void pair_l(bool valid, int n, int k1, int Q, uint64_t h, uint64_t D1, uint64_t D2, const uint64_t* pJ,
                            const uint64_t* pGT, uint64_t x, const PairMem& M, int& eps, int& p, int& m, int& err,
-                           int gmax = 64) {
+                           int gmax = 64, uint64_t done = 0ull, int k0 = -1) {
+    const uint64_t zeros_all = ~x & lowmask(n) & ~done;
     // the G-column slots hold gmax columns: a codeword with more zeros is
     // refused (the caller bounds the zeros of the codewords it passes)
-    if (valid && hd_popc64(~x & lowmask(n)) > gmax) {
+    if (valid && hd_popc64(zeros_all) > gmax) {
         err |= kErrRange;
         valid = false;
     }
@@ -705,7 +710,7 @@ CSIM_HD inline void pair_l(bool valid, int n, int k1, int Q, uint64_t h, uint64_
     // the zero columns of x, descending (the order of the shrinks), compact
     int nz = 0;
     uint64_t hz = 0ull;
-    for (uint64_t zz = valid ? (~x & lowmask(n)) : 0ull; zz; nz++) {
+    for (uint64_t zz = valid ? zeros_all : 0ull; zz; nz++) {
         const int c = 63 - hd_clz64(zz);
         zz &= ~bit1(c);
         RG(nz) = pGT[c];
@@ -725,12 +730,86 @@ CSIM_HD inline void pair_l(bool valid, int n, int k1, int Q, uint64_t h, uint64_
     }
     if (uniform_max(alive ? s.k : 0) > CSIM_TP_WIDE_FROM) tp_exp_sum<uint64_t>(s, M, alive, eps, p, m, err);
     else tp_exp_sum<uint32_t>(s, M, alive, eps, p, m, err);
-    if (alive) p -= k1 + hd_popc64(x);
+    if (alive) p -= (k0 < 0 ? k1 : k0) + hd_popc64(x);
     else {
         eps = 0;
         p = 0;
         m = 0;
     }
+}
+
+// The shrinks that every pair of theta with a codeword that agrees with x0 on
+// the top bits `pm` of [0, n) starts with: those by the zero bits of x0 in
+// pm, in descending order, as pair_l runs them.  In: theta's J rows pJ, G
+// columns pGT (row masks), h, D1, D2, Q, k.  Out, in place: the state after
+// those shrinks, with the G columns and h bits of the positions below pm (J
+// rows and G columns masked to the new k).  Returns 0 if a shrink found the
+// projection empty (every such pair is then 0), else 1.  Every lane of one
+// warp calls it; the `act` lane (one per warp) does the work in its working
+// memory M, which has room for 64 G columns, and is the only one that writes.
+CSIM_HD inline int prefix_shrink(bool act, int n, uint64_t pm, uint64_t x0, int& k, int& Q, uint64_t& h,
+                                 uint64_t& D1, uint64_t& D2, uint64_t* pJ, uint64_t* pGT, const PairMem& M) {
+    const uint64_t pz = act ? (~x0 & pm & lowmask(n)) : 0ull;
+    const int npz = hd_popc64(pz);
+    const int nlow = hd_popc64(lowmask(n) & ~pm);  // pm is a top mask: positions 0..nlow-1 stay
+    PairRegs s;
+    s.k = k;
+    s.Q = Q;
+    s.D1 = D1;
+    s.D2 = D2;
+    int nslot = 0;
+    uint64_t hz = 0ull;
+    if (act) {
+        for (int r = 0; r < k && r < 32; r++) R32(r) = (uint32_t)pJ[r];
+        for (int r = 32; r < k; r++) R64(r) = pJ[r];
+        // slots: the prefix zeros (the shrinks here), then every position below pm
+        for (uint64_t zz = pz; zz; nslot++) {
+            const int c = 63 - hd_clz64(zz);
+            zz &= ~bit1(c);
+            RG(nslot) = pGT[c];
+            hz |= (uint64_t)getbit(h, c) << nslot;
+        }
+        for (int c = nlow - 1; c >= 0; c--, nslot++) {
+            RG(nslot) = pGT[c];
+            hz |= (uint64_t)getbit(h, c) << nslot;
+        }
+    }
+    s.h = hz;
+    bool alive = act;
+    const int NQ = uniform_max(npz);
+    for (int q = 0; q < NQ; q++) {
+        const bool a = alive && q < npz;
+        const bool wide = uniform_max(a ? s.k : 0) > CSIM_TP_WIDE_FROM;
+        const int r = wide ? tp_shrink<uint64_t>(s, M, q, nslot, a) : tp_shrink<uint32_t>(s, M, q, nslot, a);
+        if (a && r == 0) alive = false;
+    }
+    if (!act) return 1;
+    if (!alive) return 0;
+    const int k2 = s.k;
+    const uint64_t km = lowmask(k2);
+    for (int r = 0; r < k2; r++) pJ[r] = read_row<uint64_t>(M, r, k2) & km;
+    uint64_t h2 = 0ull;
+    for (int c = 0; c < n; c++) {
+        if (c < nlow) {
+            const int slot = npz + nlow - 1 - c;
+            pGT[c] = RG(slot) & km;
+            h2 |= (uint64_t)getbit(s.h, slot) << c;
+        } else {
+            pGT[c] = 0ull;  // a prefix position: no pair shrinks by it again
+        }
+    }
+    k = k2;
+    Q = s.Q;
+    h = h2;
+    D1 = s.D1;
+    D2 = s.D2;
+    return 1;
+}
+
+// Top bits of [0, n) on which codewords that differ in the bits `dis` agree
+CSIM_HD inline uint64_t agree_top(uint64_t dis, int n) {
+    const uint64_t d = dis & lowmask(n);
+    return lowmask(n) & ~lowmask(64 - hd_clz64(d));
 }
 
 #undef R32

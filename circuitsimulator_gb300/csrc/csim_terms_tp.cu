@@ -30,11 +30,12 @@ namespace csim {
 constexpr int kTP = 64;  // threads per block
 
 struct TPShared {
-    // pristine theta
+    // theta, then the state its pairs start from (prefix_shrink)
     uint64_t pJ[64];
     uint64_t pGT[64];
     uint64_t h, D1, D2;
-    int n, k, Q, live;
+    unsigned long long dis;  // bits in which the block's codewords differ
+    int n, k, Q, live, dead;
     __int128 red[kTP / 32][4];
 };
 
@@ -71,6 +72,8 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
             sh.h = theta[a].h;
             sh.D1 = theta[a].D1;
             sh.D2 = theta[a].D2;
+            sh.dis = 0ull;
+            sh.dead = 0;
         }
         {
             const GState* g = theta + a;
@@ -83,6 +86,19 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
             sh.pGT[tid] = col;
         }
         __syncthreads();
+        const int64_t jb = j0 + cb * span;
+        const uint64_t x0 = codewords[jb - j0];
+        {  // the bits in which the block's codewords differ
+            uint64_t dis = 0ull;
+            for (int r = 0; r < per_thread; r++) {
+                const int64_t j = jb + tid + (int64_t)kTP * r;
+                if (j < j0 + nj) dis |= codewords[j - j0] ^ x0;
+            }
+            dis = ((uint64_t)__reduce_or_sync(kFull, (unsigned)(dis >> 32)) << 32) |
+                  __reduce_or_sync(kFull, (unsigned)dis);
+            if ((tid & 31) == 0 && dis) atomicOr(&sh.dis, (unsigned long long)dis);
+        }
+        const int k0 = sh.k;  // theta's own (prefix_shrink replaces sh.k after the next barrier)
         // the pair routine relies on a symmetric J (true of every state drawn
         // and projected by this library); anything else is refused
         bool asym = false;
@@ -93,16 +109,29 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
         const int n = sh.n;
         if (n > nmax || asym) e |= kErrArg;
         if (sh.live && !asym && n >= 1 && n <= nmax) {
+            // the shrinks all of the block's pairs share (the zeros of the
+            // codewords' common top bits) run once, on one lane
+            const uint64_t pm = pc::agree_top(sh.dis, n);
+            if (pc::hd_popc64(~x0 & pm & pc::lowmask(n)) > 0) {
+                if (tid < 32) {
+                    const pc::PairMem pmem = pc::pair_mem(smem_raw + sizeof(TPShared), nmax, 1, 0);
+                    const int ok = pc::prefix_shrink(tid == 0, n, pm, x0, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ,
+                                                     sh.pGT, pmem);
+                    if (tid == 0) sh.dead = !ok;
+                }
+                __syncthreads();
+            }
             const pc::PairMem mem = pc::pair_mem(smem_raw + sizeof(TPShared), nmax, kTP, tid);
-            const int64_t jb = j0 + cb * span;
+            const bool dead = sh.dead != 0;
             for (int r = 0; r < per_thread; r++) {
                 const int64_t j = jb + tid + (int64_t)kTP * r;
                 const bool valid = j < j0 + nj;
                 if (__all_sync(kFull, !valid)) break;  // warp-uniform exit
                 const uint64_t x = valid ? codewords[j - j0] : 0ull;
-                int eps, pp, mm;
-                pc::pair_l(valid, n, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ, sh.pGT, x, mem,
-                           eps, pp, mm, e, gmax);
+                int eps = 0, pp = 0, mm = 0;
+                if (!dead)
+                    pc::pair_l(valid, n, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ, sh.pGT, x, mem, eps, pp, mm, e, gmax,
+                               pm, k0);
                 if (!valid) continue;
                 pc::zacc(z, eps, pp, mm, P, e);
                 if (eps_o) {

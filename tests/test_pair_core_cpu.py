@@ -29,17 +29,39 @@ def tp(request):
     lib = C.CDLL(so)
     lib.tp_host_pairs.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
     lib.tp_host_pairs.restype = C.c_int
+    lib.tp_host_block.argtypes = lib.tp_host_pairs.argtypes
+    lib.tp_host_block.restype = C.c_int
 
-    def run(thetas, xs):
+    def run(thetas, xs, block=False):
         thetas = np.ascontiguousarray(thetas)
         xs = np.ascontiguousarray(np.asarray(xs, dtype=np.uint64))
         n = len(thetas) * len(xs)
         e, p, m = (np.zeros(n, dtype=np.int32) for _ in range(3))
-        err = lib.tp_host_pairs(thetas.ctypes.data, len(thetas), xs.ctypes.data, len(xs), e.ctypes.data,
-                                p.ctypes.data, m.ctypes.data)
+        fn = lib.tp_host_block if block else lib.tp_host_pairs
+        err = fn(thetas.ctypes.data, len(thetas), xs.ctypes.data, len(xs), e.ctypes.data, p.ctypes.data,
+                 m.ctypes.data)
         return err, e, p, m
 
     return run
+
+
+def _projected_thetas(oracle, rs, t, count=8):
+    rows = random_projector_rows(rs, t, max(1, t // 3))
+    r = oracle.rng(t)
+    thetas = []
+    for _ in range(5 * count):
+        s = oracle.random_state(t, r)
+        pf = 1.0
+        for q in range(len(rows[0])):
+            res = oracle.measure_pauli(s, phase_m(rows[0][q]), rows[2][q], rows[1][q])
+            pf *= res
+            if res == 0:
+                break
+        if pf:
+            thetas.append(s[0])
+        if len(thetas) == count:
+            break
+    return np.array(thetas)
 
 
 @pytest.mark.parametrize("t,k", [(1, 1), (2, 2), (3, 3), (6, 4), (12, 6), (24, 8), (31, 8), (33, 8), (40, 10),
@@ -91,3 +113,33 @@ def test_pair_core_golden(tp, golden_seeded):
         assert err == 0
         got = np.stack([e, p, m], axis=1).reshape(len(thetas), len(xs), 3)
         assert got.tolist() == ent["prod_l"]
+
+
+@pytest.mark.parametrize("t,k,d", [(3, 2, 1), (6, 3, 2), (12, 5, 4), (24, 6, 8), (33, 6, 10), (40, 8, 7),
+                                   (40, 8, 16), (57, 6, 20), (64, 6, 24)])
+def test_shared_prefix_vs_oracle(tp, oracle, t, k, d):
+    """The kernels' block path (the shrinks of the codewords' common top bits
+    once per theta, then each pair from there) against the oracle: codeword
+    sets whose top d bits agree, split by the coefficient of the one row of L
+    that has top bits (all-zero and mixed prefixes), and a single codeword
+    (every shrink shared)."""
+    rs = np.random.RandomState(900 + t + d)
+    low = (1 << (t - d)) - 1
+    L = [rand_word(rs, t) & low for _ in range(k)]
+    L[0] |= rand_word(rs, t) & ~low & ((1 << t) - 1)
+    L = np.array(L, dtype=np.uint64)
+    thetas = _projected_thetas(oracle, rs, t)
+    js = np.unique(rs.randint(0, 2 ** k, size=40))
+    top = 1 << (k - 1)  # j's bit of row 0 (codeword() takes row r at bit k-1-r)
+    for subset in ([j for j in js if j & top], [j for j in js if not j & top], [js[0]]):
+        if not subset:
+            continue
+        xs = [oracle.codeword(int(j), L) for j in subset]
+        err, e, p, m = tp(thetas, xs, block=True)
+        assert err == 0
+        w = 0
+        for a in range(len(thetas)):
+            for j in subset:
+                want = oracle.inner_product(thetas[a:a + 1], oracle.prep_l(int(j), t, L))
+                assert (e[w], p[w], m[w]) == want, (t, d, a, int(j))
+                w += 1
