@@ -15,6 +15,7 @@
 
 #include "csim_batch.h"
 #include "csim_internal.h"
+#include "csim_block_prefix.cuh"
 #include "csim_pair_core.cuh"
 #include "csim_rng.cuh"
 #include "csim_warp.cuh"
@@ -84,12 +85,8 @@ __global__ void __launch_bounds__(256) k_draw_project(const DrawDesc* desc, int6
 constexpr int kTPB = 64;
 
 struct ItemShared {
-    // the item's state, then the state its pairs start from (prefix_shrink)
-    uint64_t pJ[64];
-    uint64_t pGT[64];
-    uint64_t h, D1, D2;
-    unsigned long long dis;  // bits in which the item's codewords differ
-    int n, k, Q, live, dead;
+    pc::BlockPrefix bp;  // the item's state, then the states its two codeword groups start from
+    int n, live;
     __int128 red[kTPB / 32][8];
 };
 
@@ -116,68 +113,51 @@ __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_
         if (tid == 0) {
             sh.live = codes[it.theta] >= 0;
             sh.n = g->n;
-            sh.k = g->k;
-            sh.Q = g->Q;
-            sh.h = g->h;
-            sh.D1 = g->D1;
-            sh.D2 = g->D2;
-            sh.dis = 0ull;
-            sh.dead = 0;
+            pc::BlockState& t0 = sh.bp.st[0];
+            t0.k = g->k;
+            t0.Q = g->Q;
+            t0.h = g->h;
+            t0.D1 = g->D1;
+            t0.D2 = g->D2;
+            for (int q = 0; q < 3; q++) {
+                sh.bp.andm[q] = ~0ull;
+                sh.bp.orm[q] = 0ull;
+            }
         }
+        const int k0 = g->k;  // the state's own k, for p's correction
         {
-            sh.pJ[tid] = g->J[tid];
-            const int n = g->n, k = g->k;
+            sh.bp.st[0].pJ[tid] = g->J[tid];
+            const int n = g->n;
             uint64_t col = 0ull;
             if (tid < n)
-                for (int r = 0; r < k; r++) col |= ((g->G[r] >> tid) & 1ull) << r;
-            sh.pGT[tid] = col;
+                for (int r = 0; r < k0; r++) col |= ((g->G[r] >> tid) & 1ull) << r;
+            sh.bp.st[0].pGT[tid] = col;
         }
         __syncthreads();
-        const uint64_t x0 = it.nj > 0 ? it.cw[it.j0] : 0ull;
-        {  // the bits in which the item's codewords differ
-            uint64_t dis = 0ull;
-            for (int r = 0; r < per_thread; r++) {
-                const int64_t j = it.j0 + tid + (int64_t)kTPB * r;
-                if (j < it.j0 + it.nj) dis |= it.cw[j] ^ x0;
-            }
-            dis = ((uint64_t)__reduce_or_sync(kFull, (unsigned)(dis >> 32)) << 32) |
-                  __reduce_or_sync(kFull, (unsigned)dis);
-            if ((tid & 31) == 0 && dis) atomicOr(&sh.dis, (unsigned long long)dis);
-        }
-        const int k0 = sh.k;  // the state's own (prefix_shrink replaces sh.k after the next barrier)
         bool asym = false;
-        if (tid < sh.k)
-            for (int r = 0; r < sh.k; r++) asym |= ((sh.pJ[tid] >> r) & 1ull) != ((sh.pJ[r] >> tid) & 1ull);
+        if (tid < k0)
+            for (int r = 0; r < k0; r++)
+                asym |= ((sh.bp.st[0].pJ[tid] >> r) & 1ull) != ((sh.bp.st[0].pJ[r] >> tid) & 1ull);
         asym = __syncthreads_or(asym) != 0;
         __int128 z[4] = {0, 0, 0, 0}, zd[4] = {0, 0, 0, 0};
         int deps = 0, dp = 0, dm = 0;  // the diagonal pair, summed apart after the loop
         const int n = sh.n;
         if (n > nmax || asym) e |= kErrArg;
         if (sh.live && !asym && n >= 1 && n <= nmax) {
-            // the shrinks all of the item's pairs share (the zeros of the
-            // codewords' common top bits) run once, on one lane
-            const uint64_t pm = pc::agree_top(sh.dis, n);
-            if (it.nj > 0 && pc::hd_popc64(~x0 & pm & pc::lowmask(n)) > 0) {
-                if (tid < 32) {
-                    const pc::PairMem pmem = pc::pair_mem(smem_raw + sizeof(ItemShared), nmax, 1, 0);
-                    const int ok = pc::prefix_shrink(tid == 0, n, pm, x0, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ,
-                                                     sh.pGT, pmem);
-                    if (tid == 0) sh.dead = !ok;
-                }
-                __syncthreads();
-            }
-            const bool dead = sh.dead != 0;
+            // the shrinks that each of the item's two codeword groups shares run once
+            pc::block_prefix<kTPB>(sh.bp, it.cw + it.j0, it.nj, per_thread, n, nmax, smem_raw + sizeof(ItemShared));
             const pc::PairMem mem = pc::pair_mem(smem_raw + sizeof(ItemShared), nmax, kTPB, tid);
+            const int split = sh.bp.split;
             const int P = 2 * n;
             for (int r = 0; r < per_thread; r++) {
                 const int64_t j = it.j0 + tid + (int64_t)kTPB * r;
                 const bool valid = j < it.j0 + it.nj;
                 if (__all_sync(kFull, !valid)) break;
                 const uint64_t x = valid ? it.cw[j] : 0ull;
+                const pc::BlockState& st = sh.bp.st[split >= 0 ? (int)((x >> split) & 1ull) : 0];
                 int eps = 0, pp = 0, mm = 0;
-                if (!dead)
-                    pc::pair_l(valid, n, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ, sh.pGT, x, mem, eps, pp, mm, e, gmax,
-                               pm, k0);
+                pc::pair_l(valid && !st.dead, n, st.k, st.Q, st.h, st.D1, st.D2, st.pJ, st.pGT, x, mem, eps, pp, mm,
+                           e, gmax, st.done, k0);
                 if (!valid) continue;
                 pc::zacc(z, eps, pp, mm, P, e);
                 if (j == it.diag) {

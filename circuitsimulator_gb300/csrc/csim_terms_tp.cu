@@ -22,6 +22,7 @@
 #include <cstdint>
 
 #include "csim_internal.h"
+#include "csim_block_prefix.cuh"
 #include "csim_pair_core.cuh"
 #include "csim_warp.cuh"
 
@@ -30,12 +31,8 @@ namespace csim {
 constexpr int kTP = 64;  // threads per block
 
 struct TPShared {
-    // theta, then the state its pairs start from (prefix_shrink)
-    uint64_t pJ[64];
-    uint64_t pGT[64];
-    uint64_t h, D1, D2;
-    unsigned long long dis;  // bits in which the block's codewords differ
-    int n, k, Q, live, dead;
+    pc::BlockPrefix bp;  // theta, then the states the block's two codeword groups start from
+    int n, live;
     __int128 red[kTP / 32][4];
 };
 
@@ -67,71 +64,55 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
         if (tid == 0) {
             sh.live = code ? (code[a] >= 0) : 1;
             sh.n = theta[a].n;
-            sh.k = theta[a].k;
-            sh.Q = theta[a].Q;
-            sh.h = theta[a].h;
-            sh.D1 = theta[a].D1;
-            sh.D2 = theta[a].D2;
-            sh.dis = 0ull;
-            sh.dead = 0;
+            pc::BlockState& t0 = sh.bp.st[0];
+            t0.k = theta[a].k;
+            t0.Q = theta[a].Q;
+            t0.h = theta[a].h;
+            t0.D1 = theta[a].D1;
+            t0.D2 = theta[a].D2;
+            for (int q = 0; q < 3; q++) {
+                sh.bp.andm[q] = ~0ull;
+                sh.bp.orm[q] = 0ull;
+            }
         }
+        const GState* g = theta + a;
+        const int k0 = g->k;  // theta's own k, for p's correction
         {
-            const GState* g = theta + a;
-            sh.pJ[tid] = g->J[tid];
+            sh.bp.st[0].pJ[tid] = g->J[tid];
             // transpose G: column c as a mask over rows < k
-            const int n = g->n, k = g->k;
+            const int n = g->n;
             uint64_t col = 0ull;
             if (tid < n)
-                for (int r = 0; r < k; r++) col |= ((g->G[r] >> tid) & 1ull) << r;
-            sh.pGT[tid] = col;
+                for (int r = 0; r < k0; r++) col |= ((g->G[r] >> tid) & 1ull) << r;
+            sh.bp.st[0].pGT[tid] = col;
         }
         __syncthreads();
-        const int64_t jb = j0 + cb * span;
-        const uint64_t x0 = codewords[jb - j0];
-        {  // the bits in which the block's codewords differ
-            uint64_t dis = 0ull;
-            for (int r = 0; r < per_thread; r++) {
-                const int64_t j = jb + tid + (int64_t)kTP * r;
-                if (j < j0 + nj) dis |= codewords[j - j0] ^ x0;
-            }
-            dis = ((uint64_t)__reduce_or_sync(kFull, (unsigned)(dis >> 32)) << 32) |
-                  __reduce_or_sync(kFull, (unsigned)dis);
-            if ((tid & 31) == 0 && dis) atomicOr(&sh.dis, (unsigned long long)dis);
-        }
-        const int k0 = sh.k;  // theta's own (prefix_shrink replaces sh.k after the next barrier)
         // the pair routine relies on a symmetric J (true of every state drawn
         // and projected by this library); anything else is refused
         bool asym = false;
-        if (tid < sh.k)
-            for (int r = 0; r < sh.k; r++) asym |= ((sh.pJ[tid] >> r) & 1ull) != ((sh.pJ[r] >> tid) & 1ull);
+        if (tid < k0)
+            for (int r = 0; r < k0; r++)
+                asym |= ((sh.bp.st[0].pJ[tid] >> r) & 1ull) != ((sh.bp.st[0].pJ[r] >> tid) & 1ull);
         asym = __syncthreads_or(asym) != 0;
         __int128 z[4] = {0, 0, 0, 0};
         const int n = sh.n;
         if (n > nmax || asym) e |= kErrArg;
         if (sh.live && !asym && n >= 1 && n <= nmax) {
-            // the shrinks all of the block's pairs share (the zeros of the
-            // codewords' common top bits) run once, on one lane
-            const uint64_t pm = pc::agree_top(sh.dis, n);
-            if (pc::hd_popc64(~x0 & pm & pc::lowmask(n)) > 0) {
-                if (tid < 32) {
-                    const pc::PairMem pmem = pc::pair_mem(smem_raw + sizeof(TPShared), nmax, 1, 0);
-                    const int ok = pc::prefix_shrink(tid == 0, n, pm, x0, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ,
-                                                     sh.pGT, pmem);
-                    if (tid == 0) sh.dead = !ok;
-                }
-                __syncthreads();
-            }
+            const int64_t jb = j0 + cb * span;
+            const int64_t cnt = j0 + nj - jb < span ? j0 + nj - jb : span;
+            // the shrinks that each of the block's two codeword groups shares run once
+            pc::block_prefix<kTP>(sh.bp, codewords + (jb - j0), cnt, per_thread, n, nmax, smem_raw + sizeof(TPShared));
             const pc::PairMem mem = pc::pair_mem(smem_raw + sizeof(TPShared), nmax, kTP, tid);
-            const bool dead = sh.dead != 0;
+            const int split = sh.bp.split;
             for (int r = 0; r < per_thread; r++) {
                 const int64_t j = jb + tid + (int64_t)kTP * r;
                 const bool valid = j < j0 + nj;
                 if (__all_sync(kFull, !valid)) break;  // warp-uniform exit
                 const uint64_t x = valid ? codewords[j - j0] : 0ull;
+                const pc::BlockState& st = sh.bp.st[split >= 0 ? (int)((x >> split) & 1ull) : 0];
                 int eps = 0, pp = 0, mm = 0;
-                if (!dead)
-                    pc::pair_l(valid, n, sh.k, sh.Q, sh.h, sh.D1, sh.D2, sh.pJ, sh.pGT, x, mem, eps, pp, mm, e, gmax,
-                               pm, k0);
+                pc::pair_l(valid && !st.dead, n, st.k, st.Q, st.h, st.D1, st.D2, st.pJ, st.pGT, x, mem, eps, pp, mm,
+                           e, gmax, st.done, k0);
                 if (!valid) continue;
                 pc::zacc(z, eps, pp, mm, P, e);
                 if (eps_o) {

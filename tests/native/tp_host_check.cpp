@@ -31,40 +31,69 @@ extern "C" int tp_host_pairs(const csim_state* theta, int ntheta, const uint64_t
     return err;
 }
 
-// The kernels' block path: the shrinks by the zeros of the codewords' common
-// top bits run once per theta (prefix_shrink), then every pair continues from
-// that state (pair_l with done = those bits).
+// The kernels' block path (csim_block_prefix.cuh): the codewords split in two
+// groups at the highest bit in which they differ; each group's shared top-bit
+// shrinks run once per theta (prefix_shrink), then every pair continues from
+// its group's state (pair_l with done = that group's agreed top bits).
 extern "C" int tp_host_block(const csim_state* theta, int ntheta, const uint64_t* xs, int nx, int* eps, int* p,
                              int* m) {
+    using namespace csim::pc;
     int err = 0;
-    uint64_t pJ[64], pGT[64];
     alignas(16) uint32_t wJ32[32];
     alignas(16) uint64_t wJ64[34];
     alignas(16) uint64_t wG[64];
-    const csim::pc::PairMem mem{wJ32, wJ64, wG, 1};
-    uint64_t dis = 0;
-    for (int j = 0; j < nx; j++) dis |= xs[j] ^ xs[0];
+    const PairMem mem{wJ32, wJ64, wG, 1};
+    uint64_t andm[3] = {~0ull, ~0ull, ~0ull}, orm[3] = {0, 0, 0};
+    for (int j = 0; j < nx; j++) {
+        andm[0] &= xs[j];
+        orm[0] |= xs[j];
+    }
     for (int a = 0; a < ntheta; a++) {
         const csim_state& th = theta[a];
-        for (int c = 0; c < 64; c++) {
-            uint64_t col = 0;
-            if (c < th.n)
-                for (int r = 0; r < th.k; r++) col |= ((th.G[r] >> c) & 1ull) << r;
-            pGT[c] = col;
-            pJ[c] = th.J[c];
+        const uint64_t nm = lowmask(th.n);
+        const uint64_t dis = (andm[0] ^ orm[0]) & nm;
+        const int hb = dis ? 63 - hd_clz64(dis) : -1;
+        if (hb >= 0) {
+            andm[1] = andm[2] = ~0ull;
+            orm[1] = orm[2] = 0;
+            for (int j = 0; j < nx; j++) {
+                const int g = (int)((xs[j] >> hb) & 1ull);
+                andm[1 + g] &= xs[j];
+                orm[1 + g] |= xs[j];
+            }
         }
-        int k = th.k, Q = th.Q;
-        uint64_t h = th.h, D1 = th.D1, D2 = th.D2;
-        const uint64_t pm = nx > 0 ? csim::pc::agree_top(dis, th.n) : 0ull;
-        int ok = 1;
-        if (nx > 0 && csim::pc::hd_popc64(~xs[0] & pm & csim::pc::lowmask(th.n)) > 0)
-            ok = csim::pc::prefix_shrink(true, th.n, pm, xs[0], k, Q, h, D1, D2, pJ, pGT, mem);
+        struct {
+            uint64_t pJ[64], pGT[64], h, D1, D2, done;
+            int k, Q, ok;
+        } st[2];
+        for (int g = 0; g < (hb >= 0 ? 2 : 1); g++) {
+            for (int c = 0; c < 64; c++) {
+                uint64_t col = 0;
+                if (c < th.n)
+                    for (int r = 0; r < th.k; r++) col |= ((th.G[r] >> c) & 1ull) << r;
+                st[g].pGT[c] = col;
+                st[g].pJ[c] = th.J[c];
+            }
+            st[g].k = th.k;
+            st[g].Q = th.Q;
+            st[g].h = th.h;
+            st[g].D1 = th.D1;
+            st[g].D2 = th.D2;
+            const uint64_t am = hb >= 0 ? andm[1 + g] : andm[0], om = hb >= 0 ? orm[1 + g] : orm[0];
+            const uint64_t pm = agree_top(am ^ om, th.n);
+            st[g].done = pm;
+            st[g].ok = 1;
+            if (hd_popc64(~am & pm & nm) > 0)
+                st[g].ok = prefix_shrink(true, th.n, pm, am, st[g].k, st[g].Q, st[g].h, st[g].D1, st[g].D2, st[g].pJ,
+                                         st[g].pGT, mem);
+        }
         for (int j = 0; j < nx; j++) {
             const int w = a * nx + j;
+            const auto& s = st[hb >= 0 ? (int)((xs[j] >> hb) & 1ull) : 0];
             eps[w] = p[w] = m[w] = 0;
-            if (ok)
-                csim::pc::pair_l(true, th.n, k, Q, h, D1, D2, pJ, pGT, xs[j], mem, eps[w], p[w], m[w], err, 64, pm,
-                                 th.k);
+            if (s.ok)
+                pair_l(true, th.n, s.k, s.Q, s.h, s.D1, s.D2, s.pJ, s.pGT, xs[j], mem, eps[w], p[w], m[w], err, 64,
+                       s.done, th.k);
         }
     }
     return err;

@@ -118,11 +118,12 @@ def test_pair_core_golden(tp, golden_seeded):
 @pytest.mark.parametrize("t,k,d", [(3, 2, 1), (6, 3, 2), (12, 5, 4), (24, 6, 8), (33, 6, 10), (40, 8, 7),
                                    (40, 8, 16), (57, 6, 20), (64, 6, 24)])
 def test_shared_prefix_vs_oracle(tp, oracle, t, k, d):
-    """The kernels' block path (the shrinks of the codewords' common top bits
-    once per theta, then each pair from there) against the oracle: codeword
+    """The kernels' block path (two codeword groups split at the highest bit in
+    which the codewords differ; each group's shared top-bit shrinks once per
+    theta, then each pair from its group's state) against the oracle: codeword
     sets whose top d bits agree, split by the coefficient of the one row of L
-    that has top bits (all-zero and mixed prefixes), and a single codeword
-    (every shrink shared)."""
+    that has top bits (all-zero and mixed prefixes), the whole set (two groups
+    at the top bits), and a single codeword (every shrink shared)."""
     rs = np.random.RandomState(900 + t + d)
     low = (1 << (t - d)) - 1
     L = [rand_word(rs, t) & low for _ in range(k)]
@@ -131,7 +132,7 @@ def test_shared_prefix_vs_oracle(tp, oracle, t, k, d):
     thetas = _projected_thetas(oracle, rs, t)
     js = np.unique(rs.randint(0, 2 ** k, size=40))
     top = 1 << (k - 1)  # j's bit of row 0 (codeword() takes row r at bit k-1-r)
-    for subset in ([j for j in js if j & top], [j for j in js if not j & top], [js[0]]):
+    for subset in ([j for j in js if j & top], [j for j in js if not j & top], list(js), [js[0]]):
         if not subset:
             continue
         xs = [oracle.codeword(int(j), L) for j in subset]
