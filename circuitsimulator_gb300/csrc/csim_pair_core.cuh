@@ -526,8 +526,11 @@ CSIM_HD inline void tp_exp_sum(PairRegs& s, const PairMem& M, bool act, int& eps
     const W keep = (sizeof(W) == 8 && sidx >= 32) ? wbit<W>(sidx) : (W)0;
     WAcc w0 = {0, 0, 0}, w1 = {0, 0, 0};
     const bool any = E != (W)0;
+    // at most popc(E) steps; a dimer retires two rows, so the warp is usually
+    // done well before that, and a step with no lane in play changes nothing
     const int NE = uniform_max(T::popc(E));
     for (int it = 0; it < NE; it++) {
+        if (uniform_max(E != (W)0 ? 1 : 0) == 0) break;
         const bool live = E != (W)0;
         const int a = live ? T::ffs(E) - 1 : 0;
         const W ra = live ? read_row<W>(M, a, k) : (W)0;
