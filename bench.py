@@ -293,10 +293,11 @@ C3_WORKLOAD = os.path.join(ROOT, "tests", "golden", "workload_c3.json.gz")
 C3_LIGHT_PAIRS = 1 << 26
 
 
-def c3_queries(light=True):
+def c3_queries(light=True, every=1):
     """The batched-query workload (tests/golden/workload_c3.json.gz, 256 queries,
     t ~ U[8, 60], relative error 0.05).  light=True keeps the queries of at most
-    2^26 inner products, the ones too small to fill the GPU on their own."""
+    2^26 inner products, the ones too small to fill the GPU on their own;
+    every > 1 keeps every every-th query of the file (before that filter)."""
     import gzip
 
     from circuitsimulator_gb300 import backend
@@ -304,7 +305,7 @@ def c3_queries(light=True):
     with gzip.open(C3_WORKLOAD, "rt") as f:
         recs = json.load(f)
     out = []
-    for q in recs:
+    for q in recs[::every]:
         cfg, projs = backend.parse_protocol(q["input"])
         t, k, ex = cfg["t"], cfg["k"], cfg["exact"]
         chi = 2 ** ((t + 1) // 2) if ex else 2 ** k
@@ -317,12 +318,13 @@ def c3_queries(light=True):
     return out, len(recs)
 
 
-def batch_compare(gpu, reps=3, light=True):
+def batch_compare(gpu, reps=3, light=True, every=1):
     """Batched vs plain queries/s on the c3 queries (the light ones by default,
-    all 256 with light=False): the same queries, the same draws, results
-    checked identical.  Plain = one query after another through the
-    single-query entry points; batched = csim_run_queries."""
-    qs, total = c3_queries(light=light)
+    all 256 with light=False, every every-th of them with every > 1): the
+    same queries, the same draws, results checked identical.  Plain = one
+    query after another through the single-query entry points; batched =
+    csim_run_queries."""
+    qs, total = c3_queries(light=light, every=every)
     gpu.run_queries(qs[:4], batched=True)
     gpu.run_queries(qs[:4], batched=False)
     tp, tb = [], []
@@ -340,8 +342,13 @@ def batch_compare(gpu, reps=3, light=True):
                             for a, b in zip(rp, rb))
         pairs = sum(b["pairs"] for b in rb)
     p, b = float(np.median(tp)), float(np.median(tb))
-    what = ("c3 light: the %d of %d c3 queries with <= 2^26 inner products (t 8..23" % (len(qs), total) if light
-            else "c3: all %d queries (t 8..60, chi 2^4..2^18" % total)
+    if light:
+        what = "c3 light: the %d of %d c3 queries with <= 2^26 inner products (t 8..23" % (len(qs), total)
+    elif every > 1:
+        what = "c3 sample: every %dth of the %d c3 queries, %d queries (t %d..%d" % (
+            every, total, len(qs), min(q["cfg"]["t"] for q in qs), max(q["cfg"]["t"] for q in qs))
+    else:
+        what = "c3: all %d queries (t 8..60, chi 2^4..2^18" % total
     return {"workload": what + ", relative error 0.05, Philox draws)",
             "metric": "queries/s", "plain": len(qs) / p, "batched": len(qs) / b, "speedup": p / b,
             "identical_results": bool(same), "pairs": pairs, "reps": reps,
@@ -511,11 +518,13 @@ def main():
     ap.add_argument("--serve-count", type=int, default=300, help="queries per rate for --serve")
     ap.add_argument("--c3-full", action="store_true",
                     help="only time all 256 c3 queries, plain vs batched (about 10 minutes per arm)")
+    ap.add_argument("--c3-every", type=int, default=None, metavar="N",
+                    help="only time every N-th of the 256 c3 queries, plain vs batched")
     args = ap.parse_args()
-    if args.c3_full:
+    if args.c3_full or args.c3_every:
         from circuitsimulator_gb300 import backend
 
-        print(json.dumps(batch_compare(backend.Backend(0), reps=1, light=False)))
+        print(json.dumps(batch_compare(backend.Backend(0), reps=1, light=False, every=args.c3_every or 1)))
         return
     if args.serve:
         rates = [float(r) for r in args.serve.split(",")]
