@@ -345,7 +345,7 @@ def batch_compare(gpu, reps=3, light=True, every=1):
     if light:
         what = "c3 light: the %d of %d c3 queries with <= 2^26 inner products (t 8..23" % (len(qs), total)
     elif every > 1:
-        what = "c3 sample: every %dth of the %d c3 queries, %d queries (t %d..%d" % (
+        what = "c3 sample: 1 in %d of the %d c3 queries, %d queries (t %d..%d" % (
             every, total, len(qs), min(q["cfg"]["t"] for q in qs), max(q["cfg"]["t"] for q in qs))
     else:
         what = "c3: all %d queries (t 8..60, chi 2^4..2^18" % total
