@@ -502,11 +502,13 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
         CK(cudaMemsetAsync(dpart, 0, nparts * sizeof(__int128), ctx->stream));
         // With the C library's draws the host makes every state's rand() words.
         // The batch goes in sub-batches: the host draws sub-batch s+1 while the
-        // GPU works on sub-batch s, all launches queued on the stream.
+        // GPU works on sub-batch s, all launches queued on the stream.  The
+        // first sub-batch is small, so the GPU starts after a short draw.
         const int64_t sub = rng == CSIM_RNG_LIBC ? std::min<int64_t>(c, 1024) : c;
+        const int64_t sub0 = rng == CSIM_RNG_LIBC ? std::min<int64_t>(c, 256) : c;
         bool first = true;
-        for (int64_t s0 = 0; s0 < c; s0 += sub) {
-            const int64_t cs = std::min(sub, c - s0);
+        for (int64_t s0 = 0; s0 < c;) {
+            const int64_t cs = std::min(first ? sub0 : sub, c - s0);
             csim::GState* sth = (csim::GState*)((csim_state*)dth + s0);
             int* scode = dcode + s0;
             if (rng == CSIM_RNG_LIBC) {
@@ -550,6 +552,7 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
                                         scode, cs, 0, chi, (int)chunk, P2, spart, nullptr, nullptr, nullptr, nullptr);
             }
             if (rc) return fail(ctx, CSIM_ERR_CUDA, "term launch failed");
+            s0 += cs;
         }
         CK(cudaEventRecord(ctx->ev[2], ctx->stream));
         CKR(dbuf(ctx, kBufAcc, (size_t)c * 4 * sizeof(__int128), &v));
