@@ -318,6 +318,49 @@ def test_c2_shape_sampler_checksum(gpu):
     assert checked >= 2
 
 
+@pytest.mark.parametrize("t,k,low", [(33, 8, 12), (40, 10, 20), (64, 12, 30)])
+def test_shared_prefix_codes_vs_oracle(gpu, oracle, t, k, low):
+    """Codes whose codewords share long top bits: two rows of L span all t bits,
+    the rest only the low `low` bits, so each block's two codeword groups share
+    t - low top bits and run their shrinks once (the block-prefix path of the
+    pair kernels, through the C ABI).  Every pair bit-exact against the oracle,
+    in term order; and the sampler (ordered table) equal to the exact sum of
+    its own draws' pairs."""
+    rs = np.random.RandomState(3000 + t)
+    mask = (1 << low) - 1
+    L = np.array([rand_word(rs, t) if r < 2 else rand_word(rs, t) & mask for r in range(k)], dtype=np.uint64)
+    rows = random_projector_rows(rs, t, max(1, t // 5))
+    th = gpu.randomStabilizerState(t, 24, seed=55 + t)
+    th, _ = _project_all(gpu, th, rows)
+    th = th[:6]
+    assert len(th) > 0
+    eg, pg, mg = gpu.term_products(t, False, L, th, 0, 2 ** k)
+    eo, po, mo = oracle.term_products(t, 0, L, k, th, 0, 2 ** k, threads=os.cpu_count() or 1)
+    assert (eg.reshape(-1) == eo).all() and (pg.reshape(-1) == po).all() and (mg.reshape(-1) == mo).all()
+    P = backend.projector(rows[0], rows[1], rows[2], t)
+    count, seed = 6, 17
+    vals = gpu.singleProjectorSample(P, [int(v) for v in L], False, count, backend.RNG_PHILOX, seed)
+    drawn = gpu.randomStabilizerState(t, count, seed=seed, first=0)
+    s2 = 0.70710678118654752440
+    for i in range(count):
+        st = drawn[i:i + 1].copy()
+        pf = 1.0
+        for r in range(len(rows[0])):
+            res = gpu.measurePauli(st, phase_m(rows[0][r]), rows[2][r], rows[1][r])[0]
+            pf *= res
+            if res == 0:
+                break
+        if pf == 0:
+            assert vals[i] == 0
+            continue
+        eps, p, m = gpu.term_products(t, False, L, st, 0, 2 ** k)
+        z = _exact_sum(eps[0], p[0], m[0], 2 * t)
+        re = (z[0] + (z[1] - z[3]) * s2) * 2.0 ** -t
+        im = (z[2] + (z[1] + z[3]) * s2) * 2.0 ** -t
+        want = 2.0 ** t * ((re * pf) ** 2 + (im * pf) ** 2)
+        assert close(vals[i], want, 1e-13, 1e-300), (i, vals[i], want)
+
+
 @pytest.mark.parametrize("t,k", [(12, 6), (40, 16), (64, 12)])
 def test_pair_kernels_agree(gpu, t, k):
     """Thread-per-pair and warp-per-pair kernels: identical per-pair results and
