@@ -84,8 +84,10 @@ __global__ void __launch_bounds__(256) k_draw_project(const DrawDesc* desc, int6
 // ------------------------------------------------------------ thread-per-pair items
 constexpr int kTPB = 64;
 
+// Shared memory of a block: this struct, then the group states' J rows and G
+// columns (pc::block_state_bytes(nmax)), then the pairs' working memory
 struct ItemShared {
-    pc::BlockPrefix bp;  // the item's state, then the states its two codeword groups start from
+    pc::BlockPrefix bp;  // the item's state (group 0), then the states its codeword groups start from
     int n, live;
     __int128 red[kTPB / 32][8];
 };
@@ -104,6 +106,8 @@ __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_
                                                    __int128* part, __int128* part_diag, int* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ItemShared& sh = *reinterpret_cast<ItemShared*>(smem_raw);
+    uint64_t* const sa = reinterpret_cast<uint64_t*>(smem_raw + sizeof(ItemShared));
+    unsigned char* const pair_base = smem_raw + sizeof(ItemShared) + pc::block_state_bytes(nmax);
     const int tid = threadIdx.x;
     int e = 0;
     for (int64_t w = blockIdx.x; w < nitems; w += gridDim.x) {
@@ -113,51 +117,53 @@ __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_
         if (tid == 0) {
             sh.live = codes[it.theta] >= 0;
             sh.n = g->n;
-            pc::BlockState& t0 = sh.bp.st[0];
+            pc::BlockScalars& t0 = sh.bp.sc[0];
             t0.k = g->k;
             t0.Q = g->Q;
             t0.h = g->h;
             t0.D1 = g->D1;
             t0.D2 = g->D2;
-            for (int q = 0; q < 3; q++) {
+            for (int q = 0; q < 7; q++) {
                 sh.bp.andm[q] = ~0ull;
                 sh.bp.orm[q] = 0ull;
             }
         }
         const int k0 = g->k;  // the state's own k, for p's correction
-        {
-            sh.bp.st[0].pJ[tid] = g->J[tid];
+        uint64_t* const r0 = pc::block_state_rows(sa, nmax, 0);
+        if (tid < nmax) {
+            r0[tid] = g->J[tid];
             const int n = g->n;
             uint64_t col = 0ull;
             if (tid < n)
                 for (int r = 0; r < k0; r++) col |= ((g->G[r] >> tid) & 1ull) << r;
-            sh.bp.st[0].pGT[tid] = col;
+            r0[nmax + tid] = col;
         }
         __syncthreads();
         bool asym = false;
-        if (tid < k0)
-            for (int r = 0; r < k0; r++)
-                asym |= ((sh.bp.st[0].pJ[tid] >> r) & 1ull) != ((sh.bp.st[0].pJ[r] >> tid) & 1ull);
+        if (tid < k0 && k0 <= nmax)
+            for (int r = 0; r < k0; r++) asym |= ((r0[tid] >> r) & 1ull) != ((r0[r] >> tid) & 1ull);
         asym = __syncthreads_or(asym) != 0;
         __int128 z[4] = {0, 0, 0, 0}, zd[4] = {0, 0, 0, 0};
         int deps = 0, dp = 0, dm = 0;  // the diagonal pair, summed apart after the loop
         const int n = sh.n;
         if (n > nmax || asym) e |= kErrArg;
         if (sh.live && !asym && n >= 1 && n <= nmax) {
-            // the shrinks that each of the item's two codeword groups shares run once
-            pc::block_prefix<kTPB>(sh.bp, it.cw + it.j0, it.nj, per_thread, n, nmax, smem_raw + sizeof(ItemShared));
-            const pc::PairMem mem = pc::pair_mem(smem_raw + sizeof(ItemShared), nmax, kTPB, tid);
-            const int split = sh.bp.split;
+            // the shrinks that each of the item's codeword groups shares run once
+            pc::block_prefix<kTPB>(sh.bp, sa, nmax, it.cw + it.j0, it.nj, per_thread, n, pair_base);
+            const pc::PairMem mem = pc::pair_mem(pair_base, nmax, kTPB, tid);
+            const int split1 = sh.bp.split1, split2a = sh.bp.split2[0], split2b = sh.bp.split2[1];
             const int P = 2 * n;
             for (int r = 0; r < per_thread; r++) {
                 const int64_t j = it.j0 + tid + (int64_t)kTPB * r;
                 const bool valid = j < it.j0 + it.nj;
                 if (__all_sync(kFull, !valid)) break;
                 const uint64_t x = valid ? it.cw[j] : 0ull;
-                const pc::BlockState& st = sh.bp.st[split >= 0 ? (int)((x >> split) & 1ull) : 0];
+                const int gr = pc::block_group(split1, split2a, split2b, x);
+                const pc::BlockScalars& st = sh.bp.sc[gr];
+                const uint64_t* rows = pc::block_state_rows(sa, nmax, gr);
                 int eps = 0, pp = 0, mm = 0;
-                pc::pair_l(valid && !st.dead, n, st.k, st.Q, st.h, st.D1, st.D2, st.pJ, st.pGT, x, mem, eps, pp, mm,
-                           e, gmax, st.done, k0);
+                pc::pair_l(valid && !st.dead, n, st.k, st.Q, st.h, st.D1, st.D2, rows, rows + nmax, x, mem, eps, pp,
+                           mm, e, gmax, st.done, k0);
                 if (!valid) continue;
                 pc::zacc(z, eps, pp, mm, P, e);
                 if (j == it.diag) {
@@ -247,7 +253,9 @@ __global__ void k_reduce_slots(const __int128* part, const int64_t* range, const
 }
 
 // ------------------------------------------------------------ launchers
-size_t items_tp_smem(int nmax, int gmax) { return sizeof(ItemShared) + pc::pair_mem_bytes(nmax, gmax, kTPB); }
+size_t items_tp_smem(int nmax, int gmax) {
+    return sizeof(ItemShared) + pc::block_state_bytes(nmax) + pc::pair_mem_bytes(nmax, gmax, kTPB);
+}
 
 int launch_draw_project(const Launch& L, const DrawDesc* desc, int64_t count, GState* out, int* code) {
     if (count <= 0) return 0;

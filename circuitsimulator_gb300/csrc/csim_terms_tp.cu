@@ -30,8 +30,10 @@ namespace csim {
 
 constexpr int kTP = 64;  // threads per block
 
+// Shared memory of a block: this struct, then the group states' J rows and G
+// columns (pc::block_state_bytes(nmax)), then the pairs' working memory
 struct TPShared {
-    pc::BlockPrefix bp;  // theta, then the states the block's two codeword groups start from
+    pc::BlockPrefix bp;  // theta (group 0), then the states the block's codeword groups start from
     int n, live;
     __int128 red[kTP / 32][4];
 };
@@ -53,6 +55,8 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
                                                   int64_t part_base, int* eps_o, int* p_o, int* m_o, int* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TPShared& sh = *reinterpret_cast<TPShared*>(smem_raw);
+    uint64_t* const sa = reinterpret_cast<uint64_t*>(smem_raw + sizeof(TPShared));
+    unsigned char* const pair_base = smem_raw + sizeof(TPShared) + pc::block_state_bytes(nmax);
     const int tid = threadIdx.x;
     int e = 0;
     const int64_t span = (int64_t)kTP * per_thread;
@@ -64,35 +68,35 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
         if (tid == 0) {
             sh.live = code ? (code[a] >= 0) : 1;
             sh.n = theta[a].n;
-            pc::BlockState& t0 = sh.bp.st[0];
+            pc::BlockScalars& t0 = sh.bp.sc[0];
             t0.k = theta[a].k;
             t0.Q = theta[a].Q;
             t0.h = theta[a].h;
             t0.D1 = theta[a].D1;
             t0.D2 = theta[a].D2;
-            for (int q = 0; q < 3; q++) {
+            for (int q = 0; q < 7; q++) {
                 sh.bp.andm[q] = ~0ull;
                 sh.bp.orm[q] = 0ull;
             }
         }
         const GState* g = theta + a;
         const int k0 = g->k;  // theta's own k, for p's correction
-        {
-            sh.bp.st[0].pJ[tid] = g->J[tid];
+        uint64_t* const r0 = pc::block_state_rows(sa, nmax, 0);
+        if (tid < nmax) {
+            r0[tid] = g->J[tid];
             // transpose G: column c as a mask over rows < k
             const int n = g->n;
             uint64_t col = 0ull;
             if (tid < n)
                 for (int r = 0; r < k0; r++) col |= ((g->G[r] >> tid) & 1ull) << r;
-            sh.bp.st[0].pGT[tid] = col;
+            r0[nmax + tid] = col;
         }
         __syncthreads();
         // the pair routine relies on a symmetric J (true of every state drawn
         // and projected by this library); anything else is refused
         bool asym = false;
-        if (tid < k0)
-            for (int r = 0; r < k0; r++)
-                asym |= ((sh.bp.st[0].pJ[tid] >> r) & 1ull) != ((sh.bp.st[0].pJ[r] >> tid) & 1ull);
+        if (tid < k0 && k0 <= nmax)
+            for (int r = 0; r < k0; r++) asym |= ((r0[tid] >> r) & 1ull) != ((r0[r] >> tid) & 1ull);
         asym = __syncthreads_or(asym) != 0;
         __int128 z[4] = {0, 0, 0, 0};
         const int n = sh.n;
@@ -100,19 +104,21 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
         if (sh.live && !asym && n >= 1 && n <= nmax) {
             const int64_t jb = j0 + cb * span;
             const int64_t cnt = j0 + nj - jb < span ? j0 + nj - jb : span;
-            // the shrinks that each of the block's two codeword groups shares run once
-            pc::block_prefix<kTP>(sh.bp, codewords + (jb - j0), cnt, per_thread, n, nmax, smem_raw + sizeof(TPShared));
-            const pc::PairMem mem = pc::pair_mem(smem_raw + sizeof(TPShared), nmax, kTP, tid);
-            const int split = sh.bp.split;
+            // the shrinks that each of the block's codeword groups shares run once
+            pc::block_prefix<kTP>(sh.bp, sa, nmax, codewords + (jb - j0), cnt, per_thread, n, pair_base);
+            const pc::PairMem mem = pc::pair_mem(pair_base, nmax, kTP, tid);
+            const int split1 = sh.bp.split1, split2a = sh.bp.split2[0], split2b = sh.bp.split2[1];
             for (int r = 0; r < per_thread; r++) {
                 const int64_t j = jb + tid + (int64_t)kTP * r;
                 const bool valid = j < j0 + nj;
                 if (__all_sync(kFull, !valid)) break;  // warp-uniform exit
                 const uint64_t x = valid ? codewords[j - j0] : 0ull;
-                const pc::BlockState& st = sh.bp.st[split >= 0 ? (int)((x >> split) & 1ull) : 0];
+                const int gr = pc::block_group(split1, split2a, split2b, x);
+                const pc::BlockScalars& st = sh.bp.sc[gr];
+                const uint64_t* rows = pc::block_state_rows(sa, nmax, gr);
                 int eps = 0, pp = 0, mm = 0;
-                pc::pair_l(valid && !st.dead, n, st.k, st.Q, st.h, st.D1, st.D2, st.pJ, st.pGT, x, mem, eps, pp, mm,
-                           e, gmax, st.done, k0);
+                pc::pair_l(valid && !st.dead, n, st.k, st.Q, st.h, st.D1, st.D2, rows, rows + nmax, x, mem, eps, pp,
+                           mm, e, gmax, st.done, k0);
                 if (!valid) continue;
                 pc::zacc(z, eps, pp, mm, P, e);
                 if (eps_o) {
@@ -140,7 +146,9 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
     if (e && (tid & 31) == 0) atomicOr(err, e);
 }
 
-size_t terms_tp_smem(int nmax, int gmax) { return sizeof(TPShared) + pc::pair_mem_bytes(nmax, gmax, kTP); }
+size_t terms_tp_smem(int nmax, int gmax) {
+    return sizeof(TPShared) + pc::block_state_bytes(nmax) + pc::pair_mem_bytes(nmax, gmax, kTP);
+}
 
 int launch_terms_tp(const Launch& L, int nmax, int gmax, const uint64_t* codewords, const GState* theta,
                     const int* code, int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P, __int128* part,

@@ -3,6 +3,7 @@
 // same source the kernel runs, checked against the oracle without a GPU.
 #include <cstring>
 
+#include "../../circuitsimulator_gb300/csrc/csim_block_prefix.cuh"
 #include "../../circuitsimulator_gb300/csrc/csim_pair_core.cuh"
 #include "../../include/csim.h"
 
@@ -32,9 +33,10 @@ extern "C" int tp_host_pairs(const csim_state* theta, int ntheta, const uint64_t
 }
 
 // The kernels' block path (csim_block_prefix.cuh): the codewords split in two
-// groups at the highest bit in which they differ; each group's shared top-bit
-// shrinks run once per theta (prefix_shrink), then every pair continues from
-// its group's state (pair_l with done = that group's agreed top bits).
+// halves at the highest bit in which they differ, each half again at its own
+// highest differing bit; each group's shared top-bit shrinks run once per
+// theta (prefix_shrink), then every pair continues from its group's state
+// (pair_l with done = that group's agreed top bits).
 extern "C" int tp_host_block(const csim_state* theta, int ntheta, const uint64_t* xs, int nx, int* eps, int* p,
                              int* m) {
     using namespace csim::pc;
@@ -43,30 +45,47 @@ extern "C" int tp_host_block(const csim_state* theta, int ntheta, const uint64_t
     alignas(16) uint64_t wJ64[34];
     alignas(16) uint64_t wG[64];
     const PairMem mem{wJ32, wJ64, wG, 1};
-    uint64_t andm[3] = {~0ull, ~0ull, ~0ull}, orm[3] = {0, 0, 0};
-    for (int j = 0; j < nx; j++) {
-        andm[0] &= xs[j];
-        orm[0] |= xs[j];
-    }
     for (int a = 0; a < ntheta; a++) {
         const csim_state& th = theta[a];
         const uint64_t nm = lowmask(th.n);
-        const uint64_t dis = (andm[0] ^ orm[0]) & nm;
-        const int hb = dis ? 63 - hd_clz64(dis) : -1;
+        // AND / OR: [0] all, [1 + h] half h, [3 + 2h + q] group 2h + q
+        uint64_t andm[7], orm[7];
+        for (int q = 0; q < 7; q++) {
+            andm[q] = ~0ull;
+            orm[q] = 0;
+        }
+        for (int j = 0; j < nx; j++) {
+            andm[0] &= xs[j];
+            orm[0] |= xs[j];
+        }
+        const int hb = top_bit_or_none((andm[0] ^ orm[0]) & nm);
+        int hb2[2] = {-1, -1};
         if (hb >= 0) {
-            andm[1] = andm[2] = ~0ull;
-            orm[1] = orm[2] = 0;
             for (int j = 0; j < nx; j++) {
-                const int g = (int)((xs[j] >> hb) & 1ull);
-                andm[1 + g] &= xs[j];
-                orm[1 + g] |= xs[j];
+                const int h = (int)((xs[j] >> hb) & 1ull);
+                andm[1 + h] &= xs[j];
+                orm[1 + h] |= xs[j];
+            }
+            for (int h = 0; h < 2; h++) hb2[h] = top_bit_or_none((andm[1 + h] ^ orm[1 + h]) & nm);
+            for (int j = 0; j < nx; j++) {
+                const int h = (int)((xs[j] >> hb) & 1ull);
+                if (hb2[h] < 0) continue;
+                const int q = (int)((xs[j] >> hb2[h]) & 1ull);
+                andm[3 + 2 * h + q] &= xs[j];
+                orm[3 + 2 * h + q] |= xs[j];
             }
         }
         struct {
             uint64_t pJ[64], pGT[64], h, D1, D2, done;
-            int k, Q, ok;
-        } st[2];
-        for (int g = 0; g < (hb >= 0 ? 2 : 1); g++) {
+            int k, Q, ok, used;
+        } st[kGroups];
+        for (int g = 0; g < kGroups; g++) {
+            int slot = -1;
+            if (hb < 0) slot = g == 0 ? 0 : -1;
+            else if (hb2[g / 2] < 0) slot = (g & 1) ? -1 : 1 + g / 2;
+            else slot = 3 + g;
+            st[g].used = slot >= 0;
+            if (slot < 0) continue;
             for (int c = 0; c < 64; c++) {
                 uint64_t col = 0;
                 if (c < th.n)
@@ -79,17 +98,17 @@ extern "C" int tp_host_block(const csim_state* theta, int ntheta, const uint64_t
             st[g].h = th.h;
             st[g].D1 = th.D1;
             st[g].D2 = th.D2;
-            const uint64_t am = hb >= 0 ? andm[1 + g] : andm[0], om = hb >= 0 ? orm[1 + g] : orm[0];
-            const uint64_t pm = agree_top(am ^ om, th.n);
+            const uint64_t pm = agree_top(andm[slot] ^ orm[slot], th.n);
             st[g].done = pm;
             st[g].ok = 1;
-            if (hd_popc64(~am & pm & nm) > 0)
-                st[g].ok = prefix_shrink(true, th.n, pm, am, st[g].k, st[g].Q, st[g].h, st[g].D1, st[g].D2, st[g].pJ,
-                                         st[g].pGT, mem);
+            if (hd_popc64(~andm[slot] & pm & nm) > 0)
+                st[g].ok = prefix_shrink(true, th.n, pm, andm[slot], st[g].k, st[g].Q, st[g].h, st[g].D1, st[g].D2,
+                                         st[g].pJ, st[g].pGT, mem);
         }
         for (int j = 0; j < nx; j++) {
             const int w = a * nx + j;
-            const auto& s = st[hb >= 0 ? (int)((xs[j] >> hb) & 1ull) : 0];
+            const auto& s = st[block_group(hb, hb2[0], hb2[1], xs[j])];
+            if (!s.used) return -1;
             eps[w] = p[w] = m[w] = 0;
             if (s.ok)
                 pair_l(true, th.n, s.k, s.Q, s.h, s.D1, s.D2, s.pJ, s.pGT, xs[j], mem, eps[w], p[w], m[w], err, 64,

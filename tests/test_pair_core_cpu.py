@@ -14,7 +14,8 @@ from helpers import phase_m, rand_word, random_projector_rows
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "native", "tp_host_check.cpp")
 SO = os.path.join(HERE, "native", "_build", "libtphost.so")
-CORE = os.path.join(os.path.dirname(HERE), "circuitsimulator_gb300", "csrc", "csim_pair_core.cuh")
+CORES = [os.path.join(os.path.dirname(HERE), "circuitsimulator_gb300", "csrc", f)
+         for f in ("csim_pair_core.cuh", "csim_block_prefix.cuh")]
 
 
 @pytest.fixture(scope="module", params=["32", "0"], ids=["wide_above_32", "always_wide"])
@@ -23,7 +24,7 @@ def tp(request):
     for every k, as a lane with a small k does in a warp that holds a larger one."""
     so = SO.replace(".so", "_w%s.so" % request.param)
     os.makedirs(os.path.dirname(so), exist_ok=True)
-    if not os.path.exists(so) or os.path.getmtime(so) < max(os.path.getmtime(SRC), os.path.getmtime(CORE)):
+    if not os.path.exists(so) or os.path.getmtime(so) < max(os.path.getmtime(f) for f in [SRC] + CORES):
         subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-DCSIM_TP_WIDE_FROM=" + request.param,
                                SRC, "-o", so])
     lib = C.CDLL(so)
@@ -118,12 +119,13 @@ def test_pair_core_golden(tp, golden_seeded):
 @pytest.mark.parametrize("t,k,d", [(3, 2, 1), (6, 3, 2), (12, 5, 4), (24, 6, 8), (33, 6, 10), (40, 8, 7),
                                    (40, 8, 16), (57, 6, 20), (64, 6, 24)])
 def test_shared_prefix_vs_oracle(tp, oracle, t, k, d):
-    """The kernels' block path (two codeword groups split at the highest bit in
-    which the codewords differ; each group's shared top-bit shrinks once per
-    theta, then each pair from its group's state) against the oracle: codeword
-    sets whose top d bits agree, split by the coefficient of the one row of L
-    that has top bits (all-zero and mixed prefixes), the whole set (two groups
-    at the top bits), and a single codeword (every shrink shared)."""
+    """The kernels' block path (up to four codeword groups: halves split at the
+    highest bit in which the codewords differ, each half at its own; each
+    group's shared top-bit shrinks once per theta, then each pair from its
+    group's state) against the oracle: codeword sets whose top d bits agree,
+    split by the coefficient of the one row of L that has top bits (all-zero
+    and mixed prefixes), the whole set (groups at the top bits), and a single
+    codeword (every shrink shared)."""
     rs = np.random.RandomState(900 + t + d)
     low = (1 << (t - d)) - 1
     L = [rand_word(rs, t) & low for _ in range(k)]
