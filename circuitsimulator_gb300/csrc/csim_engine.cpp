@@ -189,7 +189,7 @@ class Engine {
         : ctx_(ctx),
           round_pairs_(round_pairs > 0 ? round_pairs : ((int64_t)1 << 26)),
           round_states_(round_states > 0 ? round_states : ((int64_t)1 << 16)),
-          per_thread_(per_thread > 0 ? per_thread : 16),
+          per_thread_(per_thread > 0 ? per_thread : 0),
           budget_(budget > 0 ? budget : ((int64_t)8 << 30)) {}
 
     ~Engine() {
@@ -542,7 +542,11 @@ int Engine::launch_round() {
     // its shared memory for that bucket's largest t, not the round's
     int64_t nbucket[kBuckets] = {0};
     int64_t niw = 0;
-    const int64_t span_tp = 64 * (int64_t)per_thread_, span_w = 64;
+    // thread-per-pair items of an evaluation: 64 * tp_per_thread(t) terms each;
+    // a launch runs as many rows per thread as its longest items need
+    auto span_tp_of = [this](int t) { return 64 * (int64_t)tp_per_thread(per_thread_, t); };
+    const int launch_pt = per_thread_ > 0 ? per_thread_ : std::max(auto_per_thread(1), auto_per_thread(64));
+    const int64_t span_w = 64;
     double hcum[CSIM_MAX_QUBITS + 1];
     int hcum_t = -1;
     for (int64_t i = 0; i < ns; i++) {
@@ -564,6 +568,7 @@ int Engine::launch_round() {
         const int64_t nj = e->chi - jb;
         if (!e->q->exact) {
             const int b = 2 * bucket_of_[e->t];
+            const int64_t span_tp = span_tp_of(e->t);
             const int64_t nall = (nj + span_tp - 1) / span_tp;
             const int64_t nlight = e->kind == 1 ? nall - light_first_item(e, span_tp) : 0;
             nbucket[b] += nall - nlight;
@@ -655,6 +660,7 @@ int Engine::launch_round() {
             // heavy items first, then light ones; a slot's items may sit in two
             // launches, so its range is kept per slot in each (see below)
             const int b = 2 * bucket_of_[e->t];
+            const int64_t span_tp = span_tp_of(e->t);
             const int64_t jl = e->kind == 1 ? light_first_item(e, span_tp) * span_tp : e->chi;
             int64_t& ch = cur[b];
             int64_t& cl = cur[b + 1];
@@ -690,7 +696,7 @@ int Engine::launch_round() {
     const csim::PairItem* ditems = (const csim::PairItem*)(db + o_items);
     for (int b = 0; b < 2 * nbuckets_; b++) {
         const int nmax = bucket_hi_[b / 2], gmax = (b & 1) ? light_zeros(nmax) : nmax;
-        if (nbucket[b] && csim::launch_items_tp(L, ditems + bstart[b], nbucket[b], dstates, dcode, per_thread_, nmax,
+        if (nbucket[b] && csim::launch_items_tp(L, ditems + bstart[b], nbucket[b], dstates, dcode, launch_pt, nmax,
                                                 gmax, part + 4 * bstart[b], partd + 4 * bstart[b]))
             return fail(ctx_, CSIM_ERR_CUDA, "pair launch failed");
     }

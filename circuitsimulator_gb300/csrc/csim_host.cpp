@@ -76,7 +76,7 @@ extern "C" int csim_set_option(csim_ctx* ctx, int32_t option, int64_t value) {
         ctx->pair_kernel = (int)value;
         return CSIM_OK;
     case CSIM_OPT_PER_THREAD:
-        if (value < 1 || value > 64) return fail(ctx, CSIM_ERR_ARG, "per-thread pairs must be 1..64");
+        if (value < 0 || value > 64) return fail(ctx, CSIM_ERR_ARG, "per-thread pairs must be 0 (by t) or 1..64");
         ctx->per_thread = (int)value;
         return CSIM_OK;
     default:
@@ -432,7 +432,8 @@ extern "C" int csim_term_products(csim_ctx* ctx, int32_t t, int32_t exact, const
         int* dm = (int*)v;
         const int rc = (!exact && ctx->pair_kernel == 0 && sym)
                            ? csim::launch_terms_tp(launch_of(ctx), t, t, dcw, (const csim::GState*)dth, nullptr, c, j0,
-                                                   nj, ctx->per_thread, 2 * t, nullptr, 0, 0, de, dp, dm)
+                                                   nj, tp_per_thread(ctx->per_thread, t), 2 * t, nullptr, 0, 0, de,
+                                                   dp, dm)
                            : csim::launch_terms(launch_of(ctx), nr, exact ? 1 : 0, dcw, (const csim::GState*)dphis,
                                                 (const csim::GState*)dth, nullptr, c, j0, nj, 64, 2 * t, nullptr,
                                                 nullptr, de, dp, dm);
@@ -466,7 +467,8 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
     const int P2 = 2 * t;
     const bool tp = !exact && ctx->pair_kernel == 0;
     const int64_t chunk = chunk_for(chi);
-    const int64_t nchunks = tp ? csim::terms_tp_blocks(chi, ctx->per_thread) : (chi + chunk - 1) / chunk;
+    const int pt = tp_per_thread(ctx->per_thread, t);
+    const int64_t nchunks = tp ? csim::terms_tp_blocks(chi, pt) : (chi + chunk - 1) / chunk;
 
     std::vector<int> hm(P->nstabs);
     for (int r = 0; r < P->nstabs; r++) hm[r] = phase_m(P->phase[r]);
@@ -538,15 +540,15 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
             int rc = 0;
             if (tp) {
                 // terms [0, jb): every zero count; terms [jb, chi): at most light_zeros(t) zeros
-                const int64_t span = 64 * (int64_t)ctx->per_thread;
+                const int64_t span = 64 * (int64_t)pt;
                 const int64_t jb = std::min(chi, (ctx->cw_split + span - 1) / span * span);
                 if (jb > 0)
-                    rc |= csim::launch_terms_tp(launch_of(ctx), t, t, dcw, sth, scode, cs, 0, jb, ctx->per_thread, P2,
-                                                spart, nchunks, 0, nullptr, nullptr, nullptr);
+                    rc |= csim::launch_terms_tp(launch_of(ctx), t, t, dcw, sth, scode, cs, 0, jb, pt, P2, spart,
+                                                nchunks, 0, nullptr, nullptr, nullptr);
                 if (jb < chi)
                     rc |= csim::launch_terms_tp(launch_of(ctx), t, light_zeros(t), dcw + jb, sth, scode, cs, jb,
-                                                chi - jb, ctx->per_thread, P2, spart, nchunks, jb / span, nullptr,
-                                                nullptr, nullptr);
+                                                chi - jb, pt, P2, spart, nchunks, jb / span, nullptr, nullptr,
+                                                nullptr);
             } else {
                 rc = csim::launch_terms(launch_of(ctx), nr, exact ? 1 : 0, dcw, (const csim::GState*)dphis, sth,
                                         scode, cs, 0, chi, (int)chunk, P2, spart, nullptr, nullptr, nullptr, nullptr);

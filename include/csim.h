@@ -122,7 +122,7 @@ int csim_rng_position(csim_ctx *ctx, uint64_t seed, uint64_t first);
 
 /* Tuning options (no counterpart in the reference). */
 #define CSIM_OPT_PAIR_KERNEL 1 /* |L>-term pairs: 0 = one thread per pair (default), 1 = one warp per pair */
-#define CSIM_OPT_PER_THREAD 2  /* |L>-term pairs per thread per work item of the thread-per-pair kernel (1..64) */
+#define CSIM_OPT_PER_THREAD 2  /* |L>-term pairs per thread per work item of the thread-per-pair kernel (1..64; 0 = by t) */
 int csim_set_option(csim_ctx *ctx, int32_t option, int64_t value);
 
 /* ----------------------------------------------- stabilizer primitives (batched) */
@@ -255,7 +255,7 @@ typedef struct csim_server csim_server;
 
 typedef struct csim_server_config {
     int32_t device;
-    int32_t per_thread;           /* terms per thread per work item (0: 16)    */
+    int32_t per_thread;           /* terms per thread per work item (0: by t)  */
     int64_t hbm_budget_bytes;     /* resident decompositions + round buffers   */
     int64_t round_pairs;          /* inner products per round (0: 2^26)        */
     int64_t round_states;         /* states per round (0: 2^16)                */
