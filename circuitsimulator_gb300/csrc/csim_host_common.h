@@ -157,7 +157,7 @@ inline int auto_per_thread(int t) { return t <= 52 ? 32 : 16; }
 inline int tp_per_thread(int fixed, int t) { return fixed > 0 ? fixed : auto_per_thread(t); }
 
 // Codeword-order parameter: the top-bit groups of ordered_codewords hold
-// about two kernel blocks (2^10 terms each at the default 16 terms per thread)
+// 2^11 terms, one or two kernel blocks (items of 2^11 or 2^10 terms)
 inline int ordered_prefix_bits(int k, int t) { return std::max(0, std::min(t, k - 11)); }
 
 // The 2^k codewords of L in the order the thread-per-pair kernel walks them in
