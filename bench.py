@@ -125,7 +125,7 @@ def dram_bytes_per_launch(states, k):
     8-byte codeword table read, the 64-byte partial sum of each (state,
     1024-term) work item written.  For the 64-state launch of
     profiles/k_terms_tp_c2_small.md this gives 0.89 MB against 1.26 MB
-    measured (662 KB read + 601 KB written); it grows with the states."""
+    measured (657 KB read + 600 KB written); it grows with the states."""
     return states * 1584 + 8 * 2 ** k + states * (2 ** k // 1024) * 64
 
 
