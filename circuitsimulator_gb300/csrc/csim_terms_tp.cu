@@ -17,6 +17,10 @@
 // column bits gathered in the same pass; the exponential sum folds each
 // monomer/dimer factor into W0/W1 as soon as that row is final
 // (stabilizer.c:372-418 never touches a finished row again).
+//
+// Before its pairs, a block runs the shrinks that each of its (up to four)
+// codeword groups shares once, on one lane per group (csim_block_prefix.cuh);
+// each pair starts from its group's state.
 #include <cuda_runtime.h>
 
 #include <cstdint>
