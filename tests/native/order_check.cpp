@@ -12,3 +12,4 @@ extern "C" int64_t order_codewords(const uint64_t* L, int k, int t, uint64_t* ou
 
 extern "C" int order_prefix_bits(int k, int t) { return csim_host::ordered_prefix_bits(k, t); }
 extern "C" int order_light_zeros(int t) { return csim_host::light_zeros(t); }
+extern "C" int order_per_thread(int fixed, int t) { return csim_host::tp_per_thread(fixed, t); }

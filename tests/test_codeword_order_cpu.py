@@ -58,3 +58,10 @@ def test_ordered_codewords(lib, t, k):
 
     for part in (got[:split], got[split:]):
         assert [key(v) for v in part] == sorted(key(v) for v in part)
+
+
+def test_items_per_thread_by_t(lib):
+    """Terms per thread per work item: 32 up to t = 52, 16 above, unless fixed
+    (CSIM_OPT_PER_THREAD).  Results never depend on it; the kernels' speed does."""
+    assert [lib.order_per_thread(0, t) for t in (1, 24, 40, 52, 53, 64)] == [32, 32, 32, 32, 16, 16]
+    assert lib.order_per_thread(8, 40) == 8 and lib.order_per_thread(16, 24) == 16
