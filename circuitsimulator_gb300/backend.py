@@ -143,6 +143,8 @@ def load_library(path=LIB_PATH):
         "csim_single_projector_samples": ([vp, vp, vp, i32, i32, i64, i32, u64, vp], C.c_int),
         "csim_multi_sampled_projector": ([vp, vp, vp, i32, i32, C.c_double, i32, i32, i32, u64, vp], C.c_int),
         "csim_exact_projector": ([vp, vp, vp, i32, i32, C.c_double, vp], C.c_int),
+        "csim_exact_projector_rows": ([vp, vp, vp, i32, i32, i64, i64, vp, vp], C.c_int),
+        "csim_median_of_means": ([vp, i32, i32, vp], C.c_int),
         "csim_decompose": ([i32, C.c_double, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp], C.c_int),
         "csim_decompose_on": ([vp, i32, C.c_double, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp], C.c_int),
         "csim_fidelity_sum": ([vp, i32, vp, i32, vp], C.c_int),
@@ -186,6 +188,21 @@ def projector(phases, xs, zs, nqubits):
                    _p(za) if len(ph) else None)
     P._keep = (ph, xa, za)
     return P
+
+
+def median_of_means(values, samples, bins):
+    """multiSampledProjector's reduction of samples x bins values in draw order
+    (libcirc/innerprod.c:17-41): bin means, then the median as the C library's
+    qsort orders them with the truncating comparator.  The same native code
+    reduces csim_multi_sampled_projector's values; needs no GPU."""
+    v = np.ascontiguousarray(np.asarray(values, dtype=np.float64).reshape(-1))
+    if len(v) != int(samples) * int(bins):
+        raise ValueError("need samples * bins values")
+    out = C.c_double(0)
+    rc = load_library().csim_median_of_means(_p(v), int(samples), int(bins), C.byref(out))
+    if rc:
+        raise CsimError(rc, "median_of_means")
+    return out.value
 
 
 class LibcRand:
@@ -358,6 +375,16 @@ class Backend:
         self._check(self.lib.csim_exact_projector(self.ctx, C.byref(P), _p(Lp), int(k), int(bool(exact)),
                                                   float(norm), C.byref(out)))
         return out.value
+
+    def exactProjectorRows(self, P, L, exact, i0, i1):
+        """Rows [i0, i1) of exactProjector as (re, im) arrays (csim_exact_projector_rows)."""
+        Lp = np.ascontiguousarray(np.asarray([int(x) for x in (L if L is not None else [])] or [0], dtype=np.uint64))
+        k = 0 if L is None else len(L)
+        n = max(0, int(i1) - int(i0))
+        re, im = np.zeros(max(n, 1)), np.zeros(max(n, 1))
+        self._check(self.lib.csim_exact_projector_rows(self.ctx, C.byref(P), _p(Lp), int(k), int(bool(exact)),
+                                                       int(i0), int(i1), _p(re), _p(im)))
+        return re[:n], im[:n]
 
     def decompose(self, t, fidbound=1e-5, rank=False, fidelity=False, forceL=False, exact=False, k=0, rng=None):
         """decompose() with the fidelity sum on this GPU (csim_decompose_on)."""

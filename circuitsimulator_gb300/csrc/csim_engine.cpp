@@ -779,18 +779,7 @@ void Engine::finish_eval(Eval* e) {
     if (e->finished) return;
     e->finished = true;
     if (e->kind == 1) {  // multiSampledProjector, innerprod.c:64-84
-        std::vector<double> binv(e->bins);
-        for (int b = 0; b < e->bins; b++) {
-            double total = 0;
-            for (int i = 0; i < e->samples; i++) total += e->val[(size_t)b * e->samples + i];
-            binv[b] = total / e->samples;
-        }
-        if (e->bins == 1) {
-            e->value = binv[0];
-        } else {
-            qsort(binv.data(), (size_t)e->bins, sizeof(double), cmp_trunc);
-            e->value = (e->bins % 2 == 1) ? binv[(e->bins - 1) / 2] : (binv[e->bins / 2] + binv[e->bins / 2 - 1]) / 2;
-        }
+        e->value = median_of_means(e->val.data(), e->samples, e->bins);
     } else {  // rows summed in row order, innerprod.c:187-198
         double tr = 0, ti = 0;
         for (int64_t s = 0; s < e->ns; s++)

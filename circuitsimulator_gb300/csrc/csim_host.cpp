@@ -628,39 +628,33 @@ extern "C" int csim_multi_sampled_projector(csim_ctx* ctx, const csim_projector*
     std::vector<double> v((size_t)samples * bins);
     CKR(sample_values(ctx, P, L, k, exact, (int64_t)samples * bins, rng, seed, v.data()));
     stats_end(ctx);
-    std::vector<double> binv(bins);
-    for (int b = 0; b < bins; b++) {
-        double total = 0;  // sequential, in draw order (innerprod.c:75-77)
-        for (int i = 0; i < samples; i++) total += v[(size_t)b * samples + i];
-        binv[b] = total / samples;
-    }
-    if (bins == 1) {
-        *out = binv[0];
-        return CSIM_OK;
-    }
-    qsort(binv.data(), (size_t)bins, sizeof(double), cmp_trunc);
-    *out = (bins % 2 == 1) ? binv[(bins - 1) / 2] : (binv[bins / 2] + binv[bins / 2 - 1]) / 2;
+    *out = median_of_means(v.data(), samples, bins);
     return CSIM_OK;
 }
 
-extern "C" int csim_exact_projector(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int32_t k,
-                                    int32_t exact, double norm, double* out) {
-    if (!ctx || !out) return fail(ctx, CSIM_ERR_ARG, "bad argument");
-    cudaSetDevice(ctx->device);
-    CKR(check_projector(ctx, P));
-    stats_begin(ctx);
-    if (P->nstabs == 0) {  // innerprod.c:150
-        *out = pow(norm, 2);
-        return CSIM_OK;
-    }
+extern "C" int csim_median_of_means(const double* values, int32_t samples, int32_t bins, double* out) {
+    if (!values || !out || samples < 1 || bins < 1) return CSIM_ERR_ARG;
+    *out = median_of_means(values, samples, bins);
+    return CSIM_OK;
+}
+
+namespace {
+
+// Rows [i0, i1) of exactProjector (innerprod.c:148-261): row i adds
+// 2^{-c_i/2} (diag_i + 2 Re off_i), where off_i = sum_{j>i} <Pi phi_i|phi_j> and
+// c_i counts the 2^{-1/2} factors of the projection.  Each row's sum is exact
+// in Z[w]; re[i - i0], im[i - i0] get the row's value in double (0 for a row
+// the projector annihilates).  *chi_out receives chi.
+int exact_rows(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int k, int exact, int64_t i0, int64_t i1,
+               double* re_out, double* im_out, int64_t* chi_out) {
     const int t = P->nqubits;
-    if (t == 0) {
-        *out = clifford_sum(P) / (1 + (double)P->nstabs);
-        return CSIM_OK;
-    }
     CKR(check_code(ctx, t, exact, L, k));
     const int64_t chi = exact ? ((int64_t)1 << ((t + 1) / 2)) : ((int64_t)1 << k);
     if (chi > ((int64_t)1 << 20)) return fail(ctx, CSIM_ERR_ARG, "chi=%lld too large for the exact projector", (long long)chi);
+    if (chi_out) *chi_out = chi;
+    if (i0 < 0 || i1 < i0 || i1 > chi) return fail(ctx, CSIM_ERR_ARG, "row range [%lld, %lld) outside [0, chi)",
+                                                  (long long)i0, (long long)i1);
+    if (i0 == i1) return CSIM_OK;
     const int nr = t > 32 ? 2 : 1;
     const int P2 = 2 * t;
     void* v;
@@ -696,6 +690,9 @@ extern "C" int csim_exact_projector(csim_ctx* ctx, const csim_projector* P, cons
     int* dcode = (int*)v;
     if (csim::launch_project(launch_of(ctx), nr, dth, chi, P->nstabs, dpm, dpz, dpx, dcode))
         return fail(ctx, CSIM_ERR_CUDA, "projection launch failed");
+    // rows outside [i0, i1) are marked annihilated, so the pair kernel skips them
+    if (i0 > 0) CK(cudaMemsetAsync(dcode, 0xff, (size_t)i0 * 4, ctx->stream));
+    if (i1 < chi) CK(cudaMemsetAsync(dcode + i1, 0xff, (size_t)(chi - i1) * 4, ctx->stream));
     const int64_t chunk = 64, nchunks = (chi + chunk - 1) / chunk;
     const size_t nparts = (size_t)chi * nchunks * 4;
     CKR(dbuf(ctx, kBufParts, nparts * sizeof(__int128), &v));
@@ -717,37 +714,76 @@ extern "C" int csim_exact_projector(csim_ctx* ctx, const csim_projector* P, cons
         csim::launch_reduce_parts(launch_of(ctx), dpartd, chi, nchunks, daccd))
         return fail(ctx, CSIM_ERR_CUDA, "reduce launch failed");
     CK(cudaEventRecord(ctx->ev[3], ctx->stream));
-    std::vector<int> code(chi);
-    std::vector<__int128> acc(chi * 4), accd(chi * 4);
-    CKR(dget(ctx, code.data(), dcode, chi));
-    CKR(dget(ctx, acc.data(), dacc, chi * 4));
-    CKR(dget(ctx, accd.data(), daccd, chi * 4));
+    const int64_t nrow = i1 - i0;
+    std::vector<int> code(nrow);
+    std::vector<__int128> acc(nrow * 4), accd(nrow * 4);
+    CKR(dget(ctx, code.data(), dcode + i0, nrow));
+    CKR(dget(ctx, acc.data(), dacc + 4 * i0, nrow * 4));
+    CKR(dget(ctx, accd.data(), daccd + 4 * i0, nrow * 4));
     CKR(finish(ctx));
     CKR(stats_batch(ctx));
-    ctx->stats.states = chi;
-    for (int64_t i = 0; i < chi; i++)
-        if (code[i] >= 0) {
-            ctx->stats.states_live++;
-            ctx->stats.pairs += chi - i;
-        }
-    stats_end(ctx);
-    // row i adds 2^{-c_i/2} (diag_i + 2 Re off_i): exact per row in Z[w],
-    // rows summed in double in row order like exactProjector's loop
-    double tr = 0, ti = 0;
-    for (int64_t i = 0; i < chi; i++) {
-        if (code[i] < 0) continue;
-        const __int128* o = &acc[4 * i];
-        const __int128* d = &accd[4 * i];
+    ctx->stats.states = nrow;
+    for (int64_t r = 0; r < nrow; r++) {
+        re_out[r] = im_out[r] = 0;
+        if (code[r] < 0) continue;
+        ctx->stats.states_live++;
+        ctx->stats.pairs += chi - (i0 + r);
+        const __int128* o = &acc[4 * r];
+        const __int128* d = &accd[4 * r];
         // 2 Re(a + b w + c w^2 + d w^3) = 2a + (b - d)(w - w^3)
         const __int128 z[4] = {d[0] + 2 * o[0], d[1] + (o[1] - o[3]), d[2], d[3] - (o[1] - o[3])};
         double re, im;
         zomega_to_complex(z, P2, &re, &im);
-        const double pf = sqrt_half_power(code[i]);
-        tr += re * pf;
-        ti += im * pf;
+        const double pf = sqrt_half_power(code[r]);
+        re_out[r] = re * pf;
+        im_out[r] = im * pf;
+    }
+    return CSIM_OK;
+}
+
+}  // namespace
+
+extern "C" int csim_exact_projector(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int32_t k,
+                                    int32_t exact, double norm, double* out) {
+    if (!ctx || !out) return fail(ctx, CSIM_ERR_ARG, "bad argument");
+    cudaSetDevice(ctx->device);
+    CKR(check_projector(ctx, P));
+    stats_begin(ctx);
+    if (P->nstabs == 0) {  // innerprod.c:150
+        *out = pow(norm, 2);
+        return CSIM_OK;
+    }
+    if (P->nqubits == 0) {
+        *out = clifford_sum(P) / (1 + (double)P->nstabs);
+        return CSIM_OK;
+    }
+    int64_t chi = 0;
+    CKR(check_code(ctx, P->nqubits, exact, L, k));
+    chi = exact ? ((int64_t)1 << ((P->nqubits + 1) / 2)) : ((int64_t)1 << k);
+    if (chi > ((int64_t)1 << 20)) return fail(ctx, CSIM_ERR_ARG, "chi=%lld too large for the exact projector", (long long)chi);
+    std::vector<double> re(chi), im(chi);
+    CKR(exact_rows(ctx, P, L, k, exact, 0, chi, re.data(), im.data(), &chi));
+    stats_end(ctx);
+    // rows summed in double in row order, like exactProjector's loop
+    double tr = 0, ti = 0;
+    for (int64_t i = 0; i < chi; i++) {
+        tr += re[i];
+        ti += im[i];
     }
     *out = sqrt(tr * tr + ti * ti);
     return CSIM_OK;
+}
+
+extern "C" int csim_exact_projector_rows(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int32_t k,
+                                         int32_t exact, int64_t i0, int64_t i1, double* re, double* im) {
+    if (!ctx || (i1 > i0 && (!re || !im))) return fail(ctx, CSIM_ERR_ARG, "bad argument");
+    cudaSetDevice(ctx->device);
+    CKR(check_projector(ctx, P));
+    if (P->nstabs == 0 || P->nqubits == 0) return fail(ctx, CSIM_ERR_ARG, "no rows: the projector has no terms");
+    stats_begin(ctx);
+    const int r = exact_rows(ctx, P, L, k, exact, i0, i1, re, im, nullptr);
+    stats_end(ctx);
+    return r;
 }
 
 // ---------------------------------------------------------------- decompose

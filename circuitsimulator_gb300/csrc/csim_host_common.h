@@ -398,4 +398,19 @@ inline int cmp_trunc(const void* a, const void* b) {  // innerprod.c:17-19
     return (int)(*(const double*)a - *(const double*)b);
 }
 
+// multiSampledProjector's reduction (innerprod.c:23-41, 75-77): the mean of
+// each bin of `samples` values in draw order, then the median of the bin
+// means as the C library's qsort orders them with the truncating comparator.
+inline double median_of_means(const double* v, int samples, int bins) {
+    std::vector<double> binv(bins);
+    for (int b = 0; b < bins; b++) {
+        double total = 0;
+        for (int i = 0; i < samples; i++) total += v[(size_t)b * samples + i];
+        binv[b] = total / samples;
+    }
+    if (bins == 1) return binv[0];
+    qsort(binv.data(), (size_t)bins, sizeof(double), cmp_trunc);
+    return (bins % 2 == 1) ? binv[(bins - 1) / 2] : (binv[bins / 2] + binv[bins / 2 - 1]) / 2;
+}
+
 }  // namespace csim_host

@@ -20,6 +20,7 @@
 #include <mutex>
 
 #include "../../include/csim.h"
+#include "csim_host_common.h"
 #include "csim_internal.h"
 
 namespace {
@@ -63,20 +64,33 @@ int scratch_for(int device, unsigned char** out) {
     return CSIM_OK;
 }
 
-double logeta_s(int d, int n) {  // stabilizer.c:677-687
-    if (d == 0) return 0.;
-    double product = 0;
-    for (int a = 1; a <= d; a++) {
-        product += log2(1 - pow(2, d - n - a));
-        product -= log2(1 - pow(2, -a));
+// Puts the caller's current device back on every return path, so a host
+// framework that binds its threads to devices sees no change.
+struct DeviceRestore {
+    int prev = -1;
+    DeviceRestore() {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
     }
-    return (-d * (d + 1) / 2) + product;
-}
+    ~DeviceRestore() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+int run_static(int32_t device, const csim_projector* P, const uint64_t* L, int32_t k, int64_t count, uint64_t seed,
+               double* values);
 
 }  // namespace
 
 extern "C" int csim_single_projector_samples_static(int32_t device, const csim_projector* P, const uint64_t* L,
                                                     int32_t k, int64_t count, uint64_t seed, double* values) {
+    DeviceRestore keep;
+    return run_static(device, P, L, k, count, seed, values);
+}
+
+namespace {
+
+int run_static(int32_t device, const csim_projector* P, const uint64_t* L, int32_t k, int64_t count, uint64_t seed,
+               double* values) {
     if (!P || !values || (k > 0 && !L)) return CSIM_ERR_ARG;
     const int t = P->nqubits, nstabs = P->nstabs;
     if (count < 1 || count > CSIM_STATIC_MAX_STATES || t < 1 || t > CSIM_MAX_QUBITS || k < 0 ||
@@ -99,18 +113,9 @@ extern "C" int csim_single_projector_samples_static(int32_t device, const csim_p
 
     // small inputs: projector, cumulative d-distribution, code rows
     int32_t pm[64];
-    for (int r = 0; r < nstabs; r++) pm[r] = 2 * (((P->phase[r] / 2) % 2) & 1) + ((P->phase[r] % 2) & 1);
-    double cum[CSIM_MAX_QUBITS + 1], dist[CSIM_MAX_QUBITS + 1], sum = 0;
-    for (int d = 0; d <= t; d++) {
-        dist[d] = pow(2, logeta_s(d, t));
-        sum += dist[d];
-    }
-    for (int d = 0; d <= t; d++) dist[d] /= sum;
-    for (int i = 0; i <= t; i++) {
-        cum[i] = 0;
-        for (int d = 0; d <= i; d++) cum[i] += dist[d];
-    }
-    for (int i = 0; i <= t; i++) cum[i] /= cum[t];
+    for (int r = 0; r < nstabs; r++) pm[r] = csim_host::phase_m(P->phase[r]);
+    double cum[CSIM_MAX_QUBITS + 1];
+    csim_host::cum_table(t, cum);  // the allocating sampler's table
     uint64_t Lrows[64] = {0};
     for (int r = 0; r < k; r++) Lrows[r] = L[r];
 
@@ -155,20 +160,21 @@ extern "C" int csim_single_projector_samples_static(int32_t device, const csim_p
     if (!ok) return CSIM_ERR_CUDA;
     if (herr) return CSIM_ERR_DEVICE;
 
-    // singleProjectorSample's value per state (innerprod.c:142): 2^t |projfactor * sum|^2
-    const double s2 = 0.70710678118654752440, scale = pow(2, t), r2 = pow(2, -0.5);
+    // singleProjectorSample's value per state (innerprod.c:142): 2^t |projfactor * sum|^2,
+    // with the allocating sampler's conversions
+    const double scale = pow(2, t);
     for (int64_t i = 0; i < count; i++) {
         if (hcode[i] < 0) {
             values[i] = 0;
             continue;
         }
-        const __int128* z = &hacc[4 * i];
-        const double re = std::ldexp((double)z[0] + (double)(z[1] - z[3]) * s2, -t);
-        const double im = std::ldexp((double)z[2] + (double)(z[1] + z[3]) * s2, -t);
-        double pf = 1;
-        for (int c = 0; c < hcode[i]; c++) pf *= r2;
+        double re, im;
+        csim_host::zomega_to_complex(&hacc[4 * i], 2 * t, &re, &im);
+        const double pf = csim_host::sqrt_half_power(hcode[i]);
         const double a = re * pf, b = im * pf;
         values[i] = scale * (a * a + b * b);
     }
     return CSIM_OK;
 }
+
+}  // namespace

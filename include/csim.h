@@ -196,10 +196,27 @@ int csim_multi_sampled_projector(csim_ctx *ctx, const csim_projector *P, const u
                                  int32_t exact, double norm, int32_t samples, int32_t bins, int32_t rng,
                                  uint64_t seed, double *out);
 
+/* The reduction of csim_multi_sampled_projector on `bins` x `samples` values in
+ * draw order: per-bin means, then their median as the C library's qsort orders
+ * them with the reference's truncating comparator (libcirc/innerprod.c:17-41).
+ * Host only; lets ranks that each drew a block of states reduce exactly as one
+ * process does. */
+int csim_median_of_means(const double *values, int32_t samples, int32_t bins, double *out);
+
 /* |sum_{i<=j} (2 - delta_ij) <Pi phi_i | phi_j>| over all chi(chi+1)/2 pairs.
  * Replaces exactProjector, libcirc/innerprod.c:148-261. */
 int csim_exact_projector(csim_ctx *ctx, const csim_projector *P, const uint64_t *L, int32_t k,
                          int32_t exact, double norm, double *out);
+
+/* Rows i0 <= i < i1 of csim_exact_projector: re[i - i0] + i im[i - i0] is row
+ * i's contribution, (diag_i + 2 Re sum_{j>i} <Pi phi_i|phi_j>) times the row's
+ * projection factor (0 for a row the projector annihilates).  The value of
+ * csim_exact_projector is |sum of all chi rows|, summed in row order; ranks that
+ * each take a range of rows and send them to one rank reproduce it bit for bit.
+ * Splits the l-range of exactProjector's MPI loop (libcirc/innerprod.c:169-195)
+ * by rows.  Needs nstabs >= 1 and t >= 1. */
+int csim_exact_projector_rows(csim_ctx *ctx, const csim_projector *P, const uint64_t *L, int32_t k,
+                              int32_t exact, int64_t i0, int64_t i1, double *re, double *im);
 
 /* ------------------------------------------------------------- many queries */
 
@@ -297,7 +314,8 @@ void csim_server_destroy(csim_server *s);
  * up (cudaGetSymbolAddress), so make that first call before any stream
  * capture.  Calls share the array: calls that overlap on the GPU (from two
  * threads, or two processes' streams on one device) race and must be
- * serialized by the caller.  Runs on the legacy default stream of `device`.
+ * serialized by the caller.  Runs on the legacy default stream of `device`;
+ * the calling thread's current device is the same after the call as before.
  * No counterpart in the reference. */
 #define CSIM_STATIC_MAX_STATES 256
 #define CSIM_STATIC_MAX_K 16

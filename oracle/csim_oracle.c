@@ -873,6 +873,77 @@ void orc_term_products(int t, int exact, const uint64_t *L, int k, int64_t nthet
     for (int i = 0; i < threads; i++) pthread_join(th[i], NULL);
 }
 
+/* multiSampledProjector (innerprod.c:23-84) with the pair work on host
+ * threads.  States are drawn and projected one after another, consuming rand()
+ * exactly as orc_single_projector_sample does (the term loop draws nothing);
+ * the (eps, p, m) of every pair come from the threaded grid; then each state's
+ * terms are added in term order with the same double arithmetic.  So the value
+ * is orc_multi_sampled_projector's, bit for bit.  values[i] (if not NULL)
+ * receives state i's singleProjectorSample value. */
+double orc_multi_sampled_projector_mt(const csim_projector *P, const uint64_t *L, int k, int exact, double norm,
+                                      int samples, int bins, orc_rng *r, int threads, double *values) {
+    if (P->nstabs == 0 || P->nqubits == 0) {
+        if (values) memset(values, 0, sizeof(double) * (size_t)samples * (size_t)bins);
+        return orc_multi_sampled_projector(P, L, k, exact, norm, samples, bins, r);
+    }
+    const int t = P->nqubits;
+    const int64_t total = (int64_t)samples * bins;
+    const int64_t size = exact ? (int64_t)pow(2, ceil((double)t / 2)) : (int64_t)pow(2, k);
+    double *val = (double *)malloc(sizeof(double) * (size_t)(total > 0 ? total : 1));
+    /* states in groups of at most 2^24 pairs */
+    int64_t group = ((int64_t)1 << 24) / size;
+    if (group < 1) group = 1;
+    csim_state *th = (csim_state *)malloc(sizeof(csim_state) * (size_t)group);
+    double *pf = (double *)malloc(sizeof(double) * (size_t)group);
+    int64_t *live = (int64_t *)malloc(sizeof(int64_t) * (size_t)group);
+    csim_state *lth = (csim_state *)malloc(sizeof(csim_state) * (size_t)group);
+    int32_t *eps = (int32_t *)malloc(sizeof(int32_t) * (size_t)(group * size));
+    int32_t *pp = (int32_t *)malloc(sizeof(int32_t) * (size_t)(group * size));
+    int32_t *mm = (int32_t *)malloc(sizeof(int32_t) * (size_t)(group * size));
+    for (int64_t o = 0; o < total; o += group) {
+        const int64_t c = total - o < group ? total - o : group;
+        int64_t nl = 0;
+        for (int64_t i = 0; i < c; i++) {
+            orc_random_state(t, r, &th[i]);
+            pf[i] = orc_project(&th[i], P);
+            if (pf[i] != 0) {
+                live[nl] = i;
+                lth[nl++] = th[i];
+            }
+            val[o + i] = 0;
+        }
+        if (nl) orc_term_products(t, exact, L, k, nl, lth, 0, size, eps, pp, mm, threads);
+        for (int64_t a = 0; a < nl; a++) {
+            double tr = 0, ti = 0;
+            for (int64_t j = 0; j < size; j++) add_w(&tr, &ti, eps[a * size + j], pp[a * size + j], mm[a * size + j]);
+            const double x = tr * pf[live[a]], y = ti * pf[live[a]];
+            val[o + live[a]] = pow(2, t) * (x * x + y * y);
+        }
+    }
+    free(th);
+    free(pf);
+    free(live);
+    free(lth);
+    free(eps);
+    free(pp);
+    free(mm);
+    double *bv = (double *)malloc(sizeof(double) * (size_t)bins);
+    for (int b = 0; b < bins; b++) {
+        double tot = 0;
+        for (int i = 0; i < samples; i++) tot += val[(int64_t)b * samples + i];
+        bv[b] = tot / samples;
+    }
+    double out = bv[0];
+    if (bins > 1) {
+        qsort(bv, (size_t)bins, sizeof(double), cmp_trunc);
+        out = (bins % 2 == 1) ? bv[(bins - 1) / 2] : (bv[bins / 2] + bv[bins / 2 - 1]) / 2;
+    }
+    if (values) memcpy(values, val, sizeof(double) * (size_t)total);
+    free(bv);
+    free(val);
+    return out;
+}
+
 /* ======================================================================
  * Elementary-update restatement of one (theta, prepL term) pair, with a
  * count of packed row operations (the roofline's work unit).

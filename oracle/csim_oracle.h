@@ -70,6 +70,12 @@ double orc_project(csim_state *s, const csim_projector *P);
 void orc_term_products(int t, int exact, const uint64_t *L, int k, int64_t ntheta, const csim_state *theta,
                        int64_t j0, int64_t nj, int32_t *eps, int32_t *p, int32_t *m, int threads);
 
+/* orc_multi_sampled_projector with the pairs on `threads` host threads; same
+ * draws, same term order, same value bit for bit.  values[i] (NULL allowed)
+ * receives each state's singleProjectorSample value. */
+double orc_multi_sampled_projector_mt(const csim_projector *P, const uint64_t *L, int k, int exact, double norm,
+                                      int samples, int bins, orc_rng *r, int threads, double *values);
+
 /* One (theta, term-of-|L>) pair by elementary rank-one updates, with the number
  * of packed 64-bit row operations it takes (the roofline's work unit).  Same
  * (eps, p, m) as orc_inner_product_exact with the prepL term of codeword x. */

@@ -1,10 +1,14 @@
 """Generates the benchmark workloads and end-to-end golden outputs.
 
-Run here, where the reference checkout exists (its Python front end compiles
-the circuits; its C backend, built by ``make -C oracle ref``, gives the
-reference outputs):
+Run where the reference checkout exists (its Python front end compiles the
+circuits; its C backend, built by ``make -C oracle ref REF=<checkout>``, gives
+the reference outputs):
 
-    python tests/golden/make_workloads.py [REFERENCE_ROOT]
+    python tests/golden/make_workloads.py REFERENCE_ROOT [--c1-golden-only]
+
+(or set CSIM_REFERENCE instead of passing REFERENCE_ROOT).  With
+--c1-golden-only the committed workloads are kept and only workload_c1_ref.json
+is recorded.
 
 Outputs (committed):
   workload_c1.txt  stdin-protocol input of the c1 configuration: seeded random
@@ -13,6 +17,9 @@ Outputs (committed):
                    0..2; exact decomposition (chi = 2^6), L = 2000, forceSample.
   workload_c2.txt  c2: n=24, t=40, 8 measured qubits; k=16 code (fidelity bound
                    0.01), L = 4096.
+  workload_c1_ref.json  the reference backend's output lines on workload_c1.txt
+                   for fixed seeds (CSIM_REF_SEED): the whole c1 query, 2000
+                   states per projector.
   e2e_cases.json.gz  small protocol inputs with the reference backend's output
                    lines for fixed seeds (CSIM_REF_SEED), used by the
                    end-to-end tests of gpubackend.
@@ -31,41 +38,14 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REFROOT = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+_ARGS = [a for a in sys.argv[1:] if not a.startswith("--")]
+REFROOT = _ARGS[0] if _ARGS else os.environ.get("CSIM_REFERENCE", "")
+if not REFROOT or not os.path.isdir(os.path.join(REFROOT, "libcirc")):
+    sys.exit("usage: make_workloads.py REFERENCE_ROOT (the reference checkout; or set CSIM_REFERENCE)")
 REFBACKEND = os.path.join(ROOT, "oracle", "_ref", "refbackend")
+sys.path.insert(0, HERE)
+from circuits import random_circuit  # noqa: E402
 sys.path.insert(0, REFROOT)
-
-
-def gate_line(n, ops):
-    """One circuit line: ops = {qubit: symbol}, '_' elsewhere."""
-    return "".join(ops.get(q, "_") for q in range(n))
-
-
-def random_circuit(n, t_target, rs):
-    lines = ["main:"]
-    t = 0
-    gates = 0
-    while t < t_target:
-        r = rs.random_sample()
-        if r < 0.55:
-            g = ["H", "S", "X", "Z"][rs.randint(4)]
-            q = rs.randint(n)
-            if g == "Z":  # Z = H X H
-                lines += [gate_line(n, {q: "H"}), gate_line(n, {q: "X"}), gate_line(n, {q: "H"})]
-            else:
-                lines.append(gate_line(n, {q: g}))
-        elif r < 0.85:
-            a, b = rs.choice(n, size=2, replace=False)
-            lines.append(gate_line(n, {int(a): "C", int(b): "X"}))
-        else:
-            q = rs.randint(n)
-            if rs.randint(2):
-                lines.append(gate_line(n, {q: "T"}))
-            else:  # T^dagger = S S S T
-                lines += [gate_line(n, {q: "S"})] * 3 + [gate_line(n, {q: "T"})]
-            t += 1
-        gates += 1
-    return "\n".join(lines) + "\n", gates
 
 
 def protocol_input(circ, measure, config, seed):
@@ -157,7 +137,27 @@ def e2e_cases():
     print("e2e cases:", len(cases))
 
 
+C1_SEEDS = (1, 4242)
+
+
+def c1_golden():
+    """The reference backend on the committed c1 workload, in full (exact
+    decomposition chi = 2^6, 2000 states per projector, forceSample), for
+    fixed seeds."""
+    text = open(os.path.join(HERE, "workload_c1.txt")).read()
+    out = []
+    for seed in C1_SEEDS:
+        lines = run_ref(text, seed)
+        out.append({"seed": seed, "ref": lines})
+        print("c1 seed", seed, lines[-2:])
+    with open(os.path.join(HERE, "workload_c1_ref.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
 def main():
+    if "--c1-golden-only" in sys.argv:
+        c1_golden()
+        return
     metas = {}
     metas["c1"] = make_workload("workload_c1.txt", 10, 12, 3,
                                 {"exact": True, "samples": 2000, "bins": 1, "forceSample": True}, 100)
@@ -166,6 +166,7 @@ def main():
     with open(os.path.join(HERE, "workloads.json"), "w") as f:
         json.dump(metas, f, indent=1)
     e2e_cases()
+    c1_golden()
 
 
 if __name__ == "__main__":

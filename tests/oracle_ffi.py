@@ -93,6 +93,10 @@ class Oracle:
         lib.orc_multi_sampled_projector.argtypes = [C.POINTER(Projector), C.c_void_p, C.c_int, C.c_int,
                                                     C.c_double, C.c_int, C.c_int, C.POINTER(RngState)]
         lib.orc_multi_sampled_projector.restype = C.c_double
+        lib.orc_multi_sampled_projector_mt.argtypes = [C.POINTER(Projector), C.c_void_p, C.c_int, C.c_int,
+                                                       C.c_double, C.c_int, C.c_int, C.POINTER(RngState), C.c_int,
+                                                       C.c_void_p]
+        lib.orc_multi_sampled_projector_mt.restype = C.c_double
         lib.orc_exact_projector.argtypes = [C.POINTER(Projector), C.c_void_p, C.c_int, C.c_int, C.c_double]
         lib.orc_exact_projector.restype = C.c_double
         lib.orc_decompose.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, _ip, _ip,
@@ -179,6 +183,17 @@ class Oracle:
         L = np.ascontiguousarray(L if L is not None else np.zeros(1), dtype=np.uint64)
         return self.lib.orc_multi_sampled_projector(C.byref(P), _ptr(L), int(k), int(exact), float(norm),
                                                     int(samples), int(bins), C.byref(r))
+
+    def multi_sampled_projector_mt(self, P, L, k, exact, norm, samples, bins, r, threads=None):
+        """orc_multi_sampled_projector on host threads: (value, per-state values)."""
+        import os
+
+        L = np.ascontiguousarray(L if L is not None else np.zeros(1), dtype=np.uint64)
+        vals = np.zeros(max(1, int(samples) * int(bins)), dtype=np.float64)
+        v = self.lib.orc_multi_sampled_projector_mt(C.byref(P), _ptr(L), int(k), int(exact), float(norm),
+                                                    int(samples), int(bins), C.byref(r),
+                                                    int(threads or os.cpu_count() or 1), _ptr(vals))
+        return v, vals[: int(samples) * int(bins)]
 
     def exact_projector(self, P, L, k, exact, norm):
         L = np.ascontiguousarray(L if L is not None else np.zeros(1), dtype=np.uint64)

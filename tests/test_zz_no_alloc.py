@@ -33,20 +33,36 @@ def _call(f, P, L, count, seed):
     return rc, out
 
 
+def _free_device_bytes():
+    import torch
+
+    return torch.cuda.mem_get_info(0)[0]
+
+
 def test_static_scratch_matches_allocating_sampler():
+    """t = 60 draws d from the upper end of the cumulative table, which this
+    entry point shares with the allocating sampler; t = 40 and 12 are the
+    workload sizes.  Free device memory is the same before and after the calls."""
     f = _static_fn()
     gpu = backend.Backend(0)
     rs = np.random.RandomState(2718)
-    for (t, k, count, seed) in ((40, 16, 200, 77), (12, 6, 256, 5)):
+    cases = []
+    for (t, k, count, seed) in ((40, 16, 200, 77), (12, 6, 256, 5), (60, 8, 64, 31)):
         L = [rand_word(rs, t) for _ in range(k)]
         rows = random_projector_rows(rs, t, max(2, t // 5))
         P = backend.projector(rows[0], rows[1], rows[2], t)
         want = gpu.singleProjectorSample(P, L, False, count, backend.RNG_PHILOX, seed)
+        cases.append((P, L, count, seed, want))
+    for c in cases:  # warm-up: symbol lookup, and each kernel's lazy module load
+        assert _call(f, *c[:4])[0] == 0
+    free0 = _free_device_bytes()
+    for (P, L, count, seed, want) in cases:
         for _ in range(2):  # two calls in a row share the scratch array
             rc, got = _call(f, P, L, count, seed)
             assert rc == 0
             for a, b in zip(got, want):
                 assert close(a, b, 1e-12, 1e-12), (a, b)
+    assert _free_device_bytes() == free0  # the calls allocated no device memory
     gpu.close()
 
 
