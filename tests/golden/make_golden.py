@@ -33,7 +33,9 @@ from circuitsimulator_gb300.state import STATE_DTYPE, block_view  # noqa: E402
 from golden.golden_io import save, state_to_json  # noqa: E402
 from oracle_ffi import RefLib, make_projector  # noqa: E402
 
-REFROOT = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REFROOT = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CSIM_REFERENCE", "")
+if not REFROOT or not os.path.isdir(os.path.join(REFROOT, "libcirc")):
+    sys.exit("usage: make_golden.py REFERENCE_ROOT (the reference checkout; or set CSIM_REFERENCE)")
 FIX = os.path.join(REFROOT, "tests", "units", "tests-c")
 
 
