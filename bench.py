@@ -20,7 +20,10 @@ protocol file tests/golden/workload_c2.txt.
          plain one-at-a-time service, Poisson arrivals of light c3 queries
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-Under torchrun each rank draws its own states (weak scaling); rank 0 prints.
+Under torchrun one query's states are split over the ranks (strong scaling,
+circuitsimulator_gb300/shard.py): each rank draws its block of the
+counter-based stream, rank 0 gathers one double per state and reduces, so the
+numerator and denominator equal one GPU's; rank 0 prints.
 """
 import argparse
 import json
@@ -120,13 +123,21 @@ class ClockSampler:
 ROWOPS_PER_PAIR_T40 = 2576.0
 
 
-def dram_bytes_per_launch(states, k):
-    """DRAM bytes of one pair-kernel launch: the states (1584 B each) and the
-    8-byte codeword table read, the 64-byte partial sum of each (state,
-    1024-term) work item written.  For the 64-state launch of
-    profiles/k_terms_tp_c2_small.md this gives 0.89 MB against 1.26 MB
-    measured (657 KB read + 600 KB written); it grows with the states."""
-    return states * 1584 + 8 * 2 ** k + states * (2 ** k // 1024) * 64
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of the light pair-kernel
+# launch over 64 projected c2 states (profiles/k_terms_tp_c2_small.md): 657 KB
+# read (the 512 KB codeword table and the states) + 600 KB written (the work
+# items' partial sums).
+MEASURED_TRAFFIC_64_STATES = 657e3 + 600e3
+MEASURED_TRAFFIC_CODEWORDS = 8 * 2 ** 16
+
+
+def dram_bytes_per_launch(states):
+    """DRAM bytes of one pair-kernel launch over `states` states, scaled from
+    the measured 64-state capture: the codeword table once, the rest in
+    proportion to the states (the states read and the partial sums written
+    both grow with them)."""
+    per_state = (MEASURED_TRAFFIC_64_STATES - MEASURED_TRAFFIC_CODEWORDS) / 64
+    return MEASURED_TRAFFIC_CODEWORDS + per_state * states
 
 
 def alu_peak_gops(num_sms, mhz):
@@ -174,7 +185,7 @@ def cpu_baseline(cfg, projs, k, L, budget_s=15.0):
 def run_ours(args, rank, world, local_rank):
     import torch
 
-    from circuitsimulator_gb300 import backend
+    from circuitsimulator_gb300 import backend, shard
 
     torch.cuda.set_device(local_rank)
     cfg, projs, exact, k, norm, L = load_workload()
@@ -182,13 +193,28 @@ def run_ours(args, rank, world, local_rank):
     P = [backend.projector(ph, xs, zs, nq) for (ph, xs, zs, nq) in projs]
     samples, bins = (args.samples or cfg["samples"]), cfg["bins"]
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-    seed0 = 1000003 * (rank + 1)
+    seed0 = 1000003
+    result = {}
 
     def step(i, rng):
+        """One query: numerator and denominator.  Philox: the states of each
+        projector split over the ranks, values gathered and reduced on rank 0
+        (on one GPU, singleProjectorSample + the native median of means, which
+        is multiSampledProjector).  rand() draws (e2e): multiSampledProjector
+        through the C ABI; with N ranks each draws its share of the states
+        from its own stream (seed + rank)."""
         st = []
         for q in range(2):
             seed = (seed0 + 2 * i + q) & 0xFFFFFFFF
-            gpu.multiSampledProjector(P[q], L, exact, norm, samples, bins, rng, seed)
+            if rng == backend.RNG_PHILOX:
+                vals = shard.sharded_values(gpu, P[q], L, exact, samples * bins, seed, rank, world)
+                if vals is not None:
+                    result[q] = shard.median_of_means(vals, samples, bins)
+            elif world == 1:
+                gpu.multiSampledProjector(P[q], L, exact, norm, samples, bins, rng, seed)
+            else:
+                lo, hi = shard.shard_bounds(samples * bins, rank, world)
+                gpu.singleProjectorSample(P[q], L, exact, hi - lo, rng, (seed + rank) & 0xFFFFFFFF)
             st.append(gpu.last_stats().as_dict())
         return st
 
@@ -256,20 +282,24 @@ def run_ours(args, rank, world, local_rank):
     roofline = {"bound": "alu", "kernel": "k_terms_tp (theta x prepL term pairs, thread per pair)",
                 "achieved": achieved, "peak": peak, "unit": "G packed row-ops/s",
                 "frac": (achieved / peak) if achieved else None,
-                "traffic": dram_bytes_per_launch(samples, k),
+                "traffic": dram_bytes_per_launch(samples * bins / world),
+                "traffic_source": "ncu dram bytes of the 64-state light launch (profiles/k_terms_tp_c2_small.md), "
+                                  "scaled to this launch's states",
                 "work_unit": "packed row-op (one 64-bit row test/XOR/update of the elementary-update algorithm)",
                 "rowops_per_pair": per_pair,
                 "peak_source": "SMs x 4 x 32 lanes x sm_max_mhz (MEASURED_PEAKS.json holds no integer peak)",
                 "pair_kernel_share": pair_ms / dev_ms}
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "strong",
         "vs_baseline": None, "dtype": "u64 GF(2) rows; Z8 / exact int128 Z[w] sums; f64 final |.|^2",
         "data": "synthetic: seeded random Clifford+T circuit (n=24, t=40, 8 measured qubits) -> G', H' "
                 "(tests/golden/workload_c2.txt); random stabilizer states drawn per step",
         "config": {"workload": "c2: t=40, chi=2^16 (k=16 code), L=%d states x 2 projectors per step" % samples,
                    "t": cfg["t"], "k": k, "samples": samples, "bins": bins, "states_per_step": states // args.steps,
-                   "live_states_per_step": live // args.steps, "pairs_per_step": pairs // args.steps // world,
+                   "live_states_per_step": live // args.steps, "pairs_per_step": pairs // args.steps,
+                   "ranks": "the states of each projector split over %d rank(s), values gathered on rank 0" % world,
+                   "last_query": {"numerator": result.get(0), "denominator": result.get(1)},
                    "l2": "flushed between steps (256 MiB write); hot data (codewords 512 KiB) is L2-resident",
                    "rng": "Philox on device (value); the C library's rand() sequence (e2e)"},
         "e2e": {"value": e2e_pairs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
