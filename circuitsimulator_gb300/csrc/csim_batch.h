@@ -40,8 +40,10 @@ int launch_draw_project(const Launch& L, const DrawDesc* desc, int64_t count, GS
 // resident blocks per SM of k_items_tp launched for states of up to nmax qubits
 // and codewords of up to gmax zeros
 int items_tp_occupancy(int nmax, int gmax);
+// queue: one device counter, zeroed by the launch (stream-ordered) and drawn from by the blocks
 int launch_items_tp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,
-                    int per_thread, int nmax, int gmax, __int128* part, __int128* part_diag);
+                    int per_thread, int nmax, int gmax, __int128* part, __int128* part_diag,
+                    unsigned long long* queue);
 int launch_items_warp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,
                       __int128* part, __int128* part_diag);
 // per-slot sums of item partials; slot s owns items [range[2s], range[2s+1]) and,

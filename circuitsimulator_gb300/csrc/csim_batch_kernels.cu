@@ -89,6 +89,7 @@ constexpr int kTPB = 64;
 struct ItemShared {
     pc::BlockPrefix bp;  // the item's state (group 0), then the states its codeword groups start from
     int n, live;
+    long long next;      // the next item taken from the work queue
     __int128 red[kTPB / 32][8];
 };
 
@@ -101,16 +102,22 @@ __device__ __forceinline__ __int128 shfl_xor_128(__int128 v, int m) {
 
 // One block per item: up to kTPB * per_thread terms of one state.  part[4w..]:
 // the item's sum; part_diag[4w..]: the term j == item.diag (exactProjector).
+// Blocks take items in table order from the work queue `queue` (a zeroed
+// counter; each block draws the next index when it finishes one), so a block
+// that drew cheap items goes on to others while a costly one runs.
 __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_t nitems, const GState* states,
                                                    const int* codes, int per_thread, int nmax, int gmax,
-                                                   __int128* part, __int128* part_diag, int* err) {
+                                                   __int128* part, __int128* part_diag,
+                                                   unsigned long long* queue, int* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ItemShared& sh = *reinterpret_cast<ItemShared*>(smem_raw);
     uint64_t* const sa = reinterpret_cast<uint64_t*>(smem_raw + sizeof(ItemShared));
     unsigned char* const pair_base = smem_raw + sizeof(ItemShared) + pc::block_state_bytes(nmax);
     const int tid = threadIdx.x;
     int e = 0;
-    for (int64_t w = blockIdx.x; w < nitems; w += gridDim.x) {
+    if (tid == 0) sh.next = (long long)atomicAdd(queue, 1ull);
+    __syncthreads();
+    for (int64_t w = sh.next; w < nitems;) {
         const PairItem it = items[w];
         __syncthreads();
         const GState* g = states + it.theta;
@@ -192,6 +199,9 @@ __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_
             if (tid < 4) part[4 * w + tid] = acc;
             else if (part_diag) part_diag[4 * w + tid - 4] = acc;
         }
+        if (tid == 0) sh.next = (long long)atomicAdd(queue, 1ull);
+        __syncthreads();
+        w = sh.next;
     }
     e = (int)__reduce_or_sync(kFull, (unsigned)e);
     if (e && (tid & 31) == 0) atomicOr(err, e);
@@ -279,9 +289,11 @@ int items_tp_occupancy(int nmax, int gmax) {
 }
 
 int launch_items_tp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,
-                    int per_thread, int nmax, int gmax, __int128* part, __int128* part_diag) {
+                    int per_thread, int nmax, int gmax, __int128* part, __int128* part_diag,
+                    unsigned long long* queue) {
     if (nitems <= 0) return 0;
-    if (nmax < 1 || nmax > 64 || gmax < 0 || gmax > nmax) return -1;
+    if (nmax < 1 || nmax > 64 || gmax < 0 || gmax > nmax || !queue) return -1;
+    if (cudaMemsetAsync(queue, 0, sizeof(unsigned long long), L.stream) != cudaSuccess) return -1;
     const size_t smem = items_tp_smem(nmax, gmax);
     if (cudaFuncSetAttribute(k_items_tp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)items_tp_smem(64, 64)) !=
         cudaSuccess)
@@ -292,7 +304,7 @@ int launch_items_tp(const Launch& L, const PairItem* items, int64_t nitems, cons
     int64_t grid = (int64_t)L.num_sms * per_sm;
     if (grid > nitems) grid = nitems;
     k_items_tp<<<(int)grid, kTPB, smem, L.stream>>>(items, nitems, states, codes, per_thread, nmax, gmax, part,
-                                                    part_diag, L.d_err);
+                                                    part_diag, queue, L.d_err);
     (*L.launches)++;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -38,6 +38,11 @@
 using namespace csim_host;
 
 namespace {
+// byte offset of the thread-per-pair launches' work-queue counter in a round's download block
+constexpr size_t kQueueOffset = 64;
+}  // namespace
+
+namespace {
 
 using Clock = std::chrono::steady_clock;
 
@@ -45,7 +50,7 @@ constexpr size_t kAlign = 256;
 inline size_t align_up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
 
 // thread-per-pair launches: one per (occupancy class of t, light or not); a
-// light launch takes codewords of at most light_zeros(t) zeros
+// light launch takes codewords of at most the light bound's zeros (tune_for)
 constexpr int kBuckets = 2 * CSIM_MAX_QUBITS;
 
 // device memory that grows on demand (contents are not kept)
@@ -103,7 +108,8 @@ struct Decomp {
     std::vector<uint64_t> L;
     uint64_t* cw = nullptr;      // codewords (exact == 0), term order
     uint64_t* cws = nullptr;     // the same in ordered_codewords' order, for sampled estimators
-    int64_t light = 0;           // first index of cws with at most light_zeros(t) zeros
+    int64_t light = 0;           // first index of cws with at most lz zeros
+    int pt = 0, lz = 0;          // thread-per-pair terms per thread and light bound (csim_host::tune_for)
     csim_state* phis = nullptr;  // term states: prepH (exact == 1), prepL (exact projector on |L>)
     uint64_t* dL = nullptr;
     size_t bytes = 0;
@@ -390,9 +396,18 @@ int Engine::ensure_decomp(QueryRec* r, bool need_phis, bool force, Decomp** out)
                 return fail(ctx_, CSIM_ERR_NOMEM, "codeword table of 2^%d terms", r->k);
             }
             d->bytes += 2 * align_up((size_t)chi * 8) + kAlign;
+            TpTune tn;
+            const csim_projector* Pw = r->q.G.nstabs > 0 ? &r->q.G : (r->q.H.nstabs > 0 ? &r->q.H : nullptr);
+            if (const int rc = tune_for(ctx_, d->t, &tn, Pw, d->L.data(), d->k)) {
+                d->release();
+                decomps_.erase(key);
+                return rc;
+            }
+            d->pt = tn.per_thread;
+            d->lz = tn.light;
             std::vector<uint64_t> ordered;
-            ordered_codewords(d->L.data(), d->k, d->t, ordered);
-            d->light = light_split(ordered, d->t);
+            ordered_codewords(d->L.data(), d->k, d->t, d->lz, ordered);
+            d->light = light_split(ordered, d->t, d->lz);
             CK(cudaMemcpy(d->cws, ordered.data(), (size_t)chi * 8, cudaMemcpyHostToDevice));
             uint64_t rows[CSIM_MAX_QUBITS] = {0};
             for (int i = 0; i < d->k; i++) rows[i] = d->L[i];
@@ -485,7 +500,7 @@ int Engine::admit(QueryRec* r, bool force, bool* admitted) {
 }
 
 // first item (of span terms, from term 0) of a sampled evaluation whose codewords all
-// have at most light_zeros(t) zeros in the ordered table
+// have at most its decomposition's light bound of zeros in the ordered table
 static int64_t light_first_item(const Eval* e, int64_t span) {
     return std::min((e->chi + span - 1) / span, (e->q->dec->light + span - 1) / span);
 }
@@ -544,8 +559,9 @@ int Engine::launch_round() {
     int64_t niw = 0;
     // thread-per-pair items of an evaluation: 64 * tp_per_thread(t) terms each;
     // a launch runs as many rows per thread as its longest items need
-    auto span_tp_of = [this](int t) { return 64 * (int64_t)tp_per_thread(per_thread_, t); };
-    const int launch_pt = per_thread_ > 0 ? per_thread_ : std::max(auto_per_thread(1), auto_per_thread(64));
+    auto span_tp_of = [this](const Eval* e) { return 64 * (int64_t)(per_thread_ > 0 ? per_thread_ : e->q->dec->pt); };
+    const int launch_pt = per_thread_ > 0 ? per_thread_ : 32;  // the largest item any t is tuned to
+    int lzmax[kBuckets] = {0};  // per light launch: the largest light bound of its items
     const int64_t span_w = 64;
     double hcum[CSIM_MAX_QUBITS + 1];
     int hcum_t = -1;
@@ -568,11 +584,12 @@ int Engine::launch_round() {
         const int64_t nj = e->chi - jb;
         if (!e->q->exact) {
             const int b = 2 * bucket_of_[e->t];
-            const int64_t span_tp = span_tp_of(e->t);
+            const int64_t span_tp = span_tp_of(e);
             const int64_t nall = (nj + span_tp - 1) / span_tp;
             const int64_t nlight = e->kind == 1 ? nall - light_first_item(e, span_tp) : 0;
             nbucket[b] += nall - nlight;
             nbucket[b + 1] += nlight;
+            if (nlight) lzmax[b + 1] = std::max(lzmax[b + 1], e->q->dec->lz);
         } else {
             niw += (nj + span_w - 1) / span_w;
         }
@@ -595,7 +612,7 @@ int Engine::launch_round() {
     const size_t w_part = align_up((size_t)ns * sizeof(csim_state));
     const size_t w_partd = align_up(w_part + (size_t)std::max<int64_t>(nitems, 1) * 64);
     const size_t work_bytes = align_up(w_partd + (size_t)std::max<int64_t>(nitems, 1) * 64);
-    // download block: err | codes | sums | sums diag
+    // download block: err (16 B), the pair launches' work-queue counter (kQueueOffset) | codes | sums | sums diag
     rs.off_codes = 256;
     rs.off_sum = align_up(rs.off_codes + (size_t)ns * 4);
     rs.off_sumd = align_up(rs.off_sum + (size_t)ns * 64);
@@ -660,7 +677,7 @@ int Engine::launch_round() {
             // heavy items first, then light ones; a slot's items may sit in two
             // launches, so its range is kept per slot in each (see below)
             const int b = 2 * bucket_of_[e->t];
-            const int64_t span_tp = span_tp_of(e->t);
+            const int64_t span_tp = span_tp_of(e);
             const int64_t jl = e->kind == 1 ? light_first_item(e, span_tp) * span_tp : e->chi;
             int64_t& ch = cur[b];
             int64_t& cl = cur[b + 1];
@@ -695,9 +712,10 @@ int Engine::launch_round() {
     CK(cudaEventRecord(rs.ev[1], ctx_->stream));
     const csim::PairItem* ditems = (const csim::PairItem*)(db + o_items);
     for (int b = 0; b < 2 * nbuckets_; b++) {
-        const int nmax = bucket_hi_[b / 2], gmax = (b & 1) ? light_zeros(nmax) : nmax;
+        const int nmax = bucket_hi_[b / 2], gmax = (b & 1) ? std::min(nmax, lzmax[b]) : nmax;
         if (nbucket[b] && csim::launch_items_tp(L, ditems + bstart[b], nbucket[b], dstates, dcode, launch_pt, nmax,
-                                                gmax, part + 4 * bstart[b], partd + 4 * bstart[b]))
+                                                gmax, part + 4 * bstart[b], partd + 4 * bstart[b],
+                                                (unsigned long long*)(dd + kQueueOffset)))
             return fail(ctx_, CSIM_ERR_CUDA, "pair launch failed");
     }
     if (csim::launch_items_warp(L, ditems + nitp, niw, dstates, dcode, part + 4 * nitp, partd + 4 * nitp))

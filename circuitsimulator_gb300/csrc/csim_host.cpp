@@ -10,6 +10,8 @@
 // All stabilizer algebra runs in the kernels; the host prepares inputs,
 // converts the kernels' exact Z[w] sums to doubles and does the per-query
 // reductions.
+#include <mutex>
+
 #include "csim_host_common.h"
 
 using namespace csim_host;
@@ -78,6 +80,10 @@ extern "C" int csim_set_option(csim_ctx* ctx, int32_t option, int64_t value) {
     case CSIM_OPT_PER_THREAD:
         if (value < 0 || value > 64) return fail(ctx, CSIM_ERR_ARG, "per-thread pairs must be 0 (by t) or 1..64");
         ctx->per_thread = (int)value;
+        return CSIM_OK;
+    case CSIM_OPT_AUTOTUNE:
+        if (value != 0 && value != 1) return fail(ctx, CSIM_ERR_ARG, "autotune must be 0 or 1");
+        ctx->autotune = (int)value;
         return CSIM_OK;
     default:
         return fail(ctx, CSIM_ERR_ARG, "unknown option %d", option);
@@ -352,21 +358,23 @@ namespace {
 // the terms |phi_j>, j in [j0, j0+nj): codewords (|L>) or prepared states (|H^t>).
 // ordered: all 2^k codewords in ordered_codewords' order (sums over all terms only)
 int stage_terms(csim_ctx* ctx, int t, int exact, const uint64_t* L, int k, int64_t j0, int64_t nj,
-                uint64_t** dcw, csim_state** dphis, bool ordered = false) {
+                uint64_t** dcw, csim_state** dphis, bool ordered = false, int lz = -1) {
     *dcw = nullptr;
     *dphis = nullptr;
     void* v;
     if (!exact && ordered && j0 == 0 && nj == ((int64_t)1 << k)) {
+        if (lz < 0) lz = light_zeros(t);
         std::vector<uint64_t> key(L, L + k);
         key.push_back((uint64_t)k);
         key.push_back((uint64_t)t);
+        key.push_back((uint64_t)lz);
         if (key != ctx->cw_key || !ctx->buf[kBufCwOrdered]) {
             std::vector<uint64_t> cw;
-            ordered_codewords(L, k, t, cw);
+            ordered_codewords(L, k, t, lz, cw);
             uint64_t* d;
             CKR(dput(ctx, kBufCwOrdered, cw.data(), cw.size(), &d));
             ctx->cw_key = key;
-            ctx->cw_split = light_split(cw, t);
+            ctx->cw_split = light_split(cw, t, lz);
         }
         *dcw = (uint64_t*)ctx->buf[kBufCwOrdered];
         return 0;
@@ -415,6 +423,8 @@ extern "C" int csim_term_products(csim_ctx* ctx, int32_t t, int32_t exact, const
                     sym = false;
                     break;
                 }
+    TpTune tn = default_tune(t);
+    if (!exact && ctx->pair_kernel == 0 && sym) CKR(tune_for(ctx, t, &tn));
     uint64_t* dcw;
     csim_state* dphis;
     CKR(stage_terms(ctx, t, exact, L, k, j0, nj, &dcw, &dphis));
@@ -432,7 +442,7 @@ extern "C" int csim_term_products(csim_ctx* ctx, int32_t t, int32_t exact, const
         int* dm = (int*)v;
         const int rc = (!exact && ctx->pair_kernel == 0 && sym)
                            ? csim::launch_terms_tp(launch_of(ctx), t, t, dcw, (const csim::GState*)dth, nullptr, c, j0,
-                                                   nj, tp_per_thread(ctx->per_thread, t), 2 * t, nullptr, 0, 0, de,
+                                                   nj, tn.per_thread, 2 * t, nullptr, 0, 0, de,
                                                    dp, dm)
                            : csim::launch_terms(launch_of(ctx), nr, exact ? 1 : 0, dcw, (const csim::GState*)dphis,
                                                 (const csim::GState*)dth, nullptr, c, j0, nj, 64, 2 * t, nullptr,
@@ -456,6 +466,9 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
     const int t = P->nqubits;
     CKR(check_code(ctx, t, exact, L, k));
     if (rng != CSIM_RNG_LIBC && rng != CSIM_RNG_PHILOX) return fail(ctx, CSIM_ERR_ARG, "unknown rng %d", rng);
+    const bool tp = !exact && ctx->pair_kernel == 0;
+    TpTune tn = default_tune(t);
+    if (tp && count > 0) CKR(tune_for(ctx, t, &tn, P, L, k));  // before any draw: tuning leaves the streams as they are
     if (rng == CSIM_RNG_LIBC && seed != CSIM_SEED_CONTINUE) ctx->lr.seed((uint32_t)seed);
     if (rng == CSIM_RNG_PHILOX && seed != CSIM_SEED_CONTINUE) {
         ctx->philox_seed = seed;
@@ -465,9 +478,8 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
     const int nr = t > 32 ? 2 : 1;
     const int64_t chi = exact ? ((int64_t)1 << ((t + 1) / 2)) : ((int64_t)1 << k);
     const int P2 = 2 * t;
-    const bool tp = !exact && ctx->pair_kernel == 0;
     const int64_t chunk = chunk_for(chi);
-    const int pt = tp_per_thread(ctx->per_thread, t);
+    const int pt = tn.per_thread;
     const int64_t nchunks = tp ? csim::terms_tp_blocks(chi, pt) : (chi + chunk - 1) / chunk;
 
     std::vector<int> hm(P->nstabs);
@@ -483,7 +495,7 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
     cum_table(t, hcum);
     uint64_t* dcw;
     csim_state* dphis;
-    CKR(stage_terms(ctx, t, exact, L, k, 0, chi, &dcw, &dphis, /*ordered=*/true));
+    CKR(stage_terms(ctx, t, exact, L, k, 0, chi, &dcw, &dphis, /*ordered=*/true, tn.light));
 
     const int64_t batch = 1 << 14;
     std::vector<uint32_t> words;
@@ -539,14 +551,14 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
             __int128* spart = dpart + (size_t)s0 * nchunks * 4;
             int rc = 0;
             if (tp) {
-                // terms [0, jb): every zero count; terms [jb, chi): at most light_zeros(t) zeros
+                // terms [0, jb): every zero count; terms [jb, chi): at most tn.light zeros
                 const int64_t span = 64 * (int64_t)pt;
                 const int64_t jb = std::min(chi, (ctx->cw_split + span - 1) / span * span);
                 if (jb > 0)
                     rc |= csim::launch_terms_tp(launch_of(ctx), t, t, dcw, sth, scode, cs, 0, jb, pt, P2, spart,
                                                 nchunks, 0, nullptr, nullptr, nullptr);
                 if (jb < chi)
-                    rc |= csim::launch_terms_tp(launch_of(ctx), t, light_zeros(t), dcw + jb, sth, scode, cs, jb,
+                    rc |= csim::launch_terms_tp(launch_of(ctx), t, tn.light, dcw + jb, sth, scode, cs, jb,
                                                 chi - jb, pt, P2, spart, nchunks, jb / span, nullptr, nullptr,
                                                 nullptr);
             } else {
@@ -590,6 +602,160 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
 
 
 }  // namespace
+
+namespace csim_host {
+
+namespace {
+
+// Tuned launch parameters per device and t, shared by every context of the
+// process (a property of the device model and the kernels, not of a context)
+struct TuneTable {
+    TpTune p[CSIM_MAX_QUBITS + 1];
+    bool done[CSIM_MAX_QUBITS + 1] = {};
+    double ms[CSIM_MAX_QUBITS + 1] = {};
+};
+std::mutex g_tune_mu;
+TuneTable g_tune[64];
+
+// One tuning pass for the t bucket [4b, 4b + 3] of t (t = 1..3 in bucket 0).
+// It runs the sampler's own path (draw, project, heavy and light pair
+// launches) on the workload about to run -- projector P and code L of k rows,
+// when given for this t -- or on a synthetic one of the bucket's largest t
+// (counter-based states projected onto ceil(0.7 t) random Pauli rows, a random
+// code of min(t, 14) rows).  The states are the tuner's own counter-based
+// draws, enough for about 2^25 pairs per trial (at least 16 waves of the
+// largest items).  Candidates: terms per thread 16 or 32 (items of 1024 or
+// 2048 pairs) and a light bound of ceil(0.5 t), ceil(0.6 t) or ceil(0.7 t)
+// zeros; after one warm-up run each is timed twice (CUDA events around the
+// pair launches) and the fastest time wins.  The caller's random streams and
+// statistics are left as they were.
+int tune_run(csim_ctx* ctx, int t, const csim_projector* Pw, const uint64_t* Lw, int kw) {
+    const int b = t / 4, lo = std::max(1, 4 * b), hi = std::min(CSIM_MAX_QUBITS, 4 * b + 3);
+    const bool own = Pw && Lw && kw > 0 && Pw->nqubits == t && Pw->nstabs > 0;
+    const int tr = own ? t : hi;
+    const csim_stats saved_stats = ctx->stats;
+    const int64_t saved_l0 = ctx->stats_launch0;
+    const uint64_t saved_ps = ctx->philox_seed, saved_pn = ctx->philox_next;
+    const LibcRand saved_lr = ctx->lr;
+    LibcRand g;
+    g.seed(0x51ed + (uint32_t)tr);
+    auto word = [&g](int n) {
+        uint64_t w = 0;
+        for (int i = 0; i < n; i++)
+            if (g.next() & 1) w |= 1ull << i;
+        return w;
+    };
+    const int nst = std::max(1, (7 * tr + 9) / 10);
+    std::vector<int32_t> ph(nst);
+    std::vector<uint64_t> xs(nst), zs(nst);
+    for (int r = 0; r < nst; r++) {
+        ph[r] = g.next() & 3;
+        xs[r] = word(tr);
+        zs[r] = word(tr);
+    }
+    const csim_projector Ps{nst, tr, ph.data(), xs.data(), zs.data()};
+    const int ks = std::min(14, tr);
+    std::vector<uint64_t> Ls(ks);
+    for (auto& w : Ls) w = word(tr);
+    const csim_projector* P = own ? Pw : &Ps;
+    const uint64_t* L = own ? Lw : Ls.data();
+    const int k = own ? kw : ks;
+    const int64_t chi = (int64_t)1 << k;
+    const int64_t count = std::max<int64_t>(128, std::min<int64_t>(4096, (((int64_t)1 << 25) + chi - 1) / chi));
+    std::vector<double> vals(count);
+    double best = 1e300;
+    int best_pt = auto_per_thread(tr), best_lf = 6;
+    int rc = 0;
+    ctx->tuning = true;
+    ctx->trial = default_tune(tr);
+    stats_begin(ctx);
+    rc = sample_values(ctx, P, L, k, 0, count, CSIM_RNG_PHILOX, 77, vals.data());  // warm-up
+    for (int pt : {16, 32}) {
+        int prev_light = -1;
+        for (int lf : {5, 6, 7}) {
+            if (rc) break;
+            ctx->trial.per_thread = pt;
+            ctx->trial.light = std::min(tr, (lf * tr + 9) / 10);
+            if (ctx->trial.light == prev_light) continue;
+            prev_light = ctx->trial.light;
+            double tmin = 1e300;
+            for (int rep = 0; rep < 2 && !rc; rep++) {
+                stats_begin(ctx);
+                rc = sample_values(ctx, P, L, k, 0, count, CSIM_RNG_PHILOX, 77, vals.data());
+                if (!rc) tmin = std::min(tmin, ctx->stats.pair_kernel_ms);
+            }
+            if (!rc && tmin < best) {
+                best = tmin;
+                best_pt = pt;
+                best_lf = lf;
+            }
+        }
+    }
+    ctx->tuning = false;
+    ctx->stats = saved_stats;
+    ctx->stats_launch0 = saved_l0;
+    ctx->philox_seed = saved_ps;
+    ctx->philox_next = saved_pn;
+    ctx->lr = saved_lr;
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    TuneTable& tt = g_tune[ctx->device & 63];
+    for (int u = lo; u <= hi; u++) {
+        if (tt.done[u]) continue;
+        tt.p[u].per_thread = best_pt;
+        tt.p[u].light = std::min(u, (best_lf * u + 9) / 10);
+        tt.done[u] = true;
+        tt.ms[u] = best;
+    }
+    return 0;
+}
+
+bool tuned_get(int device, int t, TpTune* out, double* ms) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    const TuneTable& tt = g_tune[device & 63];
+    if (!tt.done[t]) return false;
+    if (out) *out = tt.p[t];
+    if (ms) *ms = tt.ms[t];
+    return true;
+}
+
+}  // namespace
+
+int tune_for(csim_ctx* ctx, int t, TpTune* out, const csim_projector* P, const uint64_t* L, int k) {
+    if (t < 1 || t > CSIM_MAX_QUBITS) return fail(ctx, CSIM_ERR_ARG, "t=%d outside 1..64", t);
+    if (ctx->tuning) {
+        *out = ctx->trial;
+        return 0;
+    }
+    TpTune r = default_tune(t);
+    if (ctx->autotune && !tuned_get(ctx->device, t, &r, nullptr)) {
+        CKR(tune_run(ctx, t, P, L, k));
+        if (!tuned_get(ctx->device, t, &r, nullptr)) r = default_tune(t);
+    }
+    if (ctx->per_thread > 0) r.per_thread = ctx->per_thread;
+    *out = r;
+    return 0;
+}
+
+}  // namespace csim_host
+
+extern "C" int csim_autotune(csim_ctx* ctx, int32_t t, const csim_projector* P, const uint64_t* L, int32_t k,
+                             int32_t* per_thread, int32_t* light_zeros_out, double* pair_ms) {
+    if (!ctx || t < 1 || t > CSIM_MAX_QUBITS || (P && P->nqubits != t) || k < 0 || k > 30 || (k > 0 && !L))
+        return fail(ctx, CSIM_ERR_ARG, "bad argument");
+    cudaSetDevice(ctx->device);
+    TpTune tn;
+    double ms = 0;
+    if (!tuned_get(ctx->device, t, &tn, &ms)) {
+        if (P) CKR(check_projector(ctx, P));
+        CKR(tune_run(ctx, t, P, L, k));
+        if (!tuned_get(ctx->device, t, &tn, &ms)) return fail(ctx, CSIM_ERR_CUDA, "tuning left no result");
+    }
+    if (per_thread) *per_thread = tn.per_thread;
+    if (light_zeros_out) *light_zeros_out = tn.light;
+    if (pair_ms) *pair_ms = ms;
+    return CSIM_OK;
+}
 
 extern "C" int csim_single_projector_samples(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int32_t k,
                                              int32_t exact, int64_t count, int32_t rng, uint64_t seed,

@@ -156,6 +156,21 @@ inline int light_zeros(int t) { return std::min(t, (3 * t + 4) / 5); }
 inline int auto_per_thread(int t) { return t <= 52 ? 32 : 16; }
 inline int tp_per_thread(int fixed, int t) { return fixed > 0 ? fixed : auto_per_thread(t); }
 
+// Launch parameters of the thread-per-pair kernels for one t: terms per thread
+// per work item (items of 64 * per_thread terms) and the zero bound of the
+// light launch.  The defaults are the rules above; a context's autotuner
+// (csim_autotune) replaces them per t bucket with the fastest measured pair.
+struct TpTune {
+    int per_thread = 0;
+    int light = 0;
+};
+inline TpTune default_tune(int t) {
+    TpTune r;
+    r.per_thread = auto_per_thread(t);
+    r.light = light_zeros(t);
+    return r;
+}
+
 // Codeword-order parameter: the top-bit groups of ordered_codewords hold
 // 2^11 terms, one or two kernel blocks (items of 2^11 or 2^10 terms)
 inline int ordered_prefix_bits(int k, int t) { return std::max(0, std::min(t, k - 11)); }
@@ -169,7 +184,7 @@ inline int ordered_prefix_bits(int k, int t) { return std::max(0, std::min(t, k 
 // pairs of a warp mostly have the same number of shrinks, so the warp's
 // predicated loops waste few lanes.  A state's sum over all terms is exact,
 // so it does not depend on the order.
-inline void ordered_codewords(const uint64_t* L, int k, int t, std::vector<uint64_t>& out) {
+inline void ordered_codewords(const uint64_t* L, int k, int t, int lz, std::vector<uint64_t>& out) {
     const int64_t chi = (int64_t)1 << k;
     out.resize((size_t)chi);
     uint64_t x = 0;
@@ -178,7 +193,7 @@ inline void ordered_codewords(const uint64_t* L, int k, int t, std::vector<uint6
         x ^= L[k - 1 - __builtin_ctzll((unsigned long long)i)];
         out[(size_t)i] = x;
     }
-    const int wmin = t - light_zeros(t);
+    const int wmin = t - lz;
     const int d = ordered_prefix_bits(k, t);
     std::sort(out.begin(), out.end(), [wmin, d, t](uint64_t a, uint64_t b) {
         const int pa = __builtin_popcountll(a), pb = __builtin_popcountll(b);
@@ -190,14 +205,19 @@ inline void ordered_codewords(const uint64_t* L, int k, int t, std::vector<uint6
     });
 }
 
+inline void ordered_codewords(const uint64_t* L, int k, int t, std::vector<uint64_t>& out) {
+    ordered_codewords(L, k, t, light_zeros(t), out);
+}
+
 // First index of an ordered table (heavy part first) from which every codeword
-// has at most light_zeros(t) zeros.
-inline int64_t light_split(const std::vector<uint64_t>& cw, int t) {
-    const int wmin = t - light_zeros(t);
+// has at most lz zeros.
+inline int64_t light_split(const std::vector<uint64_t>& cw, int t, int lz) {
+    const int wmin = t - lz;
     int64_t j = 0;
     while (j < (int64_t)cw.size() && __builtin_popcountll(cw[(size_t)j]) < wmin) j++;
     return j;
 }
+inline int64_t light_split(const std::vector<uint64_t>& cw, int t) { return light_split(cw, t, light_zeros(t)); }
 
 // z0 + z1 w + z2 w^2 + z3 w^3 (w = e^{i pi/4}) times 2^{-P/2}, P even
 inline void zomega_to_complex(const __int128* z, int P, double* re, double* im) {
@@ -248,11 +268,25 @@ struct csim_ctx {
     int per_thread = 0;  // CSIM_OPT_PER_THREAD; 0 = auto_per_thread(t)
     cudaEvent_t ev[4] = {};
     Engine* engine = nullptr;  // created by the first batched csim_run_queries
-    std::vector<uint64_t> cw_key;  // (k, rows of L) of the ordered codeword table in kBufCwOrdered
-    int64_t cw_split = 0;          // first index of that table whose codewords have <= light_zeros(t) zeros
+    std::vector<uint64_t> cw_key;  // (k, rows of L, t, light bound) of the ordered codeword table in kBufCwOrdered
+    int64_t cw_split = 0;          // first index of that table whose codewords have <= the light bound's zeros
+    // autotuner (CSIM_OPT_AUTOTUNE): the tuned launch parameters live in a
+    // process-wide table per device (csim_host.cpp), filled a t bucket at a time
+    int autotune = 1;
+    bool tuning = false;      // a tuning pass is running on this context (its trials use `trial`)
+    csim_host::TpTune trial;  // the parameters of the trial in progress
 };
 
 namespace csim_host {
+
+// The thread-per-pair launch parameters for t on this context: a fixed
+// CSIM_OPT_PER_THREAD wins for the item size; otherwise the tuned values of
+// this device, tuning t's bucket first when the context's autotuner is on and
+// the bucket has not been tuned in this process (csim_host.cpp).  P, L, k:
+// the workload about to run, which the tuning trials then use (a synthetic
+// one when P is null).  Returns 0 or an error code.
+int tune_for(csim_ctx* ctx, int t, TpTune* out, const csim_projector* P = nullptr, const uint64_t* L = nullptr,
+             int k = 0);
 
 inline int fail(csim_ctx* ctx, int code, const char* fmt, ...) {
     char msg[512];

@@ -123,7 +123,26 @@ int csim_rng_position(csim_ctx *ctx, uint64_t seed, uint64_t first);
 /* Tuning options (no counterpart in the reference). */
 #define CSIM_OPT_PAIR_KERNEL 1 /* |L>-term pairs: 0 = one thread per pair (default), 1 = one warp per pair */
 #define CSIM_OPT_PER_THREAD 2  /* |L>-term pairs per thread per work item of the thread-per-pair kernel (1..64; 0 = by t) */
+#define CSIM_OPT_AUTOTUNE 3    /* 1 (default): tuned thread-per-pair launches, a t bucket tuned on first use; 0: fixed rules */
 int csim_set_option(csim_ctx *ctx, int32_t option, int64_t value);
+
+/* The autotuner of the thread-per-pair launches (no counterpart in the
+ * reference).  For the t bucket of t ([4b, 4b+3]) it times the sampler's own
+ * launches with each candidate -- terms per thread per work item 16 or 32
+ * (items of 1024 or 2048 pairs; 32 pairs per warp per step) and a
+ * light-launch bound of ceil(0.5 t), ceil(0.6 t) or ceil(0.7 t) zeros -- and
+ * keeps the fastest for every t of the bucket, for every context on this
+ * device in this process.  The trials run projector P and the k-row code L
+ * (the workload about to run; P->nqubits == t) on the tuner's own
+ * counter-based states, about 2^25 pairs per trial; with P null they run a
+ * synthetic workload (ceil(0.7 t) random Pauli rows, a random min(t, 14)-row
+ * code).  A bucket is tuned once; with CSIM_OPT_AUTOTUNE on (the default) the
+ * first sampler call or batched query at a new t tunes it on its own
+ * workload.  The caller's random streams and last statistics are unchanged.
+ * Returns the chosen terms per thread, light bound and the pair-kernel
+ * milliseconds of the winning trial. */
+int csim_autotune(csim_ctx *ctx, int32_t t, const csim_projector *P, const uint64_t *L, int32_t k,
+                  int32_t *per_thread, int32_t *light_zeros, double *pair_ms);
 
 /* ----------------------------------------------- stabilizer primitives (batched) */
 

@@ -199,3 +199,34 @@ def test_exact_projector_rows_compose(gpu, t, exact, k):
             for b in im:
                 ti += float(b)
         assert float(np.sqrt(tr * tr + ti * ti)) == whole, world
+
+
+# ---------------------------------------------------------------- autotuner
+def test_autotuner_leaves_results_and_streams_unchanged():
+    """A context that tunes on first use (the default) and one with the fixed
+    rules give the same values, with the reference's rand() stream continued
+    across a call that tunes a new t bucket in between; the tuned parameters
+    are among the candidates."""
+    rs = np.random.RandomState(12)
+    a, b = backend.Backend(0), backend.Backend(0)
+    try:
+        b.set_option(backend.OPT_AUTOTUNE, 0)
+        out = []
+        for g in (a, b):
+            vals = []
+            for (t, k, seed) in ((22, 9, 5), (45, 10, backend.SEED_CONTINUE), (22, 9, backend.SEED_CONTINUE)):
+                rr = np.random.RandomState(t)
+                L = [rand_word(rr, t) for _ in range(k)]
+                rows = random_projector_rows(rr, t, max(2, t // 3))
+                P = backend.projector(rows[0], rows[1], rows[2], t)
+                vals.append(g.singleProjectorSample(P, L, False, 40, backend.RNG_LIBC, seed))
+            out.append(np.concatenate(vals))
+        assert (out[0] == out[1]).all()
+        for t in (22, 45):
+            pt, lz, ms = a.autotune(t)
+            assert pt in (16, 32) and lz in {min(t, (f * t + 9) // 10) for f in (5, 6, 7)} and ms > 0, (t, pt, lz)
+        pt, lz, ms = b.autotune(60)  # explicit tuning works with the automatic one off
+        assert pt in (16, 32) and ms > 0
+    finally:
+        a.close()
+        b.close()
