@@ -404,7 +404,7 @@ int Engine::ensure_decomp(QueryRec* r, bool need_phis, bool force, Decomp** out)
                 return rc;
             }
             d->pt = tn.per_thread;
-            d->lz = tn.light;
+            d->lz = tn.kernel == 0 ? tn.light : light_zeros(d->t);  // the items kernel shares top bits per block
             std::vector<uint64_t> ordered;
             ordered_codewords(d->L.data(), d->k, d->t, d->lz, ordered);
             d->light = light_split(ordered, d->t, d->lz);

@@ -74,7 +74,7 @@ extern "C" int csim_set_option(csim_ctx* ctx, int32_t option, int64_t value) {
     if (!ctx) return CSIM_ERR_ARG;
     switch (option) {
     case CSIM_OPT_PAIR_KERNEL:
-        if (value != 0 && value != 1) return fail(ctx, CSIM_ERR_ARG, "pair kernel must be 0 or 1");
+        if (value < 0 || value > 3) return fail(ctx, CSIM_ERR_ARG, "pair kernel must be 0..3");
         ctx->pair_kernel = (int)value;
         return CSIM_OK;
     case CSIM_OPT_PER_THREAD:
@@ -357,24 +357,36 @@ namespace {
 
 // the terms |phi_j>, j in [j0, j0+nj): codewords (|L>) or prepared states (|H^t>).
 // ordered: all 2^k codewords in ordered_codewords' order (sums over all terms only)
+// ordered with tn: the table of tn's kernel -- ordered_codewords with light
+// bound tn->light (block-prefix kernel), or run_ordered_codewords with runs of
+// tn->per_thread (run kernel); ctx->cw_split is then the light launch's first term.
 int stage_terms(csim_ctx* ctx, int t, int exact, const uint64_t* L, int k, int64_t j0, int64_t nj,
-                uint64_t** dcw, csim_state** dphis, bool ordered = false, int lz = -1) {
+                uint64_t** dcw, csim_state** dphis, bool ordered = false, const TpTune* tn = nullptr) {
     *dcw = nullptr;
     *dphis = nullptr;
     void* v;
     if (!exact && ordered && j0 == 0 && nj == ((int64_t)1 << k)) {
-        if (lz < 0) lz = light_zeros(t);
+        const TpTune d0 = default_tune(t);
+        if (!tn) tn = &d0;
         std::vector<uint64_t> key(L, L + k);
         key.push_back((uint64_t)k);
         key.push_back((uint64_t)t);
-        key.push_back((uint64_t)lz);
+        key.push_back((uint64_t)tn->light);
+        key.push_back((uint64_t)tn->kernel);
+        key.push_back((uint64_t)(tn->kernel ? tn->per_thread : 0));
         if (key != ctx->cw_key || !ctx->buf[kBufCwOrdered]) {
             std::vector<uint64_t> cw;
-            ordered_codewords(L, k, t, lz, cw);
+            int64_t split;
+            if (tn->kernel == 1) {
+                split = run_ordered_codewords(L, k, t, tn->per_thread, tn->light, cw);
+            } else {
+                ordered_codewords(L, k, t, tn->light, cw);
+                split = light_split(cw, t, tn->light);
+            }
             uint64_t* d;
             CKR(dput(ctx, kBufCwOrdered, cw.data(), cw.size(), &d));
             ctx->cw_key = key;
-            ctx->cw_split = light_split(cw, t, lz);
+            ctx->cw_split = split;
         }
         *dcw = (uint64_t*)ctx->buf[kBufCwOrdered];
         return 0;
@@ -424,7 +436,7 @@ extern "C" int csim_term_products(csim_ctx* ctx, int32_t t, int32_t exact, const
                     break;
                 }
     TpTune tn = default_tune(t);
-    if (!exact && ctx->pair_kernel == 0 && sym) CKR(tune_for(ctx, t, &tn));
+    if (!exact && ctx->pair_kernel != 1 && sym) CKR(tune_for(ctx, t, &tn));
     uint64_t* dcw;
     csim_state* dphis;
     CKR(stage_terms(ctx, t, exact, L, k, j0, nj, &dcw, &dphis));
@@ -440,7 +452,7 @@ extern "C" int csim_term_products(csim_ctx* ctx, int32_t t, int32_t exact, const
         int* dp = (int*)v;
         CKR(dbuf(ctx, kBufM, c * nj * 4, &v));
         int* dm = (int*)v;
-        const int rc = (!exact && ctx->pair_kernel == 0 && sym)
+        const int rc = (!exact && ctx->pair_kernel != 1 && sym)
                            ? csim::launch_terms_tp(launch_of(ctx), t, t, dcw, (const csim::GState*)dth, nullptr, c, j0,
                                                    nj, tn.per_thread, 2 * t, nullptr, 0, 0, de,
                                                    dp, dm)
@@ -466,9 +478,11 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
     const int t = P->nqubits;
     CKR(check_code(ctx, t, exact, L, k));
     if (rng != CSIM_RNG_LIBC && rng != CSIM_RNG_PHILOX) return fail(ctx, CSIM_ERR_ARG, "unknown rng %d", rng);
-    const bool tp = !exact && ctx->pair_kernel == 0;
+    const bool tp = !exact && ctx->pair_kernel != 1;
     TpTune tn = default_tune(t);
     if (tp && count > 0) CKR(tune_for(ctx, t, &tn, P, L, k));  // before any draw: tuning leaves the streams as they are
+    // the run kernel takes whole blocks of 64 runs
+    if (tn.kernel == 1 && (exact || ((int64_t)1 << k) % (64 * (int64_t)tn.per_thread) != 0)) tn = default_tune(t);
     if (rng == CSIM_RNG_LIBC && seed != CSIM_SEED_CONTINUE) ctx->lr.seed((uint32_t)seed);
     if (rng == CSIM_RNG_PHILOX && seed != CSIM_SEED_CONTINUE) {
         ctx->philox_seed = seed;
@@ -495,7 +509,16 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
     cum_table(t, hcum);
     uint64_t* dcw;
     csim_state* dphis;
-    CKR(stage_terms(ctx, t, exact, L, k, 0, chi, &dcw, &dphis, /*ordered=*/true, tn.light));
+    CKR(stage_terms(ctx, t, exact, L, k, 0, chi, &dcw, &dphis, /*ordered=*/true, &tn));
+    unsigned char* dscr = nullptr;
+    size_t scr_bytes = 0;
+    if (tp && tn.kernel == 1) {
+        scr_bytes = csim::terms_runs_scratch_bytes(ctx->num_sms, t, std::min(t, tn.light));
+        if (!scr_bytes) return fail(ctx, CSIM_ERR_CUDA, "run kernel occupancy query failed");
+        void* sv;
+        CKR(dbuf(ctx, kBufRunScratch, scr_bytes, &sv));
+        dscr = (unsigned char*)sv;
+    }
 
     const int64_t batch = 1 << 14;
     std::vector<uint32_t> words;
@@ -550,7 +573,18 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
             first = false;
             __int128* spart = dpart + (size_t)s0 * nchunks * 4;
             int rc = 0;
-            if (tp) {
+            if (tp && tn.kernel == 1) {
+                // run kernel: terms [0, jb) in heavy runs, [jb, chi) in runs whose codewords have at most
+                // tn.light zeros below their run's agreed top bits
+                const int64_t span = 64 * (int64_t)pt;
+                const int64_t jb = ctx->cw_split;
+                if (jb > 0)
+                    rc |= csim::launch_terms_runs(launch_of(ctx), t, t, dcw, sth, scode, cs, 0, jb, pt, P2, spart,
+                                                  nchunks, 0, dscr, scr_bytes);
+                if (jb < chi)
+                    rc |= csim::launch_terms_runs(launch_of(ctx), t, std::min(t, tn.light), dcw + jb, sth, scode, cs,
+                                                  jb, chi - jb, pt, P2, spart, nchunks, jb / span, dscr, scr_bytes);
+            } else if (tp) {
                 // terms [0, jb): every zero count; terms [jb, chi): at most tn.light zeros
                 const int64_t span = 64 * (int64_t)pt;
                 const int64_t jb = std::min(chi, (ctx->cw_split + span - 1) / span * span);
@@ -664,31 +698,35 @@ int tune_run(csim_ctx* ctx, int t, const csim_projector* Pw, const uint64_t* Lw,
     const int64_t count = std::max<int64_t>(128, std::min<int64_t>(4096, (((int64_t)1 << 25) + chi - 1) / chi));
     std::vector<double> vals(count);
     double best = 1e300;
-    int best_pt = auto_per_thread(tr), best_lf = 6;
+    int best_pt = auto_per_thread(tr), best_pct = 60, best_kernel = 0;
     int rc = 0;
     ctx->tuning = true;
     ctx->trial = default_tune(tr);
     stats_begin(ctx);
     rc = sample_values(ctx, P, L, k, 0, count, CSIM_RNG_PHILOX, 77, vals.data());  // warm-up
-    for (int pt : {16, 32}) {
-        int prev_light = -1;
-        for (int lf : {5, 6, 7}) {
-            if (rc) break;
-            ctx->trial.per_thread = pt;
-            ctx->trial.light = std::min(tr, (lf * tr + 9) / 10);
-            if (ctx->trial.light == prev_light) continue;
-            prev_light = ctx->trial.light;
-            double tmin = 1e300;
-            for (int rep = 0; rep < 2 && !rc; rep++) {
-                stats_begin(ctx);
-                rc = sample_values(ctx, P, L, k, 0, count, CSIM_RNG_PHILOX, 77, vals.data());
-                if (!rc) tmin = std::min(tmin, ctx->stats.pair_kernel_ms);
-            }
-            if (!rc && tmin < best) {
-                best = tmin;
-                best_pt = pt;
-                best_lf = lf;
-            }
+    // (kernel, terms per thread, light bound in percent of t)
+    struct Cand {
+        int kernel, pt, pct;
+    };
+    static const Cand cands[] = {{0, 16, 50}, {0, 16, 60}, {0, 16, 70}, {0, 32, 50}, {0, 32, 60}, {0, 32, 70},
+                                 {1, 16, 50}, {1, 16, 55}, {1, 16, 60}, {1, 32, 50}, {1, 32, 55}, {1, 32, 60}};
+    for (const Cand& c : cands) {
+        if (rc) break;
+        if (c.kernel == 1 && chi % (64 * (int64_t)c.pt) != 0) continue;
+        ctx->trial.kernel = c.kernel;
+        ctx->trial.per_thread = c.pt;
+        ctx->trial.light = std::min(tr, (c.pct * tr + 99) / 100);
+        double tmin = 1e300;
+        for (int rep = 0; rep < 2 && !rc; rep++) {
+            stats_begin(ctx);
+            rc = sample_values(ctx, P, L, k, 0, count, CSIM_RNG_PHILOX, 77, vals.data());
+            if (!rc) tmin = std::min(tmin, ctx->stats.pair_kernel_ms);
+        }
+        if (!rc && tmin < best) {
+            best = tmin;
+            best_pt = c.pt;
+            best_pct = c.pct;
+            best_kernel = c.kernel;
         }
     }
     ctx->tuning = false;
@@ -703,7 +741,8 @@ int tune_run(csim_ctx* ctx, int t, const csim_projector* Pw, const uint64_t* Lw,
     for (int u = lo; u <= hi; u++) {
         if (tt.done[u]) continue;
         tt.p[u].per_thread = best_pt;
-        tt.p[u].light = std::min(u, (best_lf * u + 9) / 10);
+        tt.p[u].light = std::min(u, (best_pct * u + 99) / 100);
+        tt.p[u].kernel = best_kernel;
         tt.done[u] = true;
         tt.ms[u] = best;
     }
@@ -731,6 +770,14 @@ int tune_for(csim_ctx* ctx, int t, TpTune* out, const csim_projector* P, const u
     if (ctx->autotune && !tuned_get(ctx->device, t, &r, nullptr)) {
         CKR(tune_run(ctx, t, P, L, k));
         if (!tuned_get(ctx->device, t, &r, nullptr)) r = default_tune(t);
+    }
+    if (ctx->pair_kernel == 2 && r.kernel != 0) {  // the block-prefix kernel, with its own light bound
+        r.kernel = 0;
+        r.light = light_zeros(t);
+    }
+    if (ctx->pair_kernel == 3 && r.kernel != 1) {  // the run kernel, with the light bound of its runs
+        r.kernel = 1;
+        r.light = std::min(t, (11 * t + 19) / 20);
     }
     if (ctx->per_thread > 0) r.per_thread = ctx->per_thread;
     *out = r;

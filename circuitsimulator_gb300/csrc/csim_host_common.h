@@ -163,11 +163,13 @@ inline int tp_per_thread(int fixed, int t) { return fixed > 0 ? fixed : auto_per
 struct TpTune {
     int per_thread = 0;
     int light = 0;
+    int kernel = 0;  // 0: block-prefix kernel (k_terms_tp); 1: run kernel (k_terms_runs)
 };
 inline TpTune default_tune(int t) {
     TpTune r;
     r.per_thread = auto_per_thread(t);
     r.light = light_zeros(t);
+    r.kernel = 0;
     return r;
 }
 
@@ -219,6 +221,80 @@ inline int64_t light_split(const std::vector<uint64_t>& cw, int t, int lz) {
 }
 inline int64_t light_split(const std::vector<uint64_t>& cw, int t) { return light_split(cw, t, light_zeros(t)); }
 
+// Top bits of [0, n) on which codewords that differ in the bits `dis` agree
+// (csim::pc::agree_top's host twin)
+inline uint64_t agree_top_host(uint64_t dis, int n) {
+    const uint64_t nm = n >= 64 ? ~0ull : ((1ull << n) - 1);
+    const uint64_t d = dis & nm;
+    if (!d) return nm;
+    const int hb = 64 - __builtin_clzll(d);
+    return nm & ~(hb >= 64 ? ~0ull : ((1ull << hb) - 1));
+}
+
+// The 2^k codewords of L in run order, for the run kernel (k_terms_runs):
+// sorted by value, so consecutive codewords agree on long top bits, and cut
+// into runs of pt.  Each run is sorted by its codewords' zeros below the
+// run's agreed top bits (then by value); runs in which some codeword has more
+// than gl such zeros are "heavy".  Heavy runs come first, then the light ones,
+// each part ordered by the run's total zeros, so the runs of one warp have
+// about the same number of shrinks at each step.  In the table, blocks of 64
+// runs: run r of block b occupies positions b * 64 * pt + r + 64 * i.  Returns
+// the first position of the light launch (a whole number of blocks; the block
+// that holds the last heavy run goes to the heavy launch).  Needs 2^k to be a
+// multiple of 64 * pt.
+inline int64_t run_ordered_codewords(const uint64_t* L, int k, int t, int pt, int gl, std::vector<uint64_t>& out) {
+    const int64_t chi = (int64_t)1 << k;
+    std::vector<uint64_t> cw((size_t)chi);
+    uint64_t x = 0;
+    cw[0] = 0;
+    for (int64_t i = 1; i < chi; i++) {
+        x ^= L[k - 1 - __builtin_ctzll((unsigned long long)i)];
+        cw[(size_t)i] = x;
+    }
+    std::sort(cw.begin(), cw.end());
+    const uint64_t tm = t >= 64 ? ~0ull : ((1ull << t) - 1);
+    const int64_t nruns = chi / pt;
+    struct Run {
+        int64_t first;
+        int maxrem, sumrem;
+    };
+    std::vector<Run> runs((size_t)nruns);
+    for (int64_t r = 0; r < nruns; r++) {
+        uint64_t* b = &cw[(size_t)(r * pt)];
+        uint64_t am = ~0ull, om = 0ull;
+        for (int i = 0; i < pt; i++) {
+            am &= b[i];
+            om |= b[i];
+        }
+        const uint64_t low = tm & ~agree_top_host(am ^ om, t);
+        std::sort(b, b + pt, [low](uint64_t u, uint64_t v) {
+            const int ru = __builtin_popcountll(~u & low), rv = __builtin_popcountll(~v & low);
+            return ru != rv ? ru < rv : u < v;
+        });
+        int mx = 0, sm = 0;
+        for (int i = 0; i < pt; i++) {
+            const int rem = __builtin_popcountll(~b[i] & low);
+            mx = std::max(mx, rem);
+            sm += rem;
+        }
+        runs[(size_t)r] = Run{r * pt, mx, sm};
+    }
+    std::stable_sort(runs.begin(), runs.end(), [gl](const Run& u, const Run& v) {
+        const bool hu = u.maxrem > gl, hv = v.maxrem > gl;
+        if (hu != hv) return hu;
+        return u.sumrem < v.sumrem;
+    });
+    int64_t nheavy = 0;
+    while (nheavy < nruns && runs[(size_t)nheavy].maxrem > gl) nheavy++;
+    out.resize((size_t)chi);
+    for (int64_t r = 0; r < nruns; r++) {
+        const int64_t blk = r / 64, lane = r % 64;
+        for (int i = 0; i < pt; i++)
+            out[(size_t)(blk * 64 * pt + lane + 64 * i)] = cw[(size_t)(runs[(size_t)r].first + i)];
+    }
+    return (nheavy + 63) / 64 * 64 * pt;
+}
+
 // z0 + z1 w + z2 w^2 + z3 w^3 (w = e^{i pi/4}) times 2^{-P/2}, P even
 inline void zomega_to_complex(const __int128* z, int P, double* re, double* im) {
     const double s = 0.70710678118654752440;
@@ -244,7 +320,7 @@ inline double sqrt_half_power(int c) {  // projfactor of innerprod.c:104-111: c 
 enum BufId {
     kBufA, kBufB, kBufEps, kBufP, kBufM, kBufXi, kBufZeta, kBufAlpha, kBufCode, kBufWords, kBufOffsets,
     kBufCum, kBufCodewords, kBufAcc, kBufAccDiag, kBufPhis, kBufIdx, kBufConsumed, kBufPm, kBufPz, kBufPx,
-    kBufL, kBufParts, kBufPartsDiag, kBufCwOrdered, kNumBufs
+    kBufL, kBufParts, kBufPartsDiag, kBufCwOrdered, kBufRunScratch, kNumBufs
 };
 
 class Engine;                     // csim_engine.cpp: the batched query engine

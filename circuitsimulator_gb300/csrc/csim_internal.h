@@ -53,4 +53,15 @@ int launch_terms_tp(const Launch& L, int nmax, int gmax, const uint64_t* codewor
                     int64_t part_stride, int64_t part_base, int* eps_o, int* p_o, int* m_o);
 int64_t terms_tp_blocks(int64_t nj, int per_thread);
 
+// the run kernel (csim_terms_tp.cu): codewords [j0, j0 + nj) in run order
+// (csim_host::run_ordered_codewords), runs of per_thread codewords, partial
+// sums as launch_terms_tp's; gmax bounds the zeros of every codeword below its
+// run's agreed top bits.  scratch: global run memory of at least
+// terms_runs_scratch_bytes(num_sms, nmax, gmax) bytes (the grid of a launch with
+// that gmax times one block's run memory; a larger gmax gives a smaller grid).
+size_t terms_runs_scratch_bytes(int num_sms, int nmax, int gmax);
+int launch_terms_runs(const Launch& L, int nmax, int gmax, const uint64_t* codewords, const GState* theta,
+                      const int* code, int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P, __int128* part,
+                      int64_t part_stride, int64_t part_base, unsigned char* scratch, size_t scratch_bytes);
+
 }  // namespace csim

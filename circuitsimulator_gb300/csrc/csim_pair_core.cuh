@@ -105,7 +105,7 @@ struct PairMem {
 // Bytes of a block's working memory for `threads` lanes, and lane `lane`'s
 // view of it: j32 (32 rows), then j64 (rows 32..nmax-1, an even count), then
 // gmax G-column slots, each [index][thread].
-inline size_t pair_mem_bytes(int nmax, int gmax, int threads) {
+CSIM_HD inline size_t pair_mem_bytes(int nmax, int gmax, int threads) {
     const int n64 = nmax > 32 ? (((nmax + 1) & ~1) - 32) : 0;
     return (size_t)threads * (32 * 4 + (size_t)n64 * 8 + (size_t)gmax * 8);
 }
@@ -681,6 +681,34 @@ CSIM_HD inline void zacc(__int128 (&z)[4], int eps, int p, int m, int P, int& er
     }
 }
 
+// The part of a pair after its start state is in M and s: the shrinks by the
+// nz zero columns in M's slots (descending positions), then the exponential
+// sum; p is corrected by theta's own k (k0) and the weight of x, as
+// innerProductExact's p - k1 - k2 (stabilizer.c:659).  All lanes of a warp call
+// it together; `valid` = this lane has a pair.
+CSIM_HD inline void pair_finish(PairRegs& s, int nz, bool valid, const PairMem& M, uint64_t x, int k0, int& eps,
+                                int& p, int& m, int& err) {
+    eps = 0;
+    p = 0;
+    m = 0;
+    bool alive = valid;
+    const int NZ = uniform_max(nz);
+    for (int it = 0; it < NZ; it++) {
+        const bool act = alive && it < nz;
+        const bool wide = uniform_max(alive ? s.k : 0) > CSIM_TP_WIDE_FROM;
+        const int r = wide ? tp_shrink<uint64_t>(s, M, it, nz, act) : tp_shrink<uint32_t>(s, M, it, nz, act);
+        if (act && r == 0) alive = false;
+    }
+    if (uniform_max(alive ? s.k : 0) > CSIM_TP_WIDE_FROM) tp_exp_sum<uint64_t>(s, M, alive, eps, p, m, err);
+    else tp_exp_sum<uint32_t>(s, M, alive, eps, p, m, err);
+    if (alive) p -= k0 + hd_popc64(x);
+    else {
+        eps = 0;
+        p = 0;
+        m = 0;
+    }
+}
+
 // One pair: theta's J rows and G columns (as row masks), codeword x; working
 // memory M (see PairMem: 32 rows in j32, rows 32..n-1 in j64, gmax G-column
 // slots).  J must be symmetric.  `valid` = this lane has a pair (all lanes of
@@ -720,25 +748,7 @@ CSIM_HD inline void pair_l(bool valid, int n, int k1, int Q, uint64_t h, uint64_
         hz |= (uint64_t)getbit(h, c) << nz;
     }
     s.h = hz;
-    eps = 0;
-    p = 0;
-    m = 0;
-    bool alive = valid;
-    const int NZ = uniform_max(nz);
-    for (int it = 0; it < NZ; it++) {
-        const bool act = alive && it < nz;
-        const bool wide = uniform_max(alive ? s.k : 0) > CSIM_TP_WIDE_FROM;
-        const int r = wide ? tp_shrink<uint64_t>(s, M, it, nz, act) : tp_shrink<uint32_t>(s, M, it, nz, act);
-        if (act && r == 0) alive = false;
-    }
-    if (uniform_max(alive ? s.k : 0) > CSIM_TP_WIDE_FROM) tp_exp_sum<uint64_t>(s, M, alive, eps, p, m, err);
-    else tp_exp_sum<uint32_t>(s, M, alive, eps, p, m, err);
-    if (alive) p -= (k0 < 0 ? k1 : k0) + hd_popc64(x);
-    else {
-        eps = 0;
-        p = 0;
-        m = 0;
-    }
+    pair_finish(s, nz, valid, M, x, k0 < 0 ? k1 : k0, eps, p, m, err);
 }
 
 // The shrinks that every pair of theta with a codeword that agrees with x0 on
@@ -808,6 +818,120 @@ CSIM_HD inline int prefix_shrink(bool act, int n, uint64_t pm, uint64_t x0, int&
     D2 = s.D2;
     return 1;
 }
+
+// ---------------------------------------------------------------- per-thread runs
+// A thread that takes a run of codewords agreeing on the top bits pm of
+// [0, n) runs the shrinks by their common zeros in pm once (run_prefix) and
+// starts each of its pairs from that state (pair_from_run).  The state lives
+// in the thread's run memory RS: a PairMem with a G slot for every position
+// (the kernel keeps it in global memory; the host checker on the stack).
+struct RunState {
+    int k, Q, alive, npz, nlow, pad;
+    uint64_t h;  // h at the slots (bit s = slot s)
+    uint64_t D1, D2;
+    uint64_t pm;  // the run's agreed top bits, whose shrinks are done
+};
+
+#define S32(r) RS.j32[(size_t)((r) >> 2) * 4 * RS.st + ((r) & 3)]
+#define S64(r) RS.j64[(size_t)(((r) - 32) >> 1) * 2 * RS.st + (((r) - 32) & 1)]
+#define SG(c) RS.g[(size_t)(c) * RS.st]
+
+// Loads theta (J rows pJ, G columns pGT as row masks, scalars) into RS with
+// the slots laid out as prefix_shrink lays them: the zeros of x0 in pm
+// (descending), then every position below pm (descending, position c at slot
+// npz + nlow - 1 - c), and runs the shrinks by those zeros: the shrinks every
+// pair of the run starts with, in the order pair_l runs them.  Every lane of a
+// warp calls it; `act` = this lane has a run.  out.alive = 0 if a shrink
+// found the projection empty (every pair of the run is then 0).
+CSIM_HD inline void run_prefix(bool act, int n, uint64_t pm, uint64_t x0, int k, int Q, uint64_t h, uint64_t D1,
+                               uint64_t D2, const uint64_t* pJ, const uint64_t* pGT, const PairMem& RS, RunState& out) {
+    const uint64_t pz = act ? (~x0 & pm & lowmask(n)) : 0ull;
+    const int npz = hd_popc64(pz);
+    const int nlow = hd_popc64(lowmask(n) & ~pm);
+    PairRegs s;
+    s.k = k;
+    s.Q = Q;
+    s.D1 = D1;
+    s.D2 = D2;
+    int nslot = 0;
+    uint64_t hz = 0ull;
+    if (act) {
+        for (int r = 0; r < k && r < 32; r++) S32(r) = (uint32_t)pJ[r];
+        for (int r = 32; r < k; r++) S64(r) = pJ[r];
+        for (uint64_t zz = pz; zz; nslot++) {
+            const int c = 63 - hd_clz64(zz);
+            zz &= ~bit1(c);
+            SG(nslot) = pGT[c];
+            hz |= (uint64_t)getbit(h, c) << nslot;
+        }
+        for (int c = nlow - 1; c >= 0; c--, nslot++) {
+            SG(nslot) = pGT[c];
+            hz |= (uint64_t)getbit(h, c) << nslot;
+        }
+    }
+    s.h = hz;
+    bool alive = act;
+    const int NQ = uniform_max(npz);
+    for (int q = 0; q < NQ; q++) {
+        const bool a = alive && q < npz;
+        const bool wide = uniform_max(a ? s.k : 0) > CSIM_TP_WIDE_FROM;
+        const int r = wide ? tp_shrink<uint64_t>(s, RS, q, nslot, a) : tp_shrink<uint32_t>(s, RS, q, nslot, a);
+        if (a && r == 0) alive = false;
+    }
+    out.k = s.k;
+    out.Q = s.Q;
+    out.alive = alive ? 1 : 0;
+    out.npz = npz;
+    out.nlow = nlow;
+    out.pad = 0;
+    out.h = s.h;
+    out.D1 = s.D1;
+    out.D2 = s.D2;
+    out.pm = pm;
+}
+
+// One pair of a run: the run's state (rs, RS) copied into the pair's working
+// memory M -- J rows, and the G columns and h bits of x's zeros below the
+// run's prefix, in descending order -- then pair_finish.  k0: theta's own k.
+// Same (eps, p, m) as pair_l on theta.  All lanes of a warp call it together.
+CSIM_HD inline void pair_from_run(bool valid, int n, const RunState& rs, const PairMem& RS, uint64_t x,
+                                  const PairMem& M, int& eps, int& p, int& m, int& err, int gmax, int k0) {
+    const uint64_t zeros = ~x & lowmask(n) & ~rs.pm;
+    if (valid && hd_popc64(zeros) > gmax) {
+        err |= kErrRange;
+        valid = false;
+    }
+    valid = valid && rs.alive;
+    PairRegs s;
+    s.k = rs.k;
+    s.Q = rs.Q;
+    s.D1 = rs.D1;
+    s.D2 = rs.D2;
+    // J rows, whole 16-byte units: four 32-bit rows below 32, two 64-bit rows from 32 up
+    const int K = uniform_max(valid ? s.k : 0);
+    const int u32 = ((K < 32 ? K : 32) + 3) / 4, u64 = K > 32 ? (K - 32 + 1) / 2 : 0;
+    for (int u = 0; u < u32; u++)
+        if (valid && 4 * u < s.k)
+            *reinterpret_cast<U32x4*>(&R32(4 * u)) = *reinterpret_cast<const U32x4*>(&S32(4 * u));
+    for (int u = 0; u < u64; u++)
+        if (valid && 32 + 2 * u < s.k)
+            *reinterpret_cast<U64x2*>(&R64(32 + 2 * u)) = *reinterpret_cast<const U64x2*>(&S64(32 + 2 * u));
+    int nz = 0;
+    uint64_t hz = 0ull;
+    const int base = rs.npz + rs.nlow - 1;
+    for (uint64_t zz = valid ? zeros : 0ull; zz; nz++) {
+        const int c = 63 - hd_clz64(zz);
+        zz &= ~bit1(c);
+        RG(nz) = SG(base - c);
+        hz |= (uint64_t)getbit(rs.h, base - c) << nz;
+    }
+    s.h = hz;
+    pair_finish(s, nz, valid, M, x, k0, eps, p, m, err);
+}
+
+#undef S32
+#undef S64
+#undef SG
 
 // Top bits of [0, n) on which codewords that differ in the bits `dis` agree
 CSIM_HD inline uint64_t agree_top(uint64_t dis, int n) {

@@ -150,6 +150,155 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
     if (e && (tid & 31) == 0) atomicOr(err, e);
 }
 
+// ---------------------------------------------------------------- per-thread runs
+// The run kernel: codewords in runs of per_thread that agree on long top bits
+// (run order, csim_host::run_ordered_codewords).  In a block's span of
+// kTP * per_thread codewords, run r of thread t sits at positions t + kTP * i.
+// Each thread shrinks theta once by its run's common zeros in the run's
+// agreed top bits (pc::run_prefix, in its own region of the global scratch,
+// [index][thread] like the shared-memory pair memory), then starts each of its
+// pairs from that state (pc::pair_from_run).  No block-level prefix: a run of
+// 32 codewords in numeric order agrees on about 11 top bits of a 16-row code
+// at t = 40, against about 6 for a block of 2048.
+struct RunShared {
+    int n, live, k0, Q;
+    uint64_t h, D1, D2;
+    __int128 red[kTP / 32][4];
+};
+
+__global__ void __launch_bounds__(kTP) k_terms_runs(const uint64_t* codewords, const GState* theta, const int* code,
+                                                    int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P,
+                                                    int nmax, int gmax, __int128* part, int64_t part_stride,
+                                                    int64_t part_base, unsigned char* scratch, int* err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    RunShared& sh = *reinterpret_cast<RunShared*>(smem_raw);
+    uint64_t* const sJ = reinterpret_cast<uint64_t*>(smem_raw + sizeof(RunShared));  // theta's J rows, G columns
+    uint64_t* const sGT = sJ + nmax;
+    unsigned char* const pair_base = smem_raw + sizeof(RunShared) + (size_t)2 * nmax * 8;
+    const int tid = threadIdx.x;
+    int e = 0;
+    const pc::PairMem mem = pc::pair_mem(pair_base, nmax, kTP, tid);
+    const pc::PairMem rmem =
+        pc::pair_mem(scratch + (size_t)blockIdx.x * pc::pair_mem_bytes(nmax, nmax, kTP), nmax, kTP, tid);
+    const int64_t span = (int64_t)kTP * per_thread;
+    const int64_t nblk = (nj + span - 1) / span;
+    const int64_t items = ntheta * nblk;
+    for (int64_t item = blockIdx.x; item < items; item += gridDim.x) {
+        const int64_t a = item / nblk, cb = item % nblk;
+        __syncthreads();  // previous item's use of the shared state is over
+        const GState* g = theta + a;
+        if (tid == 0) {
+            sh.live = code ? (code[a] >= 0) : 1;
+            sh.n = g->n;
+            sh.k0 = g->k;
+            sh.Q = g->Q;
+            sh.h = g->h;
+            sh.D1 = g->D1;
+            sh.D2 = g->D2;
+        }
+        const int k0 = g->k;
+        if (tid < nmax) {
+            sJ[tid] = g->J[tid];
+            const int n = g->n;
+            uint64_t col = 0ull;
+            if (tid < n)
+                for (int r = 0; r < k0; r++) col |= ((g->G[r] >> tid) & 1ull) << r;
+            sGT[tid] = col;
+        }
+        __syncthreads();
+        bool asym = false;
+        if (tid < k0 && k0 <= nmax)
+            for (int r = 0; r < k0; r++) asym |= ((sJ[tid] >> r) & 1ull) != ((sJ[r] >> tid) & 1ull);
+        asym = __syncthreads_or(asym) != 0;
+        __int128 z[4] = {0, 0, 0, 0};
+        const int n = sh.n;
+        if (n > nmax || asym) e |= kErrArg;
+        if (sh.live && !asym && n >= 1 && n <= nmax) {
+            const int64_t jb = j0 + cb * span;
+            // this thread's run: positions jb + tid + kTP * i
+            uint64_t am = ~0ull, om = 0ull;
+            bool any = false;
+            for (int i = 0; i < per_thread; i++) {
+                const int64_t j = jb + tid + (int64_t)kTP * i;
+                if (j < j0 + nj) {
+                    const uint64_t x = codewords[j - j0];
+                    am &= x;
+                    om |= x;
+                    any = true;
+                }
+            }
+            const uint64_t pm = pc::agree_top(am ^ om, n);
+            pc::RunState rs;
+            pc::run_prefix(any, n, pm, am, sh.k0, sh.Q, sh.h, sh.D1, sh.D2, sJ, sGT, rmem, rs);
+            for (int i = 0; i < per_thread; i++) {
+                const int64_t j = jb + tid + (int64_t)kTP * i;
+                const bool valid = j < j0 + nj;
+                if (__all_sync(kFull, !valid)) break;  // warp-uniform exit
+                const uint64_t x = valid ? codewords[j - j0] : 0ull;
+                int eps = 0, pp = 0, mm = 0;
+                pc::pair_from_run(valid, n, rs, rmem, x, mem, eps, pp, mm, e, gmax, k0);
+                if (valid) pc::zacc(z, eps, pp, mm, P, e);
+            }
+        }
+        if (part) {
+            for (int q = 0; q < 4; q++)
+                for (int o = 16; o > 0; o >>= 1) z[q] += shfl_xor_i128(z[q], o);
+            if ((tid & 31) == 0)
+                for (int q = 0; q < 4; q++) sh.red[tid >> 5][q] = z[q];
+            __syncthreads();
+            if (tid < 4) {
+                __int128 acc = 0;
+                for (int w = 0; w < kTP / 32; w++) acc += sh.red[w][tid];
+                part[4 * (a * part_stride + part_base + cb) + tid] = acc;
+            }
+        }
+    }
+    e = (int)__reduce_or_sync(kFull, (unsigned)e);
+    if (e && (tid & 31) == 0) atomicOr(err, e);
+}
+
+namespace {
+size_t terms_runs_smem(int nmax, int gmax) {
+    return sizeof(RunShared) + (size_t)2 * nmax * 8 + pc::pair_mem_bytes(nmax, gmax, kTP);
+}
+int terms_runs_grid(const Launch& L, int nmax, int gmax, int64_t items) {
+    if (cudaFuncSetAttribute(k_terms_runs, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)terms_runs_smem(64, 64)) != cudaSuccess)
+        return -1;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_terms_runs, kTP, terms_runs_smem(nmax, gmax)) !=
+            cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    int64_t grid = (int64_t)L.num_sms * per_sm;
+    if (grid > items) grid = items;
+    return (int)grid;
+}
+}  // namespace
+
+size_t terms_runs_scratch_bytes(int num_sms, int nmax, int gmax) {
+    Launch L{nullptr, nullptr, nullptr, num_sms};
+    const int grid = terms_runs_grid(L, nmax, gmax, (int64_t)1 << 40);
+    return grid < 1 ? 0 : (size_t)grid * pc::pair_mem_bytes(nmax, nmax, kTP);
+}
+
+int launch_terms_runs(const Launch& L, int nmax, int gmax, const uint64_t* codewords, const GState* theta,
+                      const int* code, int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P, __int128* part,
+                      int64_t part_stride, int64_t part_base, unsigned char* scratch, size_t scratch_bytes) {
+    if (ntheta <= 0 || nj <= 0) return 0;
+    if (nmax < 1 || nmax > 64 || gmax < 0 || gmax > nmax || per_thread < 1 || !scratch || !part) return -1;
+    const int64_t span = (int64_t)kTP * per_thread;
+    const int64_t nblk = (nj + span - 1) / span;
+    if (part_stride < part_base + nblk) return -1;
+    const int grid = terms_runs_grid(L, nmax, gmax, ntheta * nblk);
+    if (grid < 1 || (size_t)grid * pc::pair_mem_bytes(nmax, nmax, kTP) > scratch_bytes) return -1;
+    k_terms_runs<<<grid, kTP, terms_runs_smem(nmax, gmax), L.stream>>>(codewords, theta, code, ntheta, j0, nj,
+                                                                       per_thread, P, nmax, gmax, part, part_stride,
+                                                                       part_base, scratch, L.d_err);
+    (*L.launches)++;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 size_t terms_tp_smem(int nmax, int gmax) {
     return sizeof(TPShared) + pc::block_state_bytes(nmax) + pc::pair_mem_bytes(nmax, gmax, kTP);
 }

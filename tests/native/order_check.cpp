@@ -13,3 +13,11 @@ extern "C" int64_t order_codewords(const uint64_t* L, int k, int t, uint64_t* ou
 extern "C" int order_prefix_bits(int k, int t) { return csim_host::ordered_prefix_bits(k, t); }
 extern "C" int order_light_zeros(int t) { return csim_host::light_zeros(t); }
 extern "C" int order_per_thread(int fixed, int t) { return csim_host::tp_per_thread(fixed, t); }
+
+// The run kernel's order (run_ordered_codewords); returns the light launch's first position.
+extern "C" int64_t order_runs(const uint64_t* L, int k, int t, int pt, int gl, uint64_t* out) {
+    std::vector<uint64_t> cw;
+    const int64_t split = csim_host::run_ordered_codewords(L, k, t, pt, gl, cw);
+    std::copy(cw.begin(), cw.end(), out);
+    return split;
+}

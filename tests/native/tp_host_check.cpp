@@ -117,3 +117,44 @@ extern "C" int tp_host_block(const csim_state* theta, int ntheta, const uint64_t
     }
     return err;
 }
+
+// The per-thread run path of the run kernel (run_prefix, pair_from_run):
+// xs in runs of run_len consecutive codewords; each run's common zeros in its
+// agreed top bits are shrunk once per theta, and each pair continues from that
+// state, as one kernel thread does for its run.
+extern "C" int tp_host_runs(const csim_state* theta, int ntheta, const uint64_t* xs, int nx, int run_len, int* eps,
+                            int* p, int* m) {
+    using namespace csim::pc;
+    int err = 0;
+    alignas(16) uint32_t wJ32[32], rJ32[32];
+    alignas(16) uint64_t wJ64[34], rJ64[34];
+    alignas(16) uint64_t wG[64], rG[64];
+    const PairMem mem{wJ32, wJ64, wG, 1};
+    const PairMem rmem{rJ32, rJ64, rG, 1};
+    uint64_t pGT[64];
+    for (int a = 0; a < ntheta; a++) {
+        const csim_state& th = theta[a];
+        for (int c = 0; c < 64; c++) {
+            uint64_t col = 0;
+            if (c < th.n)
+                for (int r = 0; r < th.k; r++) col |= ((th.G[r] >> c) & 1ull) << r;
+            pGT[c] = col;
+        }
+        for (int r0 = 0; r0 < nx; r0 += run_len) {
+            const int r1 = r0 + run_len < nx ? r0 + run_len : nx;
+            uint64_t am = ~0ull, om = 0ull;
+            for (int j = r0; j < r1; j++) {
+                am &= xs[j];
+                om |= xs[j];
+            }
+            const uint64_t pm = agree_top(am ^ om, th.n);
+            RunState rs;
+            run_prefix(true, th.n, pm, am, th.k, th.Q, th.h, th.D1, th.D2, th.J, pGT, rmem, rs);
+            for (int j = r0; j < r1; j++) {
+                const int w = a * nx + j;
+                pair_from_run(true, th.n, rs, rmem, xs[j], mem, eps[w], p[w], m[w], err, 64, th.k);
+            }
+        }
+    }
+    return err;
+}

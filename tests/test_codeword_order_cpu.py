@@ -26,6 +26,8 @@ def lib():
     lb = C.CDLL(SO)
     lb.order_codewords.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
     lb.order_codewords.restype = C.c_int64
+    lb.order_runs.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
+    lb.order_runs.restype = C.c_int64
     return lb
 
 
@@ -65,3 +67,42 @@ def test_items_per_thread_by_t(lib):
     (CSIM_OPT_PER_THREAD).  Results never depend on it; the kernels' speed does."""
     assert [lib.order_per_thread(0, t) for t in (1, 24, 40, 52, 53, 64)] == [32, 32, 32, 32, 16, 16]
     assert lib.order_per_thread(8, 40) == 8 and lib.order_per_thread(16, 24) == 16
+
+
+def _agree_top(dis, n):
+    nm = (1 << n) - 1
+    d = dis & nm
+    return nm if d == 0 else nm & ~((1 << d.bit_length()) - 1)
+
+
+@pytest.mark.parametrize("t,k,pt,gl", [(24, 11, 16, 12), (40, 16, 32, 22), (40, 13, 16, 20), (64, 14, 16, 35)])
+def test_run_order(lib, t, k, pt, gl):
+    """The run kernel's order: a permutation of all 2^k codewords; in each block
+    of 64 runs, thread r's run sits at positions r + 64 i; a run is pt codewords
+    consecutive in value, sorted by their zeros below the run's agreed top bits;
+    runs with a codeword of more such zeros than gl come before the split, which
+    is a whole number of blocks, and none after it."""
+    rs = np.random.RandomState(t * 7 + k)
+    L = np.array([int(rs.randint(1, 1 << 62)) & ((1 << t) - 1) for _ in range(k)], dtype=np.uint64)
+    out = np.zeros(1 << k, dtype=np.uint64)
+    split = lib.order_runs(L.ctypes.data, k, t, pt, gl, out.ctypes.data)
+    got = [int(v) for v in out]
+    allcw = sorted(_codewords(L, k))
+    assert sorted(got) == allcw
+    assert split % (64 * pt) == 0
+    rank = {v: i for i, v in enumerate(allcw)}
+    nm = (1 << t) - 1
+    for b0 in range(0, len(got), 64 * pt):
+        for r in range(64):
+            run = [got[b0 + r + 64 * i] for i in range(pt)]
+            idx = sorted(rank[v] for v in run)
+            assert idx == list(range(idx[0], idx[0] + pt)) and idx[0] % pt == 0  # consecutive in value
+            am, om = nm, 0
+            for v in run:
+                am &= v
+                om |= v
+            low = nm & ~_agree_top(am ^ om, t)
+            rem = [bin(~v & low).count("1") for v in run]
+            assert rem == sorted(rem)
+            if b0 >= split:
+                assert max(rem) <= gl

@@ -32,12 +32,18 @@ def tp(request):
     lib.tp_host_pairs.restype = C.c_int
     lib.tp_host_block.argtypes = lib.tp_host_pairs.argtypes
     lib.tp_host_block.restype = C.c_int
+    lib.tp_host_runs.argtypes = lib.tp_host_pairs.argtypes[:4] + [C.c_int] + lib.tp_host_pairs.argtypes[4:]
+    lib.tp_host_runs.restype = C.c_int
 
-    def run(thetas, xs, block=False):
+    def run(thetas, xs, block=False, run_len=0):
         thetas = np.ascontiguousarray(thetas)
         xs = np.ascontiguousarray(np.asarray(xs, dtype=np.uint64))
         n = len(thetas) * len(xs)
         e, p, m = (np.zeros(n, dtype=np.int32) for _ in range(3))
+        if run_len:
+            err = lib.tp_host_runs(thetas.ctypes.data, len(thetas), xs.ctypes.data, len(xs), run_len, e.ctypes.data,
+                                   p.ctypes.data, m.ctypes.data)
+            return err, e, p, m
         fn = lib.tp_host_block if block else lib.tp_host_pairs
         err = fn(thetas.ctypes.data, len(thetas), xs.ctypes.data, len(xs), e.ctypes.data, p.ctypes.data,
                  m.ctypes.data)
@@ -146,3 +152,24 @@ def test_shared_prefix_vs_oracle(tp, oracle, t, k, d):
                 want = oracle.inner_product(thetas[a:a + 1], oracle.prep_l(int(j), t, L))
                 assert (e[w], p[w], m[w]) == want, (t, d, a, int(j))
                 w += 1
+
+
+@pytest.mark.parametrize("t,k,run_len", [(3, 3, 4), (12, 6, 8), (24, 8, 32), (33, 9, 16), (40, 10, 32), (57, 8, 32),
+                                         (64, 8, 16)])
+def test_runs_vs_oracle(tp, oracle, t, k, run_len):
+    """The run kernel's per-thread path: the 2^k codewords in numeric order,
+    cut into runs of run_len; each run's common zeros in its agreed top bits
+    shrunk once, then every pair from that state, against the oracle."""
+    rs = np.random.RandomState(1300 + t)
+    L = np.array([rand_word(rs, t) for _ in range(k)], dtype=np.uint64)
+    thetas = _projected_thetas(oracle, rs, t, count=4)
+    js = np.arange(2 ** k)
+    xs = sorted((oracle.codeword(int(j), L), int(j)) for j in js)
+    err, e, p, m = tp(thetas, [x for x, _ in xs], run_len=run_len)
+    assert err == 0
+    w = 0
+    for a in range(len(thetas)):
+        eo, po, mo = oracle.term_products(t, 0, L, k, thetas[a:a + 1], 0, 2 ** k, threads=os.cpu_count() or 1)
+        for x, j in xs:
+            assert (e[w], p[w], m[w]) == (eo[j], po[j], mo[j]), (t, a, j)
+            w += 1
