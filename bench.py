@@ -404,16 +404,75 @@ def batch_compare(gpu, reps=3, light=True, every=1):
             "timing": "wall clock around the ABI call, host work included, median of reps"}
 
 
-def serve_compare(rate, count, seed=5):
-    """Serving on the light c3 queries under Poisson arrivals at `rate`
-    queries/s: the continuous-batching server (csim_submit as each query
-    arrives) vs plain one-at-a-time service (first come first served through
-    the single-query entry points).  Latency = result time - arrival time."""
+C5_EPS = (0.1, 0.05, 0.02)
+
+
+def c5_stream(count, seed=505, max_pairs=1 << 30):
+    """Queries of the c5 serving configuration, drawn in order from a seeded
+    stream: t ~ U[8, 64], n ~ U[8, 40], eps ~ {0.1, 0.05, 0.02}, 1..4 measured
+    qubits with a random outcome, the random Clifford+T circuits of
+    tests/golden/circuits.py through this package's front end (equal to the
+    reference's, tests/test_frontend.py).  Exact decomposition for t <= 16,
+    else a code of k = min(18, the fidelity-0.02 rule of probability.c:330)
+    rows; L from eps and failure probability 0.05 by probability.py:150-167.
+    Draws whose inner products exceed max_pairs are skipped (a c5 query at
+    eps = 0.02 and t = 60 takes 2.6e10 pairs, about a minute of GPU time), so
+    the kept stream still spans t = 8..64 and every eps.  Returns (queries,
+    draws, [(t, eps, pairs)])."""
+    import math
+
+    from circuitsimulator_gb300 import backend, sample
+
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    from circuits import compiled, random_circuit
+
+    rs = np.random.RandomState(seed)
+    out, meta, draws = [], [], 0
+    while len(out) < count:
+        draws += 1
+        n, t, nm = int(rs.randint(8, 41)), int(rs.randint(8, 65)), int(rs.randint(1, 5))
+        eps = float(C5_EPS[int(rs.randint(3))])
+        config = {"exact": True} if t <= 16 else {
+            "exact": False, "fidbound": 0.02,
+            "k": min(18, int(math.ceil(1 - 2 * t * math.log2(math.cos(math.pi / 8)) - math.log2(0.02))))}
+        config.update({"error": eps, "failprob": 0.05, "quiet": True, "seed": 7000 + draws})
+        circ = compiled(random_circuit(n, t, rs)[0])
+        qubits = sorted(rs.choice(n, size=nm, replace=False).tolist())
+        outcome = rs.randint(2, size=nm).tolist()
+        try:
+            q = next(sample.probability_steps(circ, {a: b for a, b in zip(qubits, outcome)}, config,
+                                              np.random.RandomState(draws)))
+        except Exception:  # StopIteration (answered without a backend query) or a front-end refusal
+            continue
+        cfg = q["cfg"]
+        if cfg["t"] < 1:
+            continue
+        chi = 2 ** ((cfg["t"] + 1) // 2) if cfg["exact"] else 2 ** cfg["k"]
+        na = cfg["noapprox"] or (not cfg["forceSample"] and cfg["samples"] * cfg["bins"] * 2 > chi - 1)
+        pairs = sum(chi * (chi + 1) // 2 if na else cfg["samples"] * cfg["bins"] * chi
+                    for p in q["projs"] if len(p[0]) > 0)
+        if pairs > max_pairs:
+            continue
+        q["rng"] = backend.RNG_PHILOX
+        out.append(q)
+        meta.append((cfg["t"], eps, pairs))
+    return out, draws, meta
+
+
+def serve_compare(rate, count, seed=5, c5=False):
+    """Serving under Poisson arrivals at `rate` queries/s: the continuous-batching
+    server (csim_submit as each query arrives) vs plain one-at-a-time service
+    (first come first served through the single-query entry points).  Latency
+    = result time - arrival time.  Queries: the light c3 queries, or with c5
+    the first `count` queries of c5_stream."""
     from circuitsimulator_gb300 import backend
 
-    light, _ = c3_queries(light=True)
     rs = np.random.RandomState(seed)
-    qs = [light[i] for i in rs.randint(len(light), size=count)]
+    if c5:
+        qs, draws, meta = c5_stream(count)
+    else:
+        light, _ = c3_queries(light=True)
+        qs = [light[i] for i in rs.randint(len(light), size=count)]
     arrivals = np.cumsum(rs.exponential(1.0 / rate, size=count))
 
     def pct(v):
@@ -454,8 +513,16 @@ def serve_compare(rate, count, seed=5):
         lat.append(time.perf_counter() - t0 - a)
     t_end = time.perf_counter()
     plain = dict(pct(lat), queries_per_s=count / (t_end - t0))
-    return {"workload": "c5 (scaled): %d light c3 queries (t 8..23, relative error 0.05), Poisson arrivals at "
-                        "%g queries/s" % (count, rate),
+    if c5:
+        ts = [m[0] for m in meta]
+        what = ("c5 subset: the first %d of %d draws of the seeded c5 stream with <= 2^30 inner products each "
+                "(t %d..%d, eps %s: %d at 0.02; %.3g pairs), Poisson arrivals at %g queries/s"
+                % (count, draws, min(ts), max(ts), "/".join(str(e) for e in C5_EPS),
+                   sum(1 for m in meta if m[1] == 0.02), sum(m[2] for m in meta), rate))
+    else:
+        what = ("c5 (scaled): %d light c3 queries (t 8..23, relative error 0.05), Poisson arrivals at %g queries/s"
+                % (count, rate))
+    return {"workload": what,
             "rate": rate, "server": server, "plain": plain,
             "throughput_ratio": server["queries_per_s"] / plain["queries_per_s"]}
 
@@ -613,6 +680,7 @@ def main():
     ap.add_argument("--serve", default=None, metavar="RATES",
                     help="only time serving under Poisson arrivals at these rates (queries/s, comma separated)")
     ap.add_argument("--serve-count", type=int, default=300, help="queries per rate for --serve")
+    ap.add_argument("--serve-c5", action="store_true", help="--serve on the c5 stream (all t, every eps)")
     ap.add_argument("--c3-full", action="store_true",
                     help="only time all 256 c3 queries, plain vs batched (about 10 minutes per arm)")
     ap.add_argument("--c3-every", type=int, default=None, metavar="N",
@@ -630,7 +698,7 @@ def main():
         return
     if args.serve:
         rates = [float(r) for r in args.serve.split(",")]
-        print(json.dumps([serve_compare(r, args.serve_count) for r in rates]))
+        print(json.dumps([serve_compare(r, args.serve_count, c5=args.serve_c5) for r in rates]))
         return
     if args.chain:
         shots, nbits = (int(v) for v in args.chain.lower().split("x"))
