@@ -310,6 +310,9 @@ def run_ours(args, rank, world, local_rank):
     }
     if world == 1 and not args.no_batch:
         out["batch"] = batch_compare(gpu)
+        # the same comparison on every 32nd c3 query (t 15..53, three of them heavy), so the line
+        # carries the mixed set next to the light one
+        out["batch_c3_sample"] = batch_compare(gpu, reps=1, light=False, every=32)
         out["serve"] = serve_compare(100.0, 150)
     if world == 1 and not args.no_cpu_baseline:
         try:

@@ -758,8 +758,9 @@ CSIM_HD inline void pair_l(bool valid, int n, int k1, int Q, uint64_t h, uint64_
 // those shrinks, with the G columns and h bits of the positions below pm (J
 // rows and G columns masked to the new k).  Returns 0 if a shrink found the
 // projection empty (every such pair is then 0), else 1.  Every lane of one
-// warp calls it; the `act` lane (one per warp) does the work in its working
-// memory M, which has room for 64 G columns, and is the only one that writes.
+// warp calls it; the `act` lanes (up to two per warp, each with its own group
+// state pJ/pGT and its own working memory M with room for 64 G columns) do
+// the work, and only they write.
 CSIM_HD inline int prefix_shrink(bool act, int n, uint64_t pm, uint64_t x0, int& k, int& Q, uint64_t& h,
                                  uint64_t& D1, uint64_t& D2, uint64_t* pJ, uint64_t* pGT, const PairMem& M) {
     const uint64_t pz = act ? (~x0 & pm & lowmask(n)) : 0ull;
