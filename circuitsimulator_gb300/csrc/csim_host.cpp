@@ -74,7 +74,7 @@ extern "C" int csim_set_option(csim_ctx* ctx, int32_t option, int64_t value) {
     if (!ctx) return CSIM_ERR_ARG;
     switch (option) {
     case CSIM_OPT_PAIR_KERNEL:
-        if (value < 0 || value > 3) return fail(ctx, CSIM_ERR_ARG, "pair kernel must be 0..3");
+        if (value < 0 || value > 4) return fail(ctx, CSIM_ERR_ARG, "pair kernel must be 0..4");
         ctx->pair_kernel = (int)value;
         return CSIM_OK;
     case CSIM_OPT_PER_THREAD:
@@ -357,6 +357,48 @@ namespace {
 
 // the terms |phi_j>, j in [j0, j0+nj): codewords (|L>) or prepared states (|H^t>).
 // ordered: all 2^k codewords in ordered_codewords' order (sums over all terms only)
+// G-slot bounds of the block-prefix kernel's occupancy classes for t, most
+// zeros first: t, then each largest zero bound that lets one more block per SM
+// be resident.  Classes that would hold under 3% of the 2^k codewords of L
+// merge into the next heavier class (a launch's tail costs more than its
+// occupancy gains).
+int occupancy_bounds(csim_ctx* ctx, int t, const uint64_t* L, int k, std::vector<int>& bounds) {
+    bounds.assign(1, t);
+    int last = csim::terms_tp_occupancy(t, t);
+    if (last < 1) return fail(ctx, CSIM_ERR_CUDA, "occupancy query failed");
+    for (int g = t - 1; g >= 0; g--) {
+        const int o = csim::terms_tp_occupancy(t, g);
+        if (o < 1) return fail(ctx, CSIM_ERR_CUDA, "occupancy query failed");
+        if (o > last) {
+            bounds.push_back(g);
+            last = o;
+        }
+    }
+    // zero counts of the codewords (Gray code walk)
+    std::vector<int64_t> hist(CSIM_MAX_QUBITS + 2, 0);
+    uint64_t x = 0;
+    hist[(size_t)t]++;
+    for (int64_t i = 1; i < ((int64_t)1 << k); i++) {
+        x ^= L[k - 1 - __builtin_ctzll((unsigned long long)i)];
+        hist[(size_t)(t - __builtin_popcountll(x))]++;
+    }
+    const int64_t chi = (int64_t)1 << k;
+    for (bool merged = true; merged && bounds.size() > 1;) {
+        merged = false;
+        for (size_t c = 1; c < bounds.size(); c++) {
+            const int hi = bounds[c], lo = c + 1 < bounds.size() ? bounds[c + 1] : -1;
+            int64_t n = 0;
+            for (int z = lo + 1; z <= hi; z++) n += hist[(size_t)z];
+            if (n * 100 < 3 * chi) {
+                bounds.erase(bounds.begin() + (long)c);
+                merged = true;
+                break;
+            }
+        }
+    }
+    return 0;
+}
+
 // ordered with tn: the table of tn's kernel -- ordered_codewords with light
 // bound tn->light (block-prefix kernel), or run_ordered_codewords with runs of
 // tn->per_thread (run kernel); ctx->cw_split is then the light launch's first term.
@@ -379,6 +421,10 @@ int stage_terms(csim_ctx* ctx, int t, int exact, const uint64_t* L, int k, int64
             int64_t split;
             if (tn->kernel == 1) {
                 split = run_ordered_codewords(L, k, t, tn->per_thread, tn->light, cw);
+            } else if (tn->kernel == 2) {
+                CKR(occupancy_bounds(ctx, t, L, k, ctx->cw_bounds));
+                ordered_codewords_classes(L, k, t, ctx->cw_bounds, cw, ctx->cw_starts);
+                split = 0;
             } else {
                 ordered_codewords(L, k, t, tn->light, cw);
                 split = light_split(cw, t, tn->light);
@@ -483,6 +529,7 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
     if (tp && count > 0) CKR(tune_for(ctx, t, &tn, P, L, k));  // before any draw: tuning leaves the streams as they are
     // the run kernel takes whole blocks of 64 runs
     if (tn.kernel == 1 && (exact || ((int64_t)1 << k) % (64 * (int64_t)tn.per_thread) != 0)) tn = default_tune(t);
+    if (tn.kernel == 2 && exact) tn = default_tune(t);
     if (rng == CSIM_RNG_LIBC && seed != CSIM_SEED_CONTINUE) ctx->lr.seed((uint32_t)seed);
     if (rng == CSIM_RNG_PHILOX && seed != CSIM_SEED_CONTINUE) {
         ctx->philox_seed = seed;
@@ -573,7 +620,20 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
             first = false;
             __int128* spart = dpart + (size_t)s0 * nchunks * 4;
             int rc = 0;
-            if (tp && tn.kernel == 1) {
+            if (tp && tn.kernel == 2) {
+                // one launch per occupancy class; class c's launch starts at its first whole item
+                const int64_t span = 64 * (int64_t)pt;
+                const int nc = (int)ctx->cw_bounds.size();
+                for (int c = 0; c < nc; c++) {
+                    const int64_t a0 = c == 0 ? 0 : (ctx->cw_starts[(size_t)c] + span - 1) / span * span;
+                    const int64_t b0 = c + 1 < nc ? (ctx->cw_starts[(size_t)c + 1] + span - 1) / span * span : chi;
+                    const int64_t aa = std::min(a0, chi), bb = std::min(b0, chi);
+                    if (aa < bb)
+                        rc |= csim::launch_terms_tp(launch_of(ctx), t, ctx->cw_bounds[(size_t)c], dcw + aa, sth,
+                                                    scode, cs, aa, bb - aa, pt, P2, spart, nchunks, aa / span,
+                                                    nullptr, nullptr, nullptr);
+                }
+            } else if (tp && tn.kernel == 1) {
                 // run kernel: terms [0, jb) in heavy runs, [jb, chi) in runs whose codewords have at most
                 // tn.light zeros below their run's agreed top bits
                 const int64_t span = 64 * (int64_t)pt;
@@ -709,7 +769,8 @@ int tune_run(csim_ctx* ctx, int t, const csim_projector* Pw, const uint64_t* Lw,
         int kernel, pt, pct;
     };
     static const Cand cands[] = {{0, 16, 50}, {0, 16, 60}, {0, 16, 70}, {0, 32, 50}, {0, 32, 60}, {0, 32, 70},
-                                 {1, 16, 50}, {1, 16, 55}, {1, 16, 60}, {1, 32, 50}, {1, 32, 55}, {1, 32, 60}};
+                                 {1, 16, 50}, {1, 16, 55}, {1, 16, 60}, {1, 32, 50}, {1, 32, 55}, {1, 32, 60},
+                                 {2, 16, 60}, {2, 32, 60}};
     for (const Cand& c : cands) {
         if (rc) break;
         if (c.kernel == 1 && chi % (64 * (int64_t)c.pt) != 0) continue;
@@ -779,6 +840,7 @@ int tune_for(csim_ctx* ctx, int t, TpTune* out, const csim_projector* P, const u
         r.kernel = 1;
         r.light = std::min(t, (11 * t + 19) / 20);
     }
+    if (ctx->pair_kernel == 4) r.kernel = 2;  // the block-prefix kernel, one launch per occupancy class
     if (ctx->per_thread > 0) r.per_thread = ctx->per_thread;
     *out = r;
     return 0;

@@ -163,7 +163,8 @@ inline int tp_per_thread(int fixed, int t) { return fixed > 0 ? fixed : auto_per
 struct TpTune {
     int per_thread = 0;
     int light = 0;
-    int kernel = 0;  // 0: block-prefix kernel (k_terms_tp); 1: run kernel (k_terms_runs)
+    int kernel = 0;  // 0: block-prefix kernel (k_terms_tp), heavy and light launches; 1: run kernel
+                     // (k_terms_runs); 2: block-prefix kernel, one launch per occupancy class
 };
 inline TpTune default_tune(int t) {
     TpTune r;
@@ -220,6 +221,43 @@ inline int64_t light_split(const std::vector<uint64_t>& cw, int t, int lz) {
     return j;
 }
 inline int64_t light_split(const std::vector<uint64_t>& cw, int t) { return light_split(cw, t, light_zeros(t)); }
+
+// The 2^k codewords of L ordered for launches by zero class: bounds[0] = t >
+// bounds[1] > ... are the G-slot bounds of the launches; class c holds the
+// codewords with at most bounds[c] zeros and more than bounds[c + 1].  Classes
+// in order (most zeros first), each ordered as ordered_codewords orders a
+// part (top bits, weight, value).  starts[c] = first index of class c.  With
+// bounds {t, light_zeros(t)} this is ordered_codewords' order.
+inline void ordered_codewords_classes(const uint64_t* L, int k, int t, const std::vector<int>& bounds,
+                                      std::vector<uint64_t>& out, std::vector<int64_t>& starts) {
+    const int64_t chi = (int64_t)1 << k;
+    out.resize((size_t)chi);
+    uint64_t x = 0;
+    out[0] = 0;
+    for (int64_t i = 1; i < chi; i++) {
+        x ^= L[k - 1 - __builtin_ctzll((unsigned long long)i)];
+        out[(size_t)i] = x;
+    }
+    const int nc = (int)bounds.size();
+    auto cls = [&bounds, nc, t](uint64_t v) {
+        const int z = t - __builtin_popcountll(v);
+        int c = 0;
+        while (c + 1 < nc && z <= bounds[(size_t)c + 1]) c++;
+        return c;
+    };
+    const int d = ordered_prefix_bits(k, t);
+    std::sort(out.begin(), out.end(), [&cls, d, t](uint64_t a, uint64_t b) {
+        const int ca = cls(a), cb = cls(b);
+        if (ca != cb) return ca < cb;
+        const uint64_t ta = d ? a >> (t - d) : 0, tb = d ? b >> (t - d) : 0;
+        if (ta != tb) return ta < tb;
+        const int pa = __builtin_popcountll(a), pb = __builtin_popcountll(b);
+        return pa != pb ? pa < pb : a < b;
+    });
+    starts.assign((size_t)nc + 1, chi);
+    for (int64_t i = chi - 1; i >= 0; i--) starts[(size_t)cls(out[(size_t)i])] = i;
+    for (int c = nc - 1; c >= 0; c--) starts[(size_t)c] = std::min(starts[(size_t)c], starts[(size_t)c + 1]);
+}
 
 // Top bits of [0, n) on which codewords that differ in the bits `dis` agree
 // (csim::pc::agree_top's host twin)
@@ -346,6 +384,8 @@ struct csim_ctx {
     Engine* engine = nullptr;  // created by the first batched csim_run_queries
     std::vector<uint64_t> cw_key;  // (k, rows of L, t, light bound) of the ordered codeword table in kBufCwOrdered
     int64_t cw_split = 0;          // first index of that table whose codewords have <= the light bound's zeros
+    std::vector<int> cw_bounds;        // occupancy-class order: the launches' zero bounds
+    std::vector<int64_t> cw_starts;    // and the first index of each class
     // autotuner (CSIM_OPT_AUTOTUNE): the tuned launch parameters live in a
     // process-wide table per device (csim_host.cpp), filled a t bucket at a time
     int autotune = 1;

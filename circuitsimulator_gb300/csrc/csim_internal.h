@@ -52,6 +52,9 @@ int launch_terms_tp(const Launch& L, int nmax, int gmax, const uint64_t* codewor
                     const int* code, int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P, __int128* part,
                     int64_t part_stride, int64_t part_base, int* eps_o, int* p_o, int* m_o);
 int64_t terms_tp_blocks(int64_t nj, int per_thread);
+// resident blocks per SM of the thread-per-pair kernel for states of up to nmax
+// qubits and codewords of up to gmax zeros (-1 if the query fails)
+int terms_tp_occupancy(int nmax, int gmax);
 
 // the run kernel (csim_terms_tp.cu): codewords [j0, j0 + nj) in run order
 // (csim_host::run_ordered_codewords), runs of per_thread codewords, partial

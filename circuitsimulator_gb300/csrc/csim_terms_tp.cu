@@ -327,6 +327,17 @@ int launch_terms_tp(const Launch& L, int nmax, int gmax, const uint64_t* codewor
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
+int terms_tp_occupancy(int nmax, int gmax) {
+    if (cudaFuncSetAttribute(k_terms_tp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)terms_tp_smem(64, 64)) !=
+        cudaSuccess)
+        return -1;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_terms_tp, kTP, terms_tp_smem(nmax, gmax)) !=
+        cudaSuccess)
+        return -1;
+    return per_sm;
+}
+
 int64_t terms_tp_blocks(int64_t nj, int per_thread) {
     const int64_t span = (int64_t)kTP * per_thread;
     return (nj + span - 1) / span;

@@ -21,3 +21,13 @@ extern "C" int64_t order_runs(const uint64_t* L, int k, int t, int pt, int gl, u
     std::copy(cw.begin(), cw.end(), out);
     return split;
 }
+
+// Zero-class order (ordered_codewords_classes); starts has nbounds + 1 entries.
+extern "C" void order_classes(const uint64_t* L, int k, int t, const int* bounds, int nbounds, uint64_t* out,
+                              int64_t* starts) {
+    std::vector<uint64_t> cw;
+    std::vector<int64_t> st;
+    csim_host::ordered_codewords_classes(L, k, t, std::vector<int>(bounds, bounds + nbounds), cw, st);
+    std::copy(cw.begin(), cw.end(), out);
+    std::copy(st.begin(), st.end(), starts);
+}

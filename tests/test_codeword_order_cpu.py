@@ -28,6 +28,8 @@ def lib():
     lb.order_codewords.restype = C.c_int64
     lb.order_runs.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
     lb.order_runs.restype = C.c_int64
+    lb.order_classes.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    lb.order_classes.restype = None
     return lb
 
 
@@ -106,3 +108,32 @@ def test_run_order(lib, t, k, pt, gl):
             assert rem == sorted(rem)
             if b0 >= split:
                 assert max(rem) <= gl
+
+
+@pytest.mark.parametrize("t,k", [(24, 12), (57, 12), (64, 14)])
+def test_zero_class_order(lib, t, k):
+    """Launches per zero class: with bounds {t, light_zeros(t)} the order is the
+    heavy/light order itself; with more bounds, class c (at most bounds[c]
+    zeros, more than bounds[c + 1]) starts at starts[c], classes in order, each
+    ordered by top bits, weight and value."""
+    rs = np.random.RandomState(t * 11 + k)
+    L = np.array([int(rs.randint(1, 1 << 62)) & ((1 << t) - 1) for _ in range(k)], dtype=np.uint64)
+    ref = np.zeros(1 << k, dtype=np.uint64)
+    split = lib.order_codewords(L.ctypes.data, k, t, ref.ctypes.data)
+    for bounds in ([t, lib.order_light_zeros(t)], [t, (7 * t) // 10, (3 * t) // 5, t // 2]):
+        b = np.array(bounds, dtype=np.int32)
+        out = np.zeros(1 << k, dtype=np.uint64)
+        starts = np.zeros(len(bounds) + 1, dtype=np.int64)
+        lib.order_classes(L.ctypes.data, k, t, b.ctypes.data, len(bounds), out.ctypes.data, starts.ctypes.data)
+        got = [int(v) for v in out]
+        assert sorted(got) == sorted(_codewords(L, k))
+        if len(bounds) == 2:
+            assert got == [int(v) for v in ref] and starts[1] == split
+        d = lib.order_prefix_bits(k, t)
+        assert starts[0] == 0 and starts[-1] == 1 << k and list(starts) == sorted(starts)
+        for c in range(len(bounds)):
+            part = got[starts[c]:starts[c + 1]]
+            lo = bounds[c + 1] if c + 1 < len(bounds) else -1
+            assert all(lo < t - bin(v).count("1") <= bounds[c] for v in part)
+            key = [((v >> (t - d)) if d else 0, bin(v).count("1"), v) for v in part]
+            assert key == sorted(key)

@@ -236,8 +236,9 @@ def test_autotuner_leaves_results_and_streams_unchanged():
 @pytest.mark.parametrize("t,k,pt", [(24, 11, 16), (40, 16, 32), (40, 12, 16), (57, 12, 32), (64, 14, 16)])
 def test_run_kernel_equals_block_kernel(gpu, t, k, pt):
     """The sampler through the run kernel (codewords in per-thread runs that
-    share their top-bit shrinks) and through the block-prefix kernel: identical
-    values for every state (both sums are exact), on the same counter-based draws."""
+    share their top-bit shrinks), through the block-prefix kernel with heavy and
+    light launches, and with one launch per occupancy class: identical values
+    for every state (the sums are exact), on the same counter-based draws."""
     rs = np.random.RandomState(4000 + t + k)
     L = [rand_word(rs, t) for _ in range(k)]
     rows = random_projector_rows(rs, t, int(0.7 * t))
@@ -245,11 +246,11 @@ def test_run_kernel_equals_block_kernel(gpu, t, k, pt):
     out = []
     try:
         gpu.set_option(backend.OPT_PER_THREAD, pt)
-        for kernel in (2, 3):
+        for kernel in (2, 3, 4):
             gpu.set_option(backend.OPT_PAIR_KERNEL, kernel)
             out.append(gpu.singleProjectorSample(P, L, False, 96, backend.RNG_PHILOX, 606))
     finally:
         gpu.set_option(backend.OPT_PAIR_KERNEL, 0)
         gpu.set_option(backend.OPT_PER_THREAD, 0)
-    assert (out[0] == out[1]).all()
+    assert (out[0] == out[1]).all() and (out[0] == out[2]).all()
     assert (out[0] != 0).sum() > 48
