@@ -228,6 +228,9 @@ def run_ours(args, rank, world, local_rank):
         step(i, backend.RNG_PHILOX)
         flush.zero_()
     barrier()
+    tuned = gpu.autotune(cfg["t"], P[0], [int(x) for x in L])  # done by the first warm-up step; reads the choice
+    kname = {0: "k_terms_tp (heavy and light launches)", 1: "k_terms_runs",
+             2: "k_terms_tp (one launch per occupancy class)"}[tuned[3]]
     clocks = ClockSampler(local_rank)
     clocks.start()
     launches0 = gpu.launches
@@ -279,7 +282,7 @@ def run_ours(args, rank, world, local_rank):
     kernel_rate = (pairs / world) / (pair_ms / 1e3)  # pairs/s of the pair kernel alone (rank 0 share)
     achieved = kernel_rate * per_pair / 1e9 if per_pair else None
     peak = alu_peak_gops(props.multi_processor_count, clk.get("sm_max_mhz") or 2070.0)
-    roofline = {"bound": "alu", "kernel": "k_terms_tp (theta x prepL term pairs, thread per pair)",
+    roofline = {"bound": "alu", "kernel": kname + ": (theta, prepL term) pairs, one thread per pair",
                 "achieved": achieved, "peak": peak, "unit": "G packed row-ops/s",
                 "frac": (achieved / peak) if achieved else None,
                 "traffic": dram_bytes_per_launch(samples * bins / world),
@@ -301,7 +304,9 @@ def run_ours(args, rank, world, local_rank):
                    "ranks": "the states of each projector split over %d rank(s), values gathered on rank 0" % world,
                    "last_query": {"numerator": result.get(0), "denominator": result.get(1)},
                    "l2": "flushed between steps (256 MiB write); hot data (codewords 512 KiB) is L2-resident",
-                   "rng": "Philox on device (value); the C library's rand() sequence (e2e)"},
+                   "rng": "Philox on device (value); the C library's rand() sequence (e2e)",
+                   "launch": {"kernel": kname, "terms_per_thread": tuned[0], "light_zero_bound": tuned[1],
+                              "chosen_by": "csim_autotune on this query's G' and code"}},
         "e2e": {"value": e2e_pairs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
                 "d2h_bytes_per_step": d2h // args.steps, "ms_per_step": 1e3 * e2e_s / args.steps},
         "roofline": roofline,

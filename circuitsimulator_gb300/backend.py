@@ -146,7 +146,7 @@ def load_library(path=LIB_PATH):
         "csim_exact_projector": ([vp, vp, vp, i32, i32, C.c_double, vp], C.c_int),
         "csim_exact_projector_rows": ([vp, vp, vp, i32, i32, i64, i64, vp, vp], C.c_int),
         "csim_median_of_means": ([vp, i32, i32, vp], C.c_int),
-        "csim_autotune": ([vp, i32, vp, vp, i32, vp, vp, vp], C.c_int),
+        "csim_autotune": ([vp, i32, vp, vp, i32, vp, vp, vp, vp], C.c_int),
         "csim_decompose": ([i32, C.c_double, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp], C.c_int),
         "csim_decompose_on": ([vp, i32, C.c_double, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp], C.c_int),
         "csim_fidelity_sum": ([vp, i32, vp, i32, vp], C.c_int),
@@ -270,13 +270,14 @@ class Backend:
     def autotune(self, t, P=None, L=None):
         """Tunes t's bucket if this process has not yet (csim_autotune), on
         projector P and code L when given; returns (terms per thread,
-        light-launch zero bound, pair-kernel ms of the winning trial)."""
-        pt, lz, ms = C.c_int32(0), C.c_int32(0), C.c_double(0)
+        light-launch zero bound, pair-kernel ms of the winning trial, kernel:
+        0 block-prefix heavy/light, 1 per-thread runs, 2 per occupancy class)."""
+        kern, pt, lz, ms = C.c_int32(0), C.c_int32(0), C.c_int32(0), C.c_double(0)
         Lp = np.ascontiguousarray(np.asarray([int(x) for x in (L if L is not None else [])] or [0], dtype=np.uint64))
         k = 0 if L is None else len(L)
         self._check(self.lib.csim_autotune(self.ctx, int(t), C.byref(P) if P is not None else None, _p(Lp), int(k),
-                                           C.byref(pt), C.byref(lz), C.byref(ms)))
-        return pt.value, lz.value, ms.value
+                                           C.byref(kern), C.byref(pt), C.byref(lz), C.byref(ms)))
+        return pt.value, lz.value, ms.value, kern.value
 
     def rng_position(self, seed, first):
         """Next CSIM_RNG_PHILOX draw (with SEED_CONTINUE) is state `first` of stream `seed`."""

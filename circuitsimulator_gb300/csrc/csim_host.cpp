@@ -849,7 +849,7 @@ int tune_for(csim_ctx* ctx, int t, TpTune* out, const csim_projector* P, const u
 }  // namespace csim_host
 
 extern "C" int csim_autotune(csim_ctx* ctx, int32_t t, const csim_projector* P, const uint64_t* L, int32_t k,
-                             int32_t* per_thread, int32_t* light_zeros_out, double* pair_ms) {
+                             int32_t* kernel, int32_t* per_thread, int32_t* light_zeros_out, double* pair_ms) {
     if (!ctx || t < 1 || t > CSIM_MAX_QUBITS || (P && P->nqubits != t) || k < 0 || k > 30 || (k > 0 && !L))
         return fail(ctx, CSIM_ERR_ARG, "bad argument");
     cudaSetDevice(ctx->device);
@@ -860,6 +860,7 @@ extern "C" int csim_autotune(csim_ctx* ctx, int32_t t, const csim_projector* P, 
         CKR(tune_run(ctx, t, P, L, k));
         if (!tuned_get(ctx->device, t, &tn, &ms)) return fail(ctx, CSIM_ERR_CUDA, "tuning left no result");
     }
+    if (kernel) *kernel = tn.kernel;
     if (per_thread) *per_thread = tn.per_thread;
     if (light_zeros_out) *light_zeros_out = tn.light;
     if (pair_ms) *pair_ms = ms;

@@ -142,10 +142,12 @@ int csim_set_option(csim_ctx *ctx, int32_t option, int64_t value);
  * code).  A bucket is tuned once; with CSIM_OPT_AUTOTUNE on (the default) the
  * first sampler call or batched query at a new t tunes it on its own
  * workload.  The caller's random streams and last statistics are unchanged.
- * Returns the chosen terms per thread, light bound and the pair-kernel
- * milliseconds of the winning trial. */
+ * Returns the chosen kernel (0 block-prefix with heavy and light launches,
+ * 1 per-thread runs, 2 block-prefix with one launch per occupancy class), terms
+ * per thread, light bound and the pair-kernel milliseconds of the winning trial.
+ * Any output pointer may be NULL. */
 int csim_autotune(csim_ctx *ctx, int32_t t, const csim_projector *P, const uint64_t *L, int32_t k,
-                  int32_t *per_thread, int32_t *light_zeros, double *pair_ms);
+                  int32_t *kernel, int32_t *per_thread, int32_t *light_zeros, double *pair_ms);
 
 /* ----------------------------------------------- stabilizer primitives (batched) */
 
