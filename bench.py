@@ -190,6 +190,8 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     cfg, projs, exact, k, norm, L = load_workload()
     gpu = backend.Backend(local_rank)
+    if args.no_tune:
+        gpu.set_option(backend.OPT_AUTOTUNE, 0)
     P = [backend.projector(ph, xs, zs, nq) for (ph, xs, zs, nq) in projs]
     samples, bins = (args.samples or cfg["samples"]), cfg["bins"]
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -228,7 +230,10 @@ def run_ours(args, rank, world, local_rank):
         step(i, backend.RNG_PHILOX)
         flush.zero_()
     barrier()
-    tuned = gpu.autotune(cfg["t"], P[0], [int(x) for x in L])  # done by the first warm-up step; reads the choice
+    if args.no_tune:
+        tuned = (0, 0, 0.0, 0)
+    else:  # done by the first warm-up step; this reads the choice
+        tuned = gpu.autotune(cfg["t"], P[0], [int(x) for x in L])
     kname = {0: "k_terms_tp (heavy and light launches)", 1: "k_terms_runs",
              2: "k_terms_tp (one launch per occupancy class)"}[tuned[3]]
     clocks = ClockSampler(local_rank)
@@ -305,8 +310,10 @@ def run_ours(args, rank, world, local_rank):
                    "last_query": {"numerator": result.get(0), "denominator": result.get(1)},
                    "l2": "flushed between steps (256 MiB write); hot data (codewords 512 KiB) is L2-resident",
                    "rng": "Philox on device (value); the C library's rand() sequence (e2e)",
-                   "launch": {"kernel": kname, "terms_per_thread": tuned[0], "light_zero_bound": tuned[1],
-                              "chosen_by": "csim_autotune on this query's G' and code"}},
+                   "launch": {"kernel": kname, "terms_per_thread": tuned[0] or "fixed rule (32)",
+                              "light_zero_bound": tuned[1] or "fixed rule (24)",
+                              "chosen_by": "fixed rules (--no-tune)" if args.no_tune else
+                              "csim_autotune on this query's G' and code"}},
         "e2e": {"value": e2e_pairs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
                 "d2h_bytes_per_step": d2h // args.steps, "ms_per_step": 1e3 * e2e_s / args.steps},
         "roofline": roofline,
@@ -682,6 +689,9 @@ def main():
                          "profiling cases, not bench lines")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-plain queries/s leg")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="fixed launch rules instead of the autotuner (profiling runs: a fixed launch sequence; on "
+                         "this workload the tuner picks the same launch)")
     ap.add_argument("--chain", default=None, metavar="SHOTSxBITS",
                     help="only time sampleQubits chains on the c4 circuit, plain vs batched (e.g. 16x4)")
     ap.add_argument("--chain-samples", type=int, default=None, help="L per conditional for --chain")
