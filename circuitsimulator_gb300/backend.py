@@ -32,6 +32,7 @@ EXE_PATH = os.path.join(PKG, "gpubackend")
 OPT_PAIR_KERNEL = 1
 OPT_PER_THREAD = 2
 OPT_AUTOTUNE = 3
+OPT_DIRECT_SLOTS = 4
 RNG_PHILOX = 0
 RNG_LIBC = 1
 SEED_CONTINUE = (1 << 64) - 1

@@ -74,12 +74,16 @@ extern "C" int csim_set_option(csim_ctx* ctx, int32_t option, int64_t value) {
     if (!ctx) return CSIM_ERR_ARG;
     switch (option) {
     case CSIM_OPT_PAIR_KERNEL:
-        if (value < 0 || value > 4) return fail(ctx, CSIM_ERR_ARG, "pair kernel must be 0..4");
+        if (value < 0 || value > 5) return fail(ctx, CSIM_ERR_ARG, "pair kernel must be 0..5");
         ctx->pair_kernel = (int)value;
         return CSIM_OK;
     case CSIM_OPT_PER_THREAD:
         if (value < 0 || value > 64) return fail(ctx, CSIM_ERR_ARG, "per-thread pairs must be 0 (by t) or 1..64");
         ctx->per_thread = (int)value;
+        return CSIM_OK;
+    case CSIM_OPT_DIRECT_SLOTS:
+        if (value < 0 || value > 64) return fail(ctx, CSIM_ERR_ARG, "direct slots must be 0 (by t) or 1..64");
+        ctx->direct_slots = (int)value;
         return CSIM_OK;
     case CSIM_OPT_AUTOTUNE:
         if (value != 0 && value != 1) return fail(ctx, CSIM_ERR_ARG, "autotune must be 0 or 1");
@@ -414,7 +418,7 @@ int stage_terms(csim_ctx* ctx, int t, int exact, const uint64_t* L, int k, int64
         key.push_back((uint64_t)k);
         key.push_back((uint64_t)t);
         key.push_back((uint64_t)tn->light);
-        key.push_back((uint64_t)tn->kernel);
+        key.push_back((uint64_t)(tn->kernel == 3 ? 0 : tn->kernel));  // the direct kernel walks kernel 0's order
         key.push_back((uint64_t)(tn->kernel ? tn->per_thread : 0));
         if (key != ctx->cw_key || !ctx->buf[kBufCwOrdered]) {
             std::vector<uint64_t> cw;
@@ -529,7 +533,7 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
     if (tp && count > 0) CKR(tune_for(ctx, t, &tn, P, L, k));  // before any draw: tuning leaves the streams as they are
     // the run kernel takes whole blocks of 64 runs
     if (tn.kernel == 1 && (exact || ((int64_t)1 << k) % (64 * (int64_t)tn.per_thread) != 0)) tn = default_tune(t);
-    if (tn.kernel == 2 && exact) tn = default_tune(t);
+    if ((tn.kernel == 2 || tn.kernel == 3) && exact) tn = default_tune(t);
     if (rng == CSIM_RNG_LIBC && seed != CSIM_SEED_CONTINUE) ctx->lr.seed((uint32_t)seed);
     if (rng == CSIM_RNG_PHILOX && seed != CSIM_SEED_CONTINUE) {
         ctx->philox_seed = seed;
@@ -557,6 +561,7 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
     uint64_t* dcw;
     csim_state* dphis;
     CKR(stage_terms(ctx, t, exact, L, k, 0, chi, &dcw, &dphis, /*ordered=*/true, &tn));
+    const int dsl = ctx->direct_slots > 0 ? std::min(t, ctx->direct_slots) : direct_slots(t);
     unsigned char* dscr = nullptr;
     size_t scr_bytes = 0;
     if (tp && tn.kernel == 1) {
@@ -579,6 +584,15 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
         csim::GState* dth = (csim::GState*)v;
         CKR(dbuf(ctx, kBufCode, c * 4, &v));
         int* dcode = (int*)v;
+        void* dcanon = nullptr;
+        int *dcode_dir = nullptr, *dcode_rest = nullptr;
+        if (tp && tn.kernel == 3) {
+            CKR(dbuf(ctx, kBufCanon, (size_t)c * csim::canon_bytes(), &dcanon));
+            CKR(dbuf(ctx, kBufCodeDirect, c * 4, &v));
+            dcode_dir = (int*)v;
+            CKR(dbuf(ctx, kBufCodeRest, c * 4, &v));
+            dcode_rest = (int*)v;
+        }
         const size_t nparts = (size_t)c * nchunks * 4;
         CKR(dbuf(ctx, kBufParts, nparts * sizeof(__int128), &v));
         __int128* dpart = (__int128*)v;
@@ -616,6 +630,11 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
             }
             if (csim::launch_project(launch_of(ctx), nr, sth, cs, P->nstabs, dpm, dpz, dpx, scode))
                 return fail(ctx, CSIM_ERR_CUDA, "projection launch failed");
+            if (tp && tn.kernel == 3 &&
+                csim::launch_canon(launch_of(ctx), sth, scode, cs, dsl,
+                                   (unsigned char*)dcanon + (size_t)s0 * csim::canon_bytes(), dcode_dir + s0,
+                                   dcode_rest + s0))
+                return fail(ctx, CSIM_ERR_CUDA, "pivot-form launch failed");
             if (first) CK(cudaEventRecord(ctx->ev[1], ctx->stream));
             first = false;
             __int128* spart = dpart + (size_t)s0 * nchunks * 4;
@@ -645,14 +664,22 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
                     rc |= csim::launch_terms_runs(launch_of(ctx), t, std::min(t, tn.light), dcw + jb, sth, scode, cs,
                                                   jb, chi - jb, pt, P2, spart, nchunks, jb / span, dscr, scr_bytes);
             } else if (tp) {
+                // direct kernel: every term of the states it takes; the rest (or all, for kernel 0) below
+                const int* rcode = scode;
+                if (tn.kernel == 3) {
+                    rc |= csim::launch_terms_direct(launch_of(ctx), t, dsl, dcw,
+                                                    (const unsigned char*)dcanon + (size_t)s0 * csim::canon_bytes(),
+                                                    dcode_dir + s0, cs, 0, chi, pt, P2, spart, nchunks, 0);
+                    rcode = dcode_rest + s0;
+                }
                 // terms [0, jb): every zero count; terms [jb, chi): at most tn.light zeros
                 const int64_t span = 64 * (int64_t)pt;
                 const int64_t jb = std::min(chi, (ctx->cw_split + span - 1) / span * span);
                 if (jb > 0)
-                    rc |= csim::launch_terms_tp(launch_of(ctx), t, t, dcw, sth, scode, cs, 0, jb, pt, P2, spart,
+                    rc |= csim::launch_terms_tp(launch_of(ctx), t, t, dcw, sth, rcode, cs, 0, jb, pt, P2, spart,
                                                 nchunks, 0, nullptr, nullptr, nullptr);
                 if (jb < chi)
-                    rc |= csim::launch_terms_tp(launch_of(ctx), t, tn.light, dcw + jb, sth, scode, cs, jb,
+                    rc |= csim::launch_terms_tp(launch_of(ctx), t, tn.light, dcw + jb, sth, rcode, cs, jb,
                                                 chi - jb, pt, P2, spart, nchunks, jb / span, nullptr, nullptr,
                                                 nullptr);
             } else {
@@ -770,7 +797,7 @@ int tune_run(csim_ctx* ctx, int t, const csim_projector* Pw, const uint64_t* Lw,
     };
     static const Cand cands[] = {{0, 16, 50}, {0, 16, 60}, {0, 16, 70}, {0, 32, 50}, {0, 32, 60}, {0, 32, 70},
                                  {1, 16, 50}, {1, 16, 55}, {1, 16, 60}, {1, 32, 50}, {1, 32, 55}, {1, 32, 60},
-                                 {2, 16, 60}, {2, 32, 60}};
+                                 {2, 16, 60}, {2, 32, 60}, {3, 16, 60}, {3, 32, 60}};
     for (const Cand& c : cands) {
         if (rc) break;
         if (c.kernel == 1 && chi % (64 * (int64_t)c.pt) != 0) continue;
@@ -841,6 +868,10 @@ int tune_for(csim_ctx* ctx, int t, TpTune* out, const csim_projector* P, const u
         r.light = std::min(t, (11 * t + 19) / 20);
     }
     if (ctx->pair_kernel == 4) r.kernel = 2;  // the block-prefix kernel, one launch per occupancy class
+    if (ctx->pair_kernel == 5 && r.kernel != 3) {  // the direct kernel, the rest on kernel 0 with its light bound
+        r.kernel = 3;
+        r.light = light_zeros(t);
+    }
     if (ctx->per_thread > 0) r.per_thread = ctx->per_thread;
     *out = r;
     return 0;

@@ -164,8 +164,12 @@ struct TpTune {
     int per_thread = 0;
     int light = 0;
     int kernel = 0;  // 0: block-prefix kernel (k_terms_tp), heavy and light launches; 1: run kernel
-                     // (k_terms_runs); 2: block-prefix kernel, one launch per occupancy class
+                     // (k_terms_runs); 2: block-prefix kernel, one launch per occupancy class; 3: direct
+                     // kernel (k_terms_direct), states with many non-pivot coordinates on kernel 0
 };
+// constraint slots per pair of the direct kernel: states with more non-pivot
+// coordinates (n - k) than this go to the block-prefix kernel
+inline int direct_slots(int t) { return std::min(t, 8); }
 inline TpTune default_tune(int t) {
     TpTune r;
     r.per_thread = auto_per_thread(t);
@@ -358,7 +362,8 @@ inline double sqrt_half_power(int c) {  // projfactor of innerprod.c:104-111: c 
 enum BufId {
     kBufA, kBufB, kBufEps, kBufP, kBufM, kBufXi, kBufZeta, kBufAlpha, kBufCode, kBufWords, kBufOffsets,
     kBufCum, kBufCodewords, kBufAcc, kBufAccDiag, kBufPhis, kBufIdx, kBufConsumed, kBufPm, kBufPz, kBufPx,
-    kBufL, kBufParts, kBufPartsDiag, kBufCwOrdered, kBufRunScratch, kNumBufs
+    kBufL, kBufParts, kBufPartsDiag, kBufCwOrdered, kBufRunScratch, kBufCanon, kBufCodeDirect, kBufCodeRest,
+    kNumBufs
 };
 
 class Engine;                     // csim_engine.cpp: the batched query engine
@@ -388,6 +393,7 @@ struct csim_ctx {
     std::vector<int64_t> cw_starts;    // and the first index of each class
     // autotuner (CSIM_OPT_AUTOTUNE): the tuned launch parameters live in a
     // process-wide table per device (csim_host.cpp), filled a t bucket at a time
+    int direct_slots = 0;  // CSIM_OPT_DIRECT_SLOTS; 0 = direct_slots(t)
     int autotune = 1;
     bool tuning = false;      // a tuning pass is running on this context (its trials use `trial`)
     csim_host::TpTune trial;  // the parameters of the trial in progress

@@ -56,6 +56,19 @@ int64_t terms_tp_blocks(int64_t nj, int per_thread);
 // qubits and codewords of up to gmax zeros (-1 if the query fails)
 int terms_tp_occupancy(int nmax, int gmax);
 
+// the direct kernel (csim_terms_tp.cu).  launch_canon: each live state in
+// pivot coordinates (canon_bytes() per state in `canon`); states with n - k >
+// dslots get code_direct = -1 and keep their code in code_rest (for the
+// block-prefix kernel), the others the reverse.  launch_terms_direct: all pairs
+// of the states with code >= 0 against codewords [j0, j0 + nj), partial sums as
+// launch_terms_tp's (only live states write theirs).
+size_t canon_bytes();
+int launch_canon(const Launch& L, const GState* theta, const int* code, int64_t ntheta, int dslots, void* canon,
+                 int* code_direct, int* code_rest);
+int launch_terms_direct(const Launch& L, int nmax, int dslots, const uint64_t* codewords, const void* canon,
+                        const int* code, int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P,
+                        __int128* part, int64_t part_stride, int64_t part_base);
+
 // the run kernel (csim_terms_tp.cu): codewords [j0, j0 + nj) in run order
 // (csim_host::run_ordered_codewords), runs of per_thread codewords, partial
 // sums as launch_terms_tp's; gmax bounds the zeros of every codeword below its

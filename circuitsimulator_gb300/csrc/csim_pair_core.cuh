@@ -934,6 +934,438 @@ CSIM_HD inline void pair_from_run(bool valid, int n, const RunState& rs, const P
 #undef S64
 #undef SG
 
+// ---------------------------------------------------------------- direct restriction
+// <theta|phi_x> = 2^{-(k + |x|)/2} sum over {u : h + uG has no 1 outside x} of
+// w^{q(u)}: an exponential sum of theta's form over the u whose image vanishes
+// on x's zero positions.  canon_theta rewrites theta once so that its
+// variables are k pivot coordinates P of the affine space (the image is
+// y_P = v, the other coordinates affine in v), the form re-expressed in v by
+// the same elementary substitutions the reference's basis changes make
+// (stabilizer.c:129-177).  A pair then needs no shrink for a zero of x at a
+// pivot coordinate: that variable is simply absent.  Only the zeros of x at
+// the d = n - k non-pivot coordinates are constraints (md_shrink), after which
+// the form over the remaining variables goes to the exponential sum
+// (md_exp_sum).  Variables keep their coordinate index (rows of J are indexed
+// by coordinate; a mask F marks the live ones), so nothing is compacted.
+// The result is the same complex number as innerProductExact's; eps and p are
+// equal, m is equal mod 8 (the reference's unreduced m depends on its basis).
+struct Canon {
+    uint64_t P;       // pivot coordinates: the variables
+    uint64_t D1, D2;  // the form's D, at each variable's coordinate
+    uint64_t bm;      // right-hand side bit of each non-pivot coordinate's constraint
+    int Q, k, n, pad;
+};
+
+// (D1, D2) += (d1, d2) on the bits of u, with the carry into D2 (D = 2 (2 D2 + D1) mod 8)
+CSIM_HD inline void add_D64(uint64_t& D1, uint64_t& D2, uint64_t u, int d1, int d2) {
+    const uint64_t a1 = d1 ? u : 0ull, a2 = d2 ? u : 0ull, c = D1 & a1;
+    D1 ^= a1;
+    D2 ^= a2 ^ c;
+}
+
+// theta (n qubits, k, Q, h, D1, D2, G rows, J rows as in csim_state) in pivot
+// coordinates.  Jc[c], acol[c] for c < n: J row of variable c (0 for a
+// non-pivot c), and for a non-pivot c the mask of variables its coordinate
+// depends on (0 for a pivot).  Sequential (one thread); run once per theta.
+CSIM_HD inline void canon_theta(int n, int k, int Q, uint64_t h, uint64_t D1, uint64_t D2, const uint64_t* G,
+                                const uint64_t* J, uint64_t* Jc, uint64_t* acol, Canon& out) {
+    const uint64_t nm = lowmask(n), km = lowmask(k);
+    uint64_t g[64], Jv[64];
+    int piv[64];
+    D1 &= km;
+    D2 &= km;
+    for (int a = 0; a < k; a++) {
+        g[a] = G[a] & nm;
+        Jv[a] = J[a] & km;
+    }
+    // Gauss-Jordan on the rows of G.  Row b += row a is the substitution
+    // u_a = u'_a + u'_b; all rows b of a pivot step at once form the rank-two
+    // update R J R^T with U = B (rows in B get J_a, rows in C get B), with
+    // D_b += D_a + 4 J_ab (tp_shrink's update without the swap).
+    for (int a = 0; a < k; a++) {
+        const int pc = g[a] ? hd_ffs64(g[a]) - 1 : 0;
+        piv[a] = pc;
+        uint64_t B = 0ull;
+        for (int b = 0; b < k; b++)
+            if (b != a && getbit(g[b], pc)) B |= bit1(b);
+        if (!B) continue;
+        for (int b = 0; b < k; b++)
+            if (getbit(B, b)) g[b] ^= g[a];
+        const uint64_t Ja = Jv[a], C = Ja ^ (getbit(Ja, a) ? B : 0ull);
+        for (int x = 0; x < k; x++) Jv[x] ^= (getbit(B, x) ? Ja : 0ull) ^ (getbit(C, x) ? B : 0ull);
+        add_D64(D1, D2, B, getbit(D1, a), getbit(D2, a));
+        D2 ^= B & Ja;
+    }
+    // shift v = u + w, w_a = h at a's pivot, so that y_{piv a} = v_a
+    uint64_t wv = 0ull;
+    for (int a = 0; a < k; a++)
+        if (getbit(h, piv[a])) {
+            wv |= bit1(a);
+            Q = (Q + 2 * (2 * getbit(D2, a) + getbit(D1, a))) & 7;
+            D2 ^= (uint64_t)getbit(D1, a) << a;  // D_a -> -D_a
+            D2 ^= Jv[a] & ~bit1(a) & km;          // D_b += 4 J_ab
+        }
+    // to coordinate indexing
+    uint64_t P = 0ull;
+    for (int a = 0; a < k; a++) P |= bit1(piv[a]);
+    auto map = [&](uint64_t v) {
+        uint64_t r = 0ull;
+        for (int a = 0; a < k; a++)
+            if (getbit(v, a)) r |= bit1(piv[a]);
+        return r;
+    };
+    for (int c = 0; c < 64; c++) {
+        Jc[c] = 0ull;
+        acol[c] = 0ull;
+    }
+    for (int a = 0; a < k; a++) Jc[piv[a]] = map(Jv[a]);
+    uint64_t bm = 0ull;
+    for (int c = 0; c < n; c++) {
+        if (getbit(P, c)) continue;
+        uint64_t av = 0ull;
+        for (int a = 0; a < k; a++)
+            if (getbit(g[a], c)) av |= bit1(a);
+        acol[c] = map(av);
+        if ((getbit(h, c) ^ (hd_popc64(wv & av) & 1)) != 0) bm |= bit1(c);
+    }
+    out.P = P;
+    out.D1 = map(D1);
+    out.D2 = map(D2);
+    out.bm = bm;
+    out.Q = Q;
+    out.k = k;
+    out.n = n;
+    out.pad = 0;
+}
+
+// whole row r of J with F-indexed rows (rows below 32 keep their low halves;
+// bit y >= 32 of such a row is bit r of row y, for y < KP)
+template <class W>
+CSIM_HD inline W md_read_row(const PairMem& M, int r, int KP) {
+    if (sizeof(W) == 4) return (W)R32(r);
+    if (r >= 32) return (W)R64(r);
+    return (W)((uint64_t)R32(r) | (gather_hi(M, r, KP) << 32));
+}
+
+// Rows [0, KX) of J: row x ^= (U_x ? Ji : 0) ^ (C_x ? U : 0), the rank-two
+// update R J R^T of the substitution of variable i, rows below 32 in 32 bits
+template <class W>
+CSIM_HD inline void md_rank2(const PairMem& M, int KX, W Ji, W U, W C) {
+    using T = WordTraits<W>;
+    const W ru = wbrev(U), rc = wbrev(C);
+    {
+        const uint32_t Ji32 = (uint32_t)Ji, U32 = (uint32_t)U;
+        const int sh = T::bits - 32;
+        uint32_t cu = (uint32_t)(ru >> sh), cc = (uint32_t)(rc >> sh);
+        const int K32 = KX < 32 ? KX : 32;
+        for (int x = 0; x < K32; x += 4) {
+            U32x4* pr = reinterpret_cast<U32x4*>(&R32(x));
+            U32x4 v = *pr;
+            v.a ^= (Ji32 & topmask(cu)) ^ (U32 & topmask(cc));
+            v.b ^= (Ji32 & topmask(cu << 1)) ^ (U32 & topmask(cc << 1));
+            v.c ^= (Ji32 & topmask(cu << 2)) ^ (U32 & topmask(cc << 2));
+            v.d ^= (Ji32 & topmask(cu << 3)) ^ (U32 & topmask(cc << 3));
+            cu <<= 4;
+            cc <<= 4;
+            *pr = v;
+        }
+    }
+    if (sizeof(W) == 8) {
+        W cu = (W)((uint64_t)ru << 32), cc = (W)((uint64_t)rc << 32);
+        for (int x = 32; x < KX; x += 2) {
+            U64x2* pr = reinterpret_cast<U64x2*>(&R64(x));
+            U64x2 v = *pr;
+            v.a ^= (uint64_t)((Ji & topmask(cu)) ^ (U & topmask(cc)));
+            v.b ^= (uint64_t)((Ji & topmask((W)(cu << 1))) ^ (U & topmask((W)(cc << 1))));
+            cu <<= 2;
+            cc <<= 2;
+            *pr = v;
+        }
+    }
+}
+
+// One constraint (slot q of M's G slots: a mask of variables, right-hand side
+// bit q of s.h): sum over its live variables of v = rhs.  Substitutes its
+// highest live variable i by the others (rows of J, D, and the later slots'
+// masks and right-hand sides), adds the shift when rhs = 1, and drops i from
+// F.  Returns 0 EMPTY (no live variable, rhs 1), 1 SAME (none, rhs 0), 2
+// SUCCESS; 1 when inactive.  All lanes of a warp call it together.
+template <class W>
+CSIM_HD inline int md_shrink(PairRegs& s, uint64_t& F, const PairMem& M, int q, int nz, bool act) {
+    using T = WordTraits<W>;
+    const W S = act ? (W)(RG(q) & F) : (W)0;
+    const int beta = act ? getbit(s.h, q) : 0;
+    const bool upd = S != (W)0;
+    const int i = upd ? T::bits - 1 - T::clz(S) : 0;
+    const W U = S & ~wbit<W>(i);
+    const W mi = wbit<W>(i);
+    const int KP = upd ? 64 - hd_clz64(F) : 0;
+    // later constraints: a_c += (a_c)_i U; rhs_c += (a_c)_i rhs
+    const int nrem = upd ? nz - 1 - q : 0;
+    const int NR = uniform_max(nrem);
+    uint64_t hflip = 0ull;
+    for (int t = 0; t < NR; t++) {
+        if (t < nrem) {
+            const int c = q + 1 + t;
+            uint64_t g = RG(c);
+            const bool gi = getbit(g, i) != 0;
+            g ^= (uint64_t)U & (gi ? ~0ull : 0ull);
+            RG(c) = g;
+            if (gi) hflip |= bit1(c);
+        }
+    }
+    if (beta) s.h ^= hflip;
+    const W Ji = upd ? md_read_row<W>(M, i, KP) : (W)0;
+    const W C = Ji ^ (wget<W>(Ji, i) ? U : (W)0);  // new row (and column) i
+    const int KX = uniform_max(KP);
+    if (upd) md_rank2<W>(M, KX, Ji, U, C);
+    if (upd) {
+        uint64_t D1 = s.D1, D2 = s.D2;
+        add_D64(D1, D2, (uint64_t)U, getbit(D1, i), getbit(D2, i));
+        D2 ^= (uint64_t)(U & Ji);
+        if (beta) {
+            s.Q = (s.Q + 2 * (2 * getbit(D2, i) + getbit(D1, i))) & 7;
+            D2 ^= (uint64_t)C & F & ~(uint64_t)mi;
+        }
+        s.D1 = D1;
+        s.D2 = D2;
+        F &= ~(uint64_t)mi;
+        return 2;
+    }
+    return act ? 1 - beta : 1;
+}
+// exponentialSumExact (stabilizer.c:300-481) of the form over the live
+// variables F (coordinate-indexed rows, nothing compacted): first the
+// substitution that leaves one variable (sidx, the lowest with D odd) with D
+// odd, then monomers and dimers taken from the highest live row down, so the
+// rows still in play shrink towards row 0.  W0/W1 and their combination as in
+// tp_exp_sum.  `act` as for md_shrink.
+template <class W>
+CSIM_HD inline void md_exp_sum(PairRegs& s, const PairMem& M, uint64_t F, bool act, int& eps, int& p, int& m,
+                               int& err) {
+    using T = WordTraits<W>;
+    const W Fw = act ? (W)F : (W)0;
+    uint64_t D1 = s.D1, D2 = s.D2;
+    const W Sm = (W)D1 & Fw;
+    int sidx = -1;
+    int KP = Fw ? 64 - hd_clz64((uint64_t)Fw) : 0;
+    {
+        const bool upd = Sm != (W)0;
+        const int a = upd ? T::ffs(Sm) - 1 : 0;
+        const W U = Sm & ~wbit<W>(a);
+        const W Ja = upd ? md_read_row<W>(M, a, KP) : (W)0;
+        const W C = Ja ^ (wget<W>(Ja, a) ? U : (W)0);
+        const int KX = uniform_max(upd ? KP : 0);
+        if (upd && U != (W)0) md_rank2<W>(M, KX, Ja, U, C);
+        if (upd) {
+            add_D64(D1, D2, (uint64_t)U, getbit(D1, a), getbit(D2, a));
+            D2 ^= (uint64_t)(U & Ja);
+            sidx = a;
+        }
+    }
+    W E = Fw & ~(sidx >= 0 ? wbit<W>(sidx) : (W)0);
+    // in 64-bit mode the row sidx >= 32 stays updated: its bits are bit sidx of the rows below 32
+    const W keep = (sizeof(W) == 8 && sidx >= 32) ? wbit<W>(sidx) : (W)0;
+    WAcc w0 = {0, 0, 0}, w1 = {0, 0, 0};
+    const bool any = E != (W)0;
+    const int NE = uniform_max(T::popc(E));
+    for (int it = 0; it < NE; it++) {
+        if (uniform_max(E != (W)0 ? 1 : 0) == 0) break;
+        const bool live = E != (W)0;
+        KP = live ? 64 - hd_clz64((uint64_t)(E | keep | (sidx >= 0 ? wbit<W>(sidx) : (W)0))) : 0;
+        const int a = live ? T::bits - 1 - T::clz(E) : 0;
+        const W ra = live ? md_read_row<W>(M, a, KP) : (W)0;
+        const W K = ra & E & ~wbit<W>(a);
+        const bool dimer = K != (W)0;
+        const int b = dimer ? T::bits - 1 - T::clz(K) : 0;
+        const W rb = dimer ? md_read_row<W>(M, b, KP) : (W)0;
+        const int Da = 2 * (2 * getbit(D2, a) + getbit(D1, a));
+        if (live && !dimer) {  // monomer {a}
+            tp_factor_mono(w0, Da, err);
+            if (sidx >= 0) tp_factor_mono(w1, Da + 4 * wget<W>(ra, sidx), err);
+        }
+        if (dimer) {  // dimer {a, b}
+            const int Db = 2 * (2 * getbit(D2, b) + getbit(D1, b));
+            tp_factor_dimer(w0, Da, Db, err);
+            if (sidx >= 0) tp_factor_dimer(w1, Da + 4 * wget<W>(ra, sidx), Db + 4 * wget<W>(rb, sidx), err);
+        }
+        const W Ep = dimer ? (E & ~wbit<W>(a) & ~wbit<W>(b)) : (E & ~wbit<W>(a));
+        const W vb = dimer ? (ra & Ep) : (W)0, va = dimer ? (rb & Ep) : (W)0;
+        const bool upd = (vb | va) != (W)0;
+        const int jaa = wget<W>(ra, a), jbb = wget<W>(rb, b), jab = wget<W>(ra, b);
+        const W Cb = rb ^ (jbb ? vb : (W)0) ^ (jab ? va : (W)0);
+        const W Ca = ra ^ (jab ? vb : (W)0) ^ (jaa ? va : (W)0);
+        {
+            const W zm = upd ? (Ep | keep) : (W)0;
+            const int lo = zm ? T::ffs(zm) - 1 : T::bits, hi = zm ? T::bits - T::clz(zm) : 0;
+            const int X0 = uniform_min(lo) & ~3, X1 = uniform_max(hi);
+            const W rvb = wbrev(vb), rva = wbrev(va), rcb = wbrev(Cb), rca = wbrev(Ca);
+            {
+                const int sh = T::bits - 32;
+                const int s0 = X0 < 32 ? X0 : 0;
+                const uint32_t rb32 = (uint32_t)rb, ra32 = (uint32_t)ra, vb32 = (uint32_t)vb, va32 = (uint32_t)va;
+                uint32_t cvb = (uint32_t)(rvb >> sh) << s0, cva = (uint32_t)(rva >> sh) << s0,
+                         ccb = (uint32_t)(rcb >> sh) << s0, cca = (uint32_t)(rca >> sh) << s0;
+                const int X1a = X1 < 32 ? X1 : 32;
+                for (int x = X0; x < X1a; x += 4) {
+                    U32x4* pr = reinterpret_cast<U32x4*>(&R32(x));
+                    U32x4 v = *pr;
+                    v.a ^= (rb32 & topmask(cvb)) ^ (ra32 & topmask(cva)) ^ (vb32 & topmask(ccb)) ^
+                           (va32 & topmask(cca));
+                    v.b ^= (rb32 & topmask(cvb << 1)) ^ (ra32 & topmask(cva << 1)) ^ (vb32 & topmask(ccb << 1)) ^
+                           (va32 & topmask(cca << 1));
+                    v.c ^= (rb32 & topmask(cvb << 2)) ^ (ra32 & topmask(cva << 2)) ^ (vb32 & topmask(ccb << 2)) ^
+                           (va32 & topmask(cca << 2));
+                    v.d ^= (rb32 & topmask(cvb << 3)) ^ (ra32 & topmask(cva << 3)) ^ (vb32 & topmask(ccb << 3)) ^
+                           (va32 & topmask(cca << 3));
+                    cvb <<= 4;
+                    cva <<= 4;
+                    ccb <<= 4;
+                    cca <<= 4;
+                    *pr = v;
+                }
+            }
+            if (sizeof(W) == 8) {
+                const int x0 = X0 > 32 ? (X0 & ~1) : 32;
+                const int s1 = x0 & (T::bits - 1);
+                W cvb = rvb << s1, cva = rva << s1, ccb = rcb << s1, cca = rca << s1;
+                for (int x = x0; x < X1; x += 2) {
+                    U64x2* pr = reinterpret_cast<U64x2*>(&R64(x));
+                    U64x2 v = *pr;
+                    v.a ^= (uint64_t)((rb & topmask(cvb)) ^ (ra & topmask(cva)) ^ (vb & topmask(ccb)) ^
+                                      (va & topmask(cca)));
+                    v.b ^= (uint64_t)((rb & topmask((W)(cvb << 1))) ^ (ra & topmask((W)(cva << 1))) ^
+                                      (vb & topmask((W)(ccb << 1))) ^ (va & topmask((W)(cca << 1))));
+                    cvb <<= 2;
+                    cva <<= 2;
+                    ccb <<= 2;
+                    cca <<= 2;
+                    *pr = v;
+                }
+            }
+        }
+        if (upd) {
+            const int db1 = getbit(D1, b), db2 = getbit(D2, b), da1 = getbit(D1, a), da2 = getbit(D2, a);
+            add_D64(D1, D2, (uint64_t)vb, db1, db2);
+            add_D64(D1, D2, (uint64_t)va, da1, da2);
+            W flip = (vb & rb) ^ (va & ra);
+            if (jab) flip ^= vb & va;
+            D2 ^= (uint64_t)flip;
+        }
+        if (live) E = Ep;
+    }
+    if (!act) return;
+    if (Fw == (W)0) {  // Wsigma's k == 0 case
+        eps = 1;
+        p = 0;
+        m = s.Q;
+        return;
+    }
+    const int tM0 = s.Q, tM1 = s.Q + (sidx >= 0 ? 2 * (2 * getbit(D2, sidx) + getbit(D1, sidx)) : 0);
+    const int e0 = !w0.zero, p0 = w0.zero ? 0 : w0.p, m0 = w0.zero ? 0 : (any ? (tM0 + w0.m) % 8 : tM0);
+    if (sidx < 0) {
+        eps = e0;
+        p = p0;
+        m = m0;
+        return;
+    }
+    const int e1 = !w1.zero, p1 = w1.zero ? 0 : w1.p, m1 = w1.zero ? 0 : (any ? (tM1 + w1.m) % 8 : tM1);
+    if (e0 == 0) {
+        eps = e1;
+        p = p1;
+        m = m1;
+        return;
+    }
+    if (e1 == 0) {
+        eps = e0;
+        p = p0;
+        m = m0;
+        return;
+    }
+    if (p0 != p1 || ((m1 - m0) % 2) != 0) {
+        err |= kErrExpSum;
+        return;
+    }
+    int ee, pp = 0, mm = 0;
+    partial_gamma(m1 - m0, ee, pp, mm, err);
+    eps = ee;
+    if (!ee) {
+        p = 0;
+        m = 0;
+    } else {
+        p = pp + p0;
+        m = mm + m0 % 8;
+    }
+}
+
+// One pair by direct restriction: theta in pivot coordinates (cs, Jc rows,
+// acol non-pivot masks), codeword x; working memory M with at least as many G
+// slots as x has zeros at non-pivot coordinates (dslots).  Same eps and p as
+// pair_l, m equal mod 8.  All lanes of a warp call it together.
+CSIM_HD inline void pair_direct(bool valid, int n, const Canon& cs, const uint64_t* Jc, const uint64_t* acol,
+                                uint64_t x, const PairMem& M, int& eps, int& p, int& m, int& err, int dslots, int k0) {
+    const uint64_t nm = lowmask(n);
+    uint64_t F = x & cs.P;
+    const uint64_t N = ~x & ~cs.P & nm;
+    if (valid && hd_popc64(N) > dslots) {
+        err |= kErrRange;
+        valid = false;
+    }
+    PairRegs s;
+    s.k = 0;
+    s.Q = cs.Q;
+    s.D1 = cs.D1;
+    s.D2 = cs.D2;
+    // J rows of every coordinate below the highest live one (whole 16-byte units)
+    const int KP = valid && F ? 64 - hd_clz64(F) : 0;
+    const int K = uniform_max(KP);
+    for (int u = 0; 4 * u < (K < 32 ? K : 32); u++)
+        if (4 * u < KP) {
+            U32x4 v;
+            v.a = (uint32_t)Jc[4 * u];
+            v.b = (uint32_t)Jc[4 * u + 1];
+            v.c = (uint32_t)Jc[4 * u + 2];
+            v.d = (uint32_t)Jc[4 * u + 3];
+            *reinterpret_cast<U32x4*>(&R32(4 * u)) = v;
+        }
+    for (int r = 32; r < K; r += 2)
+        if (r < KP) {
+            U64x2 v;
+            v.a = Jc[r];
+            v.b = Jc[r + 1];
+            *reinterpret_cast<U64x2*>(&R64(r)) = v;
+        }
+    // the constraints: x's zeros at non-pivot coordinates, descending
+    int nz = 0;
+    uint64_t hz = 0ull;
+    for (uint64_t zz = valid ? N : 0ull; zz; nz++) {
+        const int c = 63 - hd_clz64(zz);
+        zz &= ~bit1(c);
+        RG(nz) = acol[c];
+        hz |= (uint64_t)getbit(cs.bm, c) << nz;
+    }
+    s.h = hz;
+    eps = 0;
+    p = 0;
+    m = 0;
+    bool alive = valid;
+    const int NZ = uniform_max(nz);
+    for (int it = 0; it < NZ; it++) {
+        const bool act = alive && it < nz;
+        const bool wide = uniform_max(act && F ? 64 - hd_clz64(F) : 0) > 32;
+        const int r = wide ? md_shrink<uint64_t>(s, F, M, it, nz, act) : md_shrink<uint32_t>(s, F, M, it, nz, act);
+        if (act && r == 0) alive = false;
+    }
+    if (uniform_max(alive && F ? 64 - hd_clz64(F) : 0) > 32) md_exp_sum<uint64_t>(s, M, F, alive, eps, p, m, err);
+    else md_exp_sum<uint32_t>(s, M, F, alive, eps, p, m, err);
+    if (alive) p -= k0 + hd_popc64(x);
+    else {
+        eps = 0;
+        p = 0;
+        m = 0;
+    }
+}
+
 // Top bits of [0, n) on which codewords that differ in the bits `dis` agree
 CSIM_HD inline uint64_t agree_top(uint64_t dis, int n) {
     const uint64_t d = dis & lowmask(n);

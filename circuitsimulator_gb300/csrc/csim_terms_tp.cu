@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
             if ((tid & 31) == 0)
                 for (int q = 0; q < 4; q++) sh.red[tid >> 5][q] = z[q];
             __syncthreads();
-            if (tid < 4) {
+            if (tid < 4 && sh.live) {  // a dead state's partials stay zero (another launch may own them)
                 __int128 acc = 0;
                 for (int w = 0; w < kTP / 32; w++) acc += sh.red[w][tid];
                 part[4 * (a * part_stride + part_base + cb) + tid] = acc;
@@ -148,6 +148,144 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
     }
     e = (int)__reduce_or_sync(kFull, (unsigned)e);
     if (e && (tid & 31) == 0) atomicOr(err, e);
+}
+
+// ---------------------------------------------------------------- direct restriction
+// k_canon: one thread per state, theta in pivot coordinates (pc::canon_theta);
+// states whose d = n - k exceeds `dslots` are left to the block-prefix kernel
+// (code_direct < 0), the others to the direct kernel (code_rest < 0).
+struct CanonG {
+    pc::Canon cs;
+    uint64_t Jc[64];
+    uint64_t acol[64];
+};
+
+__global__ void __launch_bounds__(64) k_canon(const GState* theta, const int* code, int64_t ntheta, int dslots,
+                                               CanonG* out, int* code_direct, int* code_rest) {
+    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= ntheta) return;
+    const GState* g = theta + a;
+    const int c = code ? code[a] : 0;
+    const int n = g->n, k = g->k;
+    const bool direct = c >= 0 && n - k <= dslots && n >= 1 && n <= 64 && k >= 0 && k <= n;
+    code_direct[a] = direct ? c : -1;
+    code_rest[a] = direct ? -1 : c;
+    if (!direct) return;
+    uint64_t G[64], J[64];
+    for (int r = 0; r < k; r++) {
+        G[r] = g->G[r];
+        J[r] = g->J[r];
+    }
+    pc::canon_theta(n, k, g->Q, g->h, g->D1, g->D2, G, J, out[a].Jc, out[a].acol, out[a].cs);
+}
+
+// The direct kernel: one thread per (theta, term) pair like k_terms_tp, each
+// pair by pc::pair_direct from its state's pivot form, which a block loads
+// into shared memory once per item.  The per-pair working memory needs no
+// G slot per zero, only dslots constraint slots.
+struct DirectShared {
+    pc::Canon cs;
+    int live, pad0, pad1, pad2;
+    __int128 red[kTP / 32][4];
+};
+
+__global__ void __launch_bounds__(kTP) k_terms_direct(const uint64_t* codewords, const CanonG* canon, const int* code,
+                                                      int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P,
+                                                      int nmax, int dslots, __int128* part, int64_t part_stride,
+                                                      int64_t part_base, int* err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    DirectShared& sh = *reinterpret_cast<DirectShared*>(smem_raw);
+    uint64_t* const sJ = reinterpret_cast<uint64_t*>(smem_raw + sizeof(DirectShared));  // 64 rows, then 64 masks
+    uint64_t* const sA = sJ + 64;
+    unsigned char* const pair_base = smem_raw + sizeof(DirectShared) + 2 * 64 * 8;
+    const int tid = threadIdx.x;
+    int e = 0;
+    const pc::PairMem mem = pc::pair_mem(pair_base, nmax, kTP, tid);
+    const int64_t span = (int64_t)kTP * per_thread;
+    const int64_t nblk = (nj + span - 1) / span;
+    const int64_t items = ntheta * nblk;
+    for (int64_t item = blockIdx.x; item < items; item += gridDim.x) {
+        const int64_t a = item / nblk, cb = item % nblk;
+        __syncthreads();  // previous item's use of the shared state is over
+        if (tid == 0) {
+            sh.live = code[a] >= 0;
+            sh.cs = canon[a].cs;
+        }
+        sJ[tid] = canon[a].Jc[tid];
+        sA[tid] = canon[a].acol[tid];
+        __syncthreads();
+        __int128 z[4] = {0, 0, 0, 0};
+        const int n = sh.cs.n;
+        if (sh.live && n > nmax) e |= kErrArg;
+        if (sh.live && n >= 1 && n <= nmax) {
+            const int64_t jb = j0 + cb * span;
+            for (int r = 0; r < per_thread; r++) {
+                const int64_t j = jb + tid + (int64_t)kTP * r;
+                const bool valid = j < j0 + nj;
+                if (__all_sync(kFull, !valid)) break;  // warp-uniform exit
+                const uint64_t x = valid ? codewords[j - j0] : 0ull;
+                int eps = 0, pp = 0, mm = 0;
+                pc::pair_direct(valid, n, sh.cs, sJ, sA, x, mem, eps, pp, mm, e, dslots, sh.cs.k);
+                if (valid) pc::zacc(z, eps, pp, mm, P, e);
+            }
+        }
+        if (part) {
+            for (int q = 0; q < 4; q++)
+                for (int o = 16; o > 0; o >>= 1) z[q] += shfl_xor_i128(z[q], o);
+            if ((tid & 31) == 0)
+                for (int q = 0; q < 4; q++) sh.red[tid >> 5][q] = z[q];
+            __syncthreads();
+            if (tid < 4 && sh.live) {
+                __int128 acc = 0;
+                for (int w = 0; w < kTP / 32; w++) acc += sh.red[w][tid];
+                part[4 * (a * part_stride + part_base + cb) + tid] = acc;
+            }
+        }
+    }
+    e = (int)__reduce_or_sync(kFull, (unsigned)e);
+    if (e && (tid & 31) == 0) atomicOr(err, e);
+}
+
+size_t canon_bytes() { return sizeof(CanonG); }
+
+int launch_canon(const Launch& L, const GState* theta, const int* code, int64_t ntheta, int dslots, void* canon,
+                 int* code_direct, int* code_rest) {
+    if (ntheta <= 0) return 0;
+    const int64_t blocks = (ntheta + 63) / 64;
+    k_canon<<<(int)blocks, 64, 0, L.stream>>>(theta, code, ntheta, dslots, (CanonG*)canon, code_direct, code_rest);
+    (*L.launches)++;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+namespace {
+size_t terms_direct_smem(int nmax, int dslots) {
+    return sizeof(DirectShared) + 2 * 64 * 8 + pc::pair_mem_bytes(nmax, dslots, kTP);
+}
+}  // namespace
+
+int launch_terms_direct(const Launch& L, int nmax, int dslots, const uint64_t* codewords, const void* canon,
+                        const int* code, int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P,
+                        __int128* part, int64_t part_stride, int64_t part_base) {
+    if (ntheta <= 0 || nj <= 0) return 0;
+    if (nmax < 1 || nmax > 64 || dslots < 0 || dslots > nmax || per_thread < 1 || !part || !canon || !code)
+        return -1;
+    const int64_t span = (int64_t)kTP * per_thread;
+    const int64_t nblk = (nj + span - 1) / span;
+    if (part_stride < part_base + nblk) return -1;
+    if (cudaFuncSetAttribute(k_terms_direct, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)terms_direct_smem(64, 64)) != cudaSuccess)
+        return -1;
+    const size_t smem = terms_direct_smem(nmax, dslots);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_terms_direct, kTP, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    int64_t grid = (int64_t)L.num_sms * per_sm;
+    if (grid > ntheta * nblk) grid = ntheta * nblk;
+    k_terms_direct<<<(int)grid, kTP, smem, L.stream>>>(codewords, (const CanonG*)canon, code, ntheta, j0, nj,
+                                                        per_thread, P, nmax, dslots, part, part_stride, part_base,
+                                                        L.d_err);
+    (*L.launches)++;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 // ---------------------------------------------------------------- per-thread runs

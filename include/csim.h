@@ -124,8 +124,11 @@ int csim_rng_position(csim_ctx *ctx, uint64_t seed, uint64_t first);
 #define CSIM_OPT_PAIR_KERNEL 1 /* |L>-term pairs: 0 = one thread per pair, the tuner's kernel (default); 1 = one warp
                                   per pair; 2 = one thread per pair, block-shared top-bit shrinks; 3 = one thread per
                                   pair, per-thread runs of codewords with shared top-bit shrinks; 4 = as 2, one
-                                  launch per occupancy class of the codewords' zero counts */
+                                  launch per occupancy class of the codewords' zero counts; 5 = one thread per
+                                  pair, direct restriction of each state's pivot form */
 #define CSIM_OPT_PER_THREAD 2  /* |L>-term pairs per thread per work item of the thread-per-pair kernel (1..64; 0 = by t) */
+#define CSIM_OPT_DIRECT_SLOTS 4 /* direct kernel: constraint slots per pair (1..64; 0 = min(t, 8)); states with more
+                                   non-pivot coordinates (n - k) go to the block-prefix kernel */
 #define CSIM_OPT_AUTOTUNE 3    /* 1 (default): tuned thread-per-pair launches, a t bucket tuned on first use; 0: fixed rules */
 int csim_set_option(csim_ctx *ctx, int32_t option, int64_t value);
 

@@ -158,3 +158,26 @@ extern "C" int tp_host_runs(const csim_state* theta, int ntheta, const uint64_t*
     }
     return err;
 }
+
+// The direct-restriction path (canon_theta once per theta, pair_direct per
+// pair): eps, p and m mod 8 of every pair, for comparison with the oracle.
+extern "C" int tp_host_direct(const csim_state* theta, int ntheta, const uint64_t* xs, int nx, int* eps, int* p,
+                              int* m) {
+    using namespace csim::pc;
+    int err = 0;
+    alignas(16) uint32_t wJ32[32];
+    alignas(16) uint64_t wJ64[34];
+    alignas(16) uint64_t wG[64];
+    const PairMem mem{wJ32, wJ64, wG, 1};
+    uint64_t Jc[64], acol[64];
+    for (int a = 0; a < ntheta; a++) {
+        const csim_state& th = theta[a];
+        Canon cs;
+        canon_theta(th.n, th.k, th.Q, th.h, th.D1, th.D2, th.G, th.J, Jc, acol, cs);
+        for (int j = 0; j < nx; j++) {
+            const int w = a * nx + j;
+            pair_direct(true, th.n, cs, Jc, acol, xs[j], mem, eps[w], p[w], m[w], err, 64, th.k);
+        }
+    }
+    return err;
+}

@@ -238,8 +238,10 @@ def test_autotuner_leaves_results_and_streams_unchanged():
 def test_run_kernel_equals_block_kernel(gpu, t, k, pt):
     """The sampler through the run kernel (codewords in per-thread runs that
     share their top-bit shrinks), through the block-prefix kernel with heavy and
-    light launches, and with one launch per occupancy class: identical values
-    for every state (the sums are exact), on the same counter-based draws."""
+    light launches, with one launch per occupancy class, and through the
+    direct kernel (alone, and split with the block-prefix kernel by each
+    state's number of non-pivot coordinates): identical values for every state
+    (the sums are exact), on the same counter-based draws."""
     rs = np.random.RandomState(4000 + t + k)
     L = [rand_word(rs, t) for _ in range(k)]
     rows = random_projector_rows(rs, t, int(0.7 * t))
@@ -247,11 +249,16 @@ def test_run_kernel_equals_block_kernel(gpu, t, k, pt):
     out = []
     try:
         gpu.set_option(backend.OPT_PER_THREAD, pt)
-        for kernel in (2, 3, 4):
+        for kernel in (2, 3, 4, 5):
             gpu.set_option(backend.OPT_PAIR_KERNEL, kernel)
             out.append(gpu.singleProjectorSample(P, L, False, 96, backend.RNG_PHILOX, 606))
+        # the direct kernel with one constraint slot: states with n - k > 1 go to the block-prefix kernel
+        gpu.set_option(backend.OPT_DIRECT_SLOTS, 1)
+        out.append(gpu.singleProjectorSample(P, L, False, 96, backend.RNG_PHILOX, 606))
     finally:
+        gpu.set_option(backend.OPT_DIRECT_SLOTS, 0)
         gpu.set_option(backend.OPT_PAIR_KERNEL, 0)
         gpu.set_option(backend.OPT_PER_THREAD, 0)
-    assert (out[0] == out[1]).all() and (out[0] == out[2]).all()
+    for o in out[1:]:
+        assert (o == out[0]).all()
     assert (out[0] != 0).sum() > 48

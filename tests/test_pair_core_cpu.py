@@ -34,12 +34,18 @@ def tp(request):
     lib.tp_host_block.restype = C.c_int
     lib.tp_host_runs.argtypes = lib.tp_host_pairs.argtypes[:4] + [C.c_int] + lib.tp_host_pairs.argtypes[4:]
     lib.tp_host_runs.restype = C.c_int
+    lib.tp_host_direct.argtypes = lib.tp_host_pairs.argtypes
+    lib.tp_host_direct.restype = C.c_int
 
     def run(thetas, xs, block=False, run_len=0):
         thetas = np.ascontiguousarray(thetas)
         xs = np.ascontiguousarray(np.asarray(xs, dtype=np.uint64))
         n = len(thetas) * len(xs)
         e, p, m = (np.zeros(n, dtype=np.int32) for _ in range(3))
+        if run_len == -1:
+            err = lib.tp_host_direct(thetas.ctypes.data, len(thetas), xs.ctypes.data, len(xs), e.ctypes.data,
+                                     p.ctypes.data, m.ctypes.data)
+            return err, e, p, m
         if run_len:
             err = lib.tp_host_runs(thetas.ctypes.data, len(thetas), xs.ctypes.data, len(xs), run_len, e.ctypes.data,
                                    p.ctypes.data, m.ctypes.data)
@@ -173,3 +179,29 @@ def test_runs_vs_oracle(tp, oracle, t, k, run_len):
         for x, j in xs:
             assert (e[w], p[w], m[w]) == (eo[j], po[j], mo[j]), (t, a, j)
             w += 1
+
+
+@pytest.mark.parametrize("t,k,nshrink", [(1, 1, 0), (3, 3, 0), (8, 4, 0), (12, 6, 4), (24, 8, 0), (33, 8, 0),
+                                         (40, 10, 0), (40, 10, 20), (57, 8, 0), (64, 9, 0), (64, 8, 40)])
+def test_direct_vs_oracle(tp, oracle, t, k, nshrink):
+    """The direct kernel's path: theta once in pivot coordinates
+    (canon_theta), each pair by removing the variables at x's zero pivot
+    coordinates, a constraint per zero at a non-pivot coordinate (md_shrink),
+    then the exponential sum (md_exp_sum).  eps and p equal the oracle's and
+    m equals it mod 8 (the reference's unreduced m depends on its basis; the
+    inner product is the same complex number).  nshrink random shrinks first
+    lower k, so many pairs carry several constraints."""
+    rs = np.random.RandomState(1700 + t + nshrink)
+    L = np.array([rand_word(rs, t) for _ in range(k)], dtype=np.uint64)
+    thetas = _projected_thetas(oracle, rs, t, count=4)
+    for i in range(len(thetas)):
+        one = thetas[i:i + 1].copy()
+        for _ in range(nshrink):
+            oracle.shrink(one, rand_word(rs, t), int(rs.randint(2)), 0)
+        thetas[i] = one[0]
+    xs = [oracle.codeword(int(j), L) for j in range(2 ** k)]
+    err, e, p, m = tp(thetas, xs, run_len=-1)
+    assert err == 0
+    eo, po, mo = oracle.term_products(t, 0, L, k, thetas, 0, 2 ** k, threads=os.cpu_count() or 1)
+    ok = (e == eo) & ((e == 0) | ((p == po) & ((m % 8) == (mo % 8))))
+    assert ok.all(), (t, k, nshrink, int((~ok).sum()))
