@@ -121,6 +121,9 @@ class ClockSampler:
 # measured by `python oracle/rowops.py 24 400` over 9600 pairs (each checked
 # against the dense restatement): 2576 row-ops/pair, 33% orthogonal pairs.
 ROWOPS_PER_PAIR_T40 = 2576.0
+# Rows of J and constraint masks the direct-restriction path reads, copies or
+# updates per c2 pair (the same 9600 pairs, CSIM_COUNT_ROWS hook of the host build).
+DIRECT_ROWS_PER_PAIR_T40 = 265.4
 
 
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of the light pair-kernel
@@ -192,6 +195,10 @@ def run_ours(args, rank, world, local_rank):
     gpu = backend.Backend(local_rank)
     if args.no_tune:
         gpu.set_option(backend.OPT_AUTOTUNE, 0)
+    if args.pair_kernel is not None:
+        gpu.set_option(backend.OPT_PAIR_KERNEL, args.pair_kernel)
+    if args.per_thread is not None:
+        gpu.set_option(backend.OPT_PER_THREAD, args.per_thread)
     P = [backend.projector(ph, xs, zs, nq) for (ph, xs, zs, nq) in projs]
     samples, bins = (args.samples or cfg["samples"]), cfg["bins"]
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -230,12 +237,14 @@ def run_ours(args, rank, world, local_rank):
         step(i, backend.RNG_PHILOX)
         flush.zero_()
     barrier()
-    if args.no_tune:
-        tuned = (0, 0, 0.0, 0)
+    if args.no_tune:  # the launch the fixed rules and the forcing options give
+        forced = {2: 0, 3: 1, 4: 2, 5: 3}.get(args.pair_kernel, 0)
+        tuned = (args.per_thread or 0, 0, 0.0, forced)
     else:  # done by the first warm-up step; this reads the choice
         tuned = gpu.autotune(cfg["t"], P[0], [int(x) for x in L])
     kname = {0: "k_terms_tp (heavy and light launches)", 1: "k_terms_runs",
-             2: "k_terms_tp (one launch per occupancy class)"}[tuned[3]]
+             2: "k_terms_tp (one launch per occupancy class)",
+             3: "k_terms_direct (each state restricted once in pivot form)"}[tuned[3]]
     clocks = ClockSampler(local_rank)
     clocks.start()
     launches0 = gpu.launches
@@ -293,8 +302,10 @@ def run_ours(args, rank, world, local_rank):
                 "traffic": dram_bytes_per_launch(samples * bins / world),
                 "traffic_source": "ncu dram bytes of the 64-state light launch (profiles/k_terms_tp_c2_small.md), "
                                   "scaled to this launch's states",
-                "work_unit": "packed row-op (one 64-bit row test/XOR/update of the elementary-update algorithm)",
+                "work_unit": "packed row-op of the reference's algorithm (one 64-bit row test/XOR/update of its "
+                             "elementary updates), whichever kernel runs",
                 "rowops_per_pair": per_pair,
+                "kernel_rows_per_pair": DIRECT_ROWS_PER_PAIR_T40 if tuned[3] == 3 else per_pair,
                 "peak_source": "SMs x 4 x 32 lanes x sm_max_mhz (MEASURED_PEAKS.json holds no integer peak)",
                 "pair_kernel_share": pair_ms / dev_ms}
     out = {
@@ -621,6 +632,57 @@ def c3_rates(ts=(28, 41, 47, 57), count=2000):
             "inner products/s (pair kernel, CUDA events)", "rates": out}
 
 
+def pair_rates(count_pairs=1 << 26):
+    """Pair-kernel rate of each thread-per-pair kernel (CSIM_OPT_PAIR_KERNEL 2
+    block prefix, 3 runs, 4 occupancy classes, 5 direct restriction) at 16 and
+    32 terms per thread, and the autotuner's choice: the c2 query's G' and
+    code, and random projector rows (0.7 t of them) and codes at t = 24, 48,
+    57, 64.  Each rate is the best of two calls of about `count_pairs` pairs
+    (counter-based states, CUDA-event pair-kernel time)."""
+    from circuitsimulator_gb300 import backend
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import rand_word, random_projector_rows
+
+    cfg, projs, exact, k, norm, L = load_workload()
+    cases = [("c2", cfg["t"], k, backend.projector(*projs[0]), [int(x) for x in L])]
+    for t, kk in ((24, 14), (48, 16), (57, 18), (64, 14)):
+        rs = np.random.RandomState(t)
+        rows = random_projector_rows(rs, t, int(0.7 * t))
+        cases.append(("random", t, kk, backend.projector(rows[0], rows[1], rows[2], t),
+                      [rand_word(rs, t) for _ in range(kk)]))
+    gpu = backend.Backend(0)
+    gpu.set_option(backend.OPT_AUTOTUNE, 0)
+    names = {2: "block prefix", 3: "runs", 4: "occupancy classes", 5: "direct"}
+    out = []
+    for name, t, kk, P, LL in cases:
+        count = max(64, count_pairs >> kk)
+        rec = {"case": name, "t": t, "k": kk, "states": count}
+        for kern, kname in names.items():
+            if kern == 3 and (1 << kk) % (64 * 32):
+                continue
+            for pt in (16, 32):
+                gpu.set_option(backend.OPT_PAIR_KERNEL, kern)
+                gpu.set_option(backend.OPT_PER_THREAD, pt)
+                best = 0.0
+                for _ in range(2):
+                    gpu.singleProjectorSample(P, LL, False, count, backend.RNG_PHILOX, 7)
+                    st = gpu.last_stats()
+                    best = max(best, st.pairs / (st.pair_kernel_ms / 1e3))
+                rec["%s pt %d" % (kname, pt)] = best
+        out.append(rec)
+    gpu.set_option(backend.OPT_PAIR_KERNEL, 0)
+    gpu.set_option(backend.OPT_PER_THREAD, 0)
+    gpu.set_option(backend.OPT_AUTOTUNE, 1)
+    tuned_names = {0: "block prefix", 1: "runs", 2: "occupancy classes", 3: "direct"}
+    for rec, (name, t, kk, P, LL) in zip(out, cases):
+        pt, lz, ms, kern = gpu.autotune(t, P, LL)
+        rec["tuned"] = {"kernel": tuned_names[kern], "terms_per_thread": pt, "light_zero_bound": lz}
+    gpu.close()
+    return {"workload": "pair-kernel rates per kernel, c2 and random codes", "metric":
+            "inner products/s (pair kernel, CUDA events)", "rates": out}
+
+
 def run_reference(args, rank, world):
     """The reference's algorithm on the host cores (the oracle port of
     libcirc/stabilizer.c + stateprep.c + innerprod.c: the reference's own C
@@ -692,6 +754,12 @@ def main():
     ap.add_argument("--no-tune", action="store_true",
                     help="fixed launch rules instead of the autotuner (profiling runs: a fixed launch sequence; on "
                          "this workload the tuner picks the same launch)")
+    ap.add_argument("--pair-rates", action="store_true",
+                    help="only time each thread-per-pair kernel at t = 24..64 (c2 and random codes)")
+    ap.add_argument("--pair-kernel", type=int, default=None,
+                    help="force the pair kernel (CSIM_OPT_PAIR_KERNEL: 2 block prefix, 3 runs, 4 occupancy classes, "
+                         "5 direct restriction); with --no-tune a fixed launch sequence of that kernel")
+    ap.add_argument("--per-thread", type=int, default=None, help="force terms per thread (CSIM_OPT_PER_THREAD)")
     ap.add_argument("--chain", default=None, metavar="SHOTSxBITS",
                     help="only time sampleQubits chains on the c4 circuit, plain vs batched (e.g. 16x4)")
     ap.add_argument("--chain-samples", type=int, default=None, help="L per conditional for --chain")
@@ -706,6 +774,9 @@ def main():
     ap.add_argument("--c3-rates", action="store_true",
                     help="only time the pair kernel inside c3 queries against random codes of the same t and k")
     args = ap.parse_args()
+    if args.pair_rates:
+        print(json.dumps(pair_rates()))
+        return
     if args.c3_rates:
         print(json.dumps(c3_rates()))
         return

@@ -40,10 +40,17 @@ int launch_draw_project(const Launch& L, const DrawDesc* desc, int64_t count, GS
 // resident blocks per SM of k_items_tp launched for states of up to nmax qubits
 // and codewords of up to gmax zeros
 int items_tp_occupancy(int nmax, int gmax);
-// queue: one device counter, zeroed by the launch (stream-ordered) and drawn from by the blocks
+// queue: one device counter, zeroed by the launch (stream-ordered) and drawn from by the blocks.
+// only_live: write the partial sums of live states' items only (the other items are another launch's)
 int launch_items_tp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,
                     int per_thread, int nmax, int gmax, __int128* part, __int128* part_diag,
-                    unsigned long long* queue);
+                    unsigned long long* queue, bool only_live = false);
+// the direct kernel over the items; canon, code_direct, code_rest as launch_canon
+// wrote them for the items' states.  Writes every item's partial sums except
+// those of states with code_rest >= 0 (launch_items_tp with code_rest, only_live).
+int launch_items_direct(const Launch& L, const PairItem* items, int64_t nitems, const void* canon,
+                        const int* code_direct, const int* code_rest, int per_thread, int nmax, int dslots,
+                        __int128* part, __int128* part_diag, unsigned long long* queue);
 int launch_items_warp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,
                       __int128* part, __int128* part_diag);
 // per-slot sums of item partials; slot s owns items [range[2s], range[2s+1]) and,

@@ -7,6 +7,8 @@
 //                   query's projector (innerprod.c:97-116 / :224-241)
 //   k_items_tp      the thread-per-pair kernel over an item table of
 //                   (state, range of |L> terms) work items
+//   k_items_direct  the same items by direct restriction of each state's
+//                   pivot form (launch_canon), one thread per pair
 //   k_items_warp    the warp-per-pair kernel over (state, range of term states)
 //   k_reduce_slots  per-slot sums of the items' partial sums
 #include <cuda_runtime.h>
@@ -108,7 +110,7 @@ __device__ __forceinline__ __int128 shfl_xor_128(__int128 v, int m) {
 __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_t nitems, const GState* states,
                                                    const int* codes, int per_thread, int nmax, int gmax,
                                                    __int128* part, __int128* part_diag,
-                                                   unsigned long long* queue, int* err) {
+                                                   unsigned long long* queue, int only_live, int* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ItemShared& sh = *reinterpret_cast<ItemShared*>(smem_raw);
     uint64_t* const sa = reinterpret_cast<uint64_t*>(smem_raw + sizeof(ItemShared));
@@ -136,8 +138,9 @@ __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_
             }
         }
         const int k0 = g->k;  // the state's own k, for p's correction
+        const bool live0 = codes[it.theta] >= 0;  // sh.live, before the barrier that publishes it
         uint64_t* const r0 = pc::block_state_rows(sa, nmax, 0);
-        if (tid < nmax) {
+        if (live0 && tid < nmax) {
             r0[tid] = g->J[tid];
             const int n = g->n;
             uint64_t col = 0ull;
@@ -147,13 +150,13 @@ __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_
         }
         __syncthreads();
         bool asym = false;
-        if (tid < k0 && k0 <= nmax)
+        if (sh.live && tid < k0 && k0 <= nmax)
             for (int r = 0; r < k0; r++) asym |= ((r0[tid] >> r) & 1ull) != ((r0[r] >> tid) & 1ull);
         asym = __syncthreads_or(asym) != 0;
         __int128 z[4] = {0, 0, 0, 0}, zd[4] = {0, 0, 0, 0};
         int deps = 0, dp = 0, dm = 0;  // the diagonal pair, summed apart after the loop
         const int n = sh.n;
-        if (n > nmax || asym) e |= kErrArg;
+        if (sh.live && (n > nmax || asym)) e |= kErrArg;
         if (sh.live && !asym && n >= 1 && n <= nmax) {
             // the shrinks that each of the item's codeword groups shares run once
             pc::block_prefix<kTPB>(sh.bp, sa, nmax, it.cw + it.j0, it.nj, per_thread, n, pair_base);
@@ -182,20 +185,118 @@ __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_
             pc::zacc(zd, deps, dp, dm, P, e);
             for (int q = 0; q < 4; q++) z[q] -= zd[q];
         }
-        for (int q = 0; q < 4; q++)
-            for (int o = 16; o > 0; o >>= 1) {
-                z[q] += shfl_xor_128(z[q], o);
-                zd[q] += shfl_xor_128(zd[q], o);
-            }
-        if ((tid & 31) == 0)
-            for (int q = 0; q < 4; q++) {
-                sh.red[tid >> 5][q] = z[q];
-                sh.red[tid >> 5][4 + q] = zd[q];
-            }
+        if (sh.live) {  // block-uniform
+            for (int q = 0; q < 4; q++)
+                for (int o = 16; o > 0; o >>= 1) {
+                    z[q] += shfl_xor_128(z[q], o);
+                    zd[q] += shfl_xor_128(zd[q], o);
+                }
+            if ((tid & 31) == 0)
+                for (int q = 0; q < 4; q++) {
+                    sh.red[tid >> 5][q] = z[q];
+                    sh.red[tid >> 5][4 + q] = zd[q];
+                }
+        }
         __syncthreads();
-        if (tid < 8) {
+        if (tid < 8 && (sh.live || !only_live)) {
             __int128 acc = 0;
-            for (int ww = 0; ww < kTPB / 32; ww++) acc += sh.red[ww][tid];
+            if (sh.live)
+                for (int ww = 0; ww < kTPB / 32; ww++) acc += sh.red[ww][tid];
+            if (tid < 4) part[4 * w + tid] = acc;
+            else if (part_diag) part_diag[4 * w + tid - 4] = acc;
+        }
+        if (tid == 0) sh.next = (long long)atomicAdd(queue, 1ull);
+        __syncthreads();
+        w = sh.next;
+    }
+    e = (int)__reduce_or_sync(kFull, (unsigned)e);
+    if (e && (tid & 31) == 0) atomicOr(err, e);
+}
+
+// ------------------------------------------------------------ direct-restriction items
+// The direct kernel (pc::pair_direct) over the item table.  A block loads the
+// item's state in pivot form into shared memory, then runs one thread per
+// pair.  Items whose state launch_canon left to the block-prefix kernel
+// (code_rest >= 0) are that kernel's to write; this one writes all others,
+// zeros for dead states.
+struct DirectItemShared {
+    pc::Canon cs;
+    int live, skip;
+    long long next;  // the next item taken from the work queue
+    __int128 red[kTPB / 32][8];
+};
+static_assert(kTPB == 64, "one thread per row of the 64-row pivot form");
+
+__global__ void __launch_bounds__(kTPB) k_items_direct(const PairItem* items, int64_t nitems,
+                                                       const pc::CanonG* canon, const int* code_direct,
+                                                       const int* code_rest, int per_thread, int nmax, int dslots,
+                                                       __int128* part, __int128* part_diag,
+                                                       unsigned long long* queue, int* err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    DirectItemShared& sh = *reinterpret_cast<DirectItemShared*>(smem_raw);
+    uint64_t* const sJ = reinterpret_cast<uint64_t*>(smem_raw + sizeof(DirectItemShared));  // 64 rows
+    uint64_t* const sA = sJ + 64;                                                             // 64 masks
+    unsigned char* const pair_base = smem_raw + sizeof(DirectItemShared) + 2 * 64 * 8;
+    const int tid = threadIdx.x;
+    int e = 0;
+    const pc::PairMem mem = pc::pair_mem(pair_base, nmax, kTPB, tid);
+    if (tid == 0) sh.next = (long long)atomicAdd(queue, 1ull);
+    __syncthreads();
+    for (int64_t w = sh.next; w < nitems;) {
+        const PairItem it = items[w];
+        __syncthreads();  // the previous item's use of the shared state is over
+        if (tid == 0) {
+            sh.live = code_direct[it.theta] >= 0;
+            sh.skip = code_rest[it.theta] >= 0;
+            if (sh.live) sh.cs = canon[it.theta].cs;
+        }
+        __syncthreads();
+        if (sh.live) {
+            sJ[tid] = canon[it.theta].Jc[tid];
+            sA[tid] = canon[it.theta].acol[tid];
+        }
+        __syncthreads();
+        __int128 z[4] = {0, 0, 0, 0}, zd[4] = {0, 0, 0, 0};
+        if (sh.live) {  // block-uniform
+            const int n = sh.cs.n;
+            if (n > nmax) e |= kErrArg;
+            if (n >= 1 && n <= nmax) {
+                const int P = 2 * n;
+                int deps = 0, dp = 0, dm = 0;  // the diagonal pair, summed apart
+                for (int r = 0; r < per_thread; r++) {
+                    const int64_t j = it.j0 + tid + (int64_t)kTPB * r;
+                    const bool valid = j < it.j0 + it.nj;
+                    if (__all_sync(kFull, !valid)) break;  // warp-uniform exit
+                    const uint64_t x = valid ? it.cw[j] : 0ull;
+                    int eps = 0, pp = 0, mm = 0;
+                    pc::pair_direct(valid, n, sh.cs, sJ, sA, x, mem, eps, pp, mm, e, dslots, sh.cs.k);
+                    if (!valid) continue;
+                    pc::zacc(z, eps, pp, mm, P, e);
+                    if (j == it.diag) {
+                        deps = eps;
+                        dp = pp;
+                        dm = mm;
+                    }
+                }
+                pc::zacc(zd, deps, dp, dm, P, e);
+                for (int q = 0; q < 4; q++) z[q] -= zd[q];
+            }
+            for (int q = 0; q < 4; q++)
+                for (int o = 16; o > 0; o >>= 1) {
+                    z[q] += shfl_xor_128(z[q], o);
+                    zd[q] += shfl_xor_128(zd[q], o);
+                }
+            if ((tid & 31) == 0)
+                for (int q = 0; q < 4; q++) {
+                    sh.red[tid >> 5][q] = z[q];
+                    sh.red[tid >> 5][4 + q] = zd[q];
+                }
+        }
+        __syncthreads();
+        if (tid < 8 && !sh.skip) {
+            __int128 acc = 0;
+            if (sh.live)
+                for (int ww = 0; ww < kTPB / 32; ww++) acc += sh.red[ww][tid];
             if (tid < 4) part[4 * w + tid] = acc;
             else if (part_diag) part_diag[4 * w + tid - 4] = acc;
         }
@@ -290,7 +391,7 @@ int items_tp_occupancy(int nmax, int gmax) {
 
 int launch_items_tp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,
                     int per_thread, int nmax, int gmax, __int128* part, __int128* part_diag,
-                    unsigned long long* queue) {
+                    unsigned long long* queue, bool only_live) {
     if (nitems <= 0) return 0;
     if (nmax < 1 || nmax > 64 || gmax < 0 || gmax > nmax || !queue) return -1;
     if (cudaMemsetAsync(queue, 0, sizeof(unsigned long long), L.stream) != cudaSuccess) return -1;
@@ -304,7 +405,36 @@ int launch_items_tp(const Launch& L, const PairItem* items, int64_t nitems, cons
     int64_t grid = (int64_t)L.num_sms * per_sm;
     if (grid > nitems) grid = nitems;
     k_items_tp<<<(int)grid, kTPB, smem, L.stream>>>(items, nitems, states, codes, per_thread, nmax, gmax, part,
-                                                    part_diag, queue, L.d_err);
+                                                    part_diag, queue, only_live ? 1 : 0, L.d_err);
+    (*L.launches)++;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+namespace {
+size_t items_direct_smem(int nmax, int dslots) {
+    return sizeof(DirectItemShared) + 2 * 64 * 8 + pc::pair_mem_bytes(nmax, dslots, kTPB);
+}
+}  // namespace
+
+int launch_items_direct(const Launch& L, const PairItem* items, int64_t nitems, const void* canon,
+                        const int* code_direct, const int* code_rest, int per_thread, int nmax, int dslots,
+                        __int128* part, __int128* part_diag, unsigned long long* queue) {
+    if (nitems <= 0) return 0;
+    if (nmax < 1 || nmax > 64 || dslots < 0 || dslots > nmax || per_thread < 1 || !queue || !canon) return -1;
+    if (cudaMemsetAsync(queue, 0, sizeof(unsigned long long), L.stream) != cudaSuccess) return -1;
+    if (cudaFuncSetAttribute(k_items_direct, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)items_direct_smem(64, 64)) != cudaSuccess)
+        return -1;
+    const size_t smem = items_direct_smem(nmax, dslots);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_items_direct, kTPB, smem) != cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    int64_t grid = (int64_t)L.num_sms * per_sm;
+    if (grid > nitems) grid = nitems;
+    k_items_direct<<<(int)grid, kTPB, smem, L.stream>>>(items, nitems, (const pc::CanonG*)canon, code_direct,
+                                                        code_rest, per_thread, nmax, dslots, part, part_diag, queue,
+                                                        L.d_err);
     (*L.launches)++;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

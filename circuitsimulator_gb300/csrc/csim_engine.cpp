@@ -9,7 +9,9 @@
 // evaluations (one evaluation = one projector of one query), up to a budget
 // of inner products, and runs:
 //   k_draw_project  draw or copy every state, then project it (innerprod.c:97-116)
+//   k_canon         the states of direct-restriction evaluations in pivot form
 //   k_items_tp      (state, |L> term range) items, thread per pair
+//   k_items_direct  the same items by direct restriction, thread per pair
 //   k_items_warp    (state, prepH term range) items, warp per pair
 //   k_reduce_slots  exact Z[w] sums per state
 // Two round buffers alternate.  The host builds round r+1 and queues it behind
@@ -49,9 +51,10 @@ using Clock = std::chrono::steady_clock;
 constexpr size_t kAlign = 256;
 inline size_t align_up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
 
-// thread-per-pair launches: one per (occupancy class of t, light or not); a
-// light launch takes codewords of at most the light bound's zeros (tune_for)
-constexpr int kBuckets = 2 * CSIM_MAX_QUBITS;
+// thread-per-pair launches: three per occupancy class of t (heavy, light,
+// direct); a light launch takes codewords of at most the light bound's zeros,
+// a direct launch the evaluations the tuner gave the direct kernel (tune_for)
+constexpr int kBuckets = 3 * CSIM_MAX_QUBITS;
 
 // device memory that grows on demand (contents are not kept)
 struct DevBuf {
@@ -110,6 +113,7 @@ struct Decomp {
     uint64_t* cws = nullptr;     // the same in ordered_codewords' order, for sampled estimators
     int64_t light = 0;           // first index of cws with at most lz zeros
     int pt = 0, lz = 0;          // thread-per-pair terms per thread and light bound (csim_host::tune_for)
+    int kern = 0;                // the tuner's kernel: 3 = direct restriction, else the block-prefix kernel
     csim_state* phis = nullptr;  // term states: prepH (exact == 1), prepL (exact projector on |L>)
     uint64_t* dL = nullptr;
     size_t bytes = 0;
@@ -404,6 +408,7 @@ int Engine::ensure_decomp(QueryRec* r, bool need_phis, bool force, Decomp** out)
                 return rc;
             }
             d->pt = tn.per_thread;
+            d->kern = tn.kernel;
             d->lz = tn.kernel == 0 ? tn.light : light_zeros(d->t);  // the items kernel shares top bits per block
             std::vector<uint64_t> ordered;
             ordered_codewords(d->L.data(), d->k, d->t, d->lz, ordered);
@@ -583,9 +588,13 @@ int Engine::launch_round() {
         const int64_t jb = e->kind == 2 ? rs.slots[i].s : 0;
         const int64_t nj = e->chi - jb;
         if (!e->q->exact) {
-            const int b = 2 * bucket_of_[e->t];
+            const int b = 3 * bucket_of_[e->t];
             const int64_t span_tp = span_tp_of(e);
             const int64_t nall = (nj + span_tp - 1) / span_tp;
+            if (e->q->dec->kern == 3) {
+                nbucket[b + 2] += nall;
+                continue;
+            }
             const int64_t nlight = e->kind == 1 ? nall - light_first_item(e, span_tp) : 0;
             nbucket[b] += nall - nlight;
             nbucket[b + 1] += nlight;
@@ -607,11 +616,16 @@ int Engine::launch_round() {
     const size_t o_range = align_up(o_items + (size_t)nitems * sizeof(csim::PairItem));
     const size_t o_range2 = align_up(o_range + (size_t)ns * 16);
     const size_t up_bytes = align_up(o_range2 + (size_t)ns * 16);
-    // work block: states | parts | parts diag
+    bool any_direct = false;
+    for (int b = 2; b < kBuckets; b += 3) any_direct |= nbucket[b] > 0;
+    // work block: states | parts | parts diag | pivot forms | direct and rest codes (direct launches)
     const size_t w_states = 0;
     const size_t w_part = align_up((size_t)ns * sizeof(csim_state));
     const size_t w_partd = align_up(w_part + (size_t)std::max<int64_t>(nitems, 1) * 64);
-    const size_t work_bytes = align_up(w_partd + (size_t)std::max<int64_t>(nitems, 1) * 64);
+    const size_t w_canon = align_up(w_partd + (size_t)std::max<int64_t>(nitems, 1) * 64);
+    const size_t w_cdir = align_up(w_canon + (any_direct ? (size_t)ns * csim::canon_bytes() : 0));
+    const size_t w_crest = align_up(w_cdir + (any_direct ? (size_t)ns * 4 : 0));
+    const size_t work_bytes = align_up(w_crest + (any_direct ? (size_t)ns * 4 : 0));
     // download block: err (16 B), the pair launches' work-queue counter (kQueueOffset) | codes | sums | sums diag
     rs.off_codes = 256;
     rs.off_sum = align_up(rs.off_codes + (size_t)ns * 4);
@@ -673,10 +687,20 @@ int Engine::launch_round() {
         hdesc[i] = d;
         const int64_t jb = e->kind == 2 ? s : 0;
         const int64_t diag = e->kind == 2 ? s : -1;
-        if (!r->exact) {
+        if (!r->exact && r->dec->kern == 3) {
+            // all of a slot's items in its bucket's direct launch
+            const int64_t span_tp = span_tp_of(e);
+            int64_t& cd = cur[3 * bucket_of_[e->t] + 2];
+            hrange[2 * i] = cd;
+            for (int64_t j = jb; j < e->chi; j += span_tp)
+                hitems[cd++] = csim::PairItem{i, j, std::min(span_tp, e->chi - j), diag,
+                                              e->kind == 1 ? r->dec->cws : r->dec->cw, nullptr};
+            hrange[2 * i + 1] = cd;
+            hrange2[2 * i] = hrange2[2 * i + 1] = 0;
+        } else if (!r->exact) {
             // heavy items first, then light ones; a slot's items may sit in two
             // launches, so its range is kept per slot in each (see below)
-            const int b = 2 * bucket_of_[e->t];
+            const int b = 3 * bucket_of_[e->t];
             const int64_t span_tp = span_tp_of(e);
             const int64_t jl = e->kind == 1 ? light_first_item(e, span_tp) * span_tp : e->chi;
             int64_t& ch = cur[b];
@@ -711,12 +735,32 @@ int Engine::launch_round() {
         return fail(ctx_, CSIM_ERR_CUDA, "draw/project launch failed");
     CK(cudaEventRecord(rs.ev[1], ctx_->stream));
     const csim::PairItem* ditems = (const csim::PairItem*)(db + o_items);
-    for (int b = 0; b < 2 * nbuckets_; b++) {
-        const int nmax = bucket_hi_[b / 2], gmax = (b & 1) ? std::min(nmax, lzmax[b]) : nmax;
-        if (nbucket[b] && csim::launch_items_tp(L, ditems + bstart[b], nbucket[b], dstates, dcode, launch_pt, nmax,
-                                                gmax, part + 4 * bstart[b], partd + 4 * bstart[b],
-                                                (unsigned long long*)(dd + kQueueOffset)))
-            return fail(ctx_, CSIM_ERR_CUDA, "pair launch failed");
+    unsigned long long* const queue = (unsigned long long*)(dd + kQueueOffset);
+    // direct launches: the states in pivot form; those with more non-pivot
+    // coordinates than the constraint slots go to the block-prefix kernel
+    const int dslots_max = ctx_->direct_slots > 0 ? ctx_->direct_slots : direct_slots(CSIM_MAX_QUBITS);
+    void* const canon = wb + w_canon;
+    int* const cdir = (int*)(wb + w_cdir);
+    int* const crest = (int*)(wb + w_crest);
+    if (any_direct && csim::launch_canon(L, dstates, dcode, ns, dslots_max, canon, cdir, crest))
+        return fail(ctx_, CSIM_ERR_CUDA, "pivot form launch failed");
+    for (int b = 0; b < 3 * nbuckets_; b++) {
+        if (!nbucket[b]) continue;
+        const int nmax = bucket_hi_[b / 3];
+        const csim::PairItem* it = ditems + bstart[b];
+        int rc = 0;
+        if (b % 3 == 2) {
+            rc = csim::launch_items_direct(L, it, nbucket[b], canon, cdir, crest, launch_pt, nmax,
+                                           std::min(nmax, dslots_max), part + 4 * bstart[b], partd + 4 * bstart[b],
+                                           queue) ||
+                 csim::launch_items_tp(L, it, nbucket[b], dstates, crest, launch_pt, nmax, nmax, part + 4 * bstart[b],
+                                       partd + 4 * bstart[b], queue, true);
+        } else {
+            const int gmax = b % 3 == 1 ? std::min(nmax, lzmax[b]) : nmax;
+            rc = csim::launch_items_tp(L, it, nbucket[b], dstates, dcode, launch_pt, nmax, gmax, part + 4 * bstart[b],
+                                       partd + 4 * bstart[b], queue);
+        }
+        if (rc) return fail(ctx_, CSIM_ERR_CUDA, "pair launch failed");
     }
     if (csim::launch_items_warp(L, ditems + nitp, niw, dstates, dcode, part + 4 * nitp, partd + 4 * nitp))
         return fail(ctx_, CSIM_ERR_CUDA, "pair launch failed");

@@ -949,11 +949,26 @@ CSIM_HD inline void pair_from_run(bool valid, int n, const RunState& rs, const P
 // by coordinate; a mask F marks the live ones), so nothing is compacted.
 // The result is the same complex number as innerProductExact's; eps and p are
 // equal, m is equal mod 8 (the reference's unreduced m depends on its basis).
+// CSIM_COUNT_ROWS(r): the direct path touched r rows of J or constraint
+// masks for one pair (each row read, copied or updated once).  A host build
+// that measures the path's work per pair defines it; it is empty otherwise.
+#ifndef CSIM_COUNT_ROWS
+#define CSIM_COUNT_ROWS(r) ((void)0)
+#endif
+
 struct Canon {
     uint64_t P;       // pivot coordinates: the variables
     uint64_t D1, D2;  // the form's D, at each variable's coordinate
     uint64_t bm;      // right-hand side bit of each non-pivot coordinate's constraint
     int Q, k, n, pad;
+};
+
+// A state's pivot form as the direct kernels read it (canon_theta): the
+// scalars, each coordinate's J row and each non-pivot coordinate's variables.
+struct CanonG {
+    Canon cs;
+    uint64_t Jc[64];
+    uint64_t acol[64];
 };
 
 // (D1, D2) += (d1, d2) on the bits of u, with the carry into D2 (D = 2 (2 D2 + D1) mod 8)
@@ -1118,6 +1133,7 @@ CSIM_HD inline int md_shrink(PairRegs& s, uint64_t& F, const PairMem& M, int q, 
     const W Ji = upd ? md_read_row<W>(M, i, KP) : (W)0;
     const W C = Ji ^ (wget<W>(Ji, i) ? U : (W)0);  // new row (and column) i
     const int KX = uniform_max(KP);
+    if (upd) CSIM_COUNT_ROWS(nrem + 1 + KP);
     if (upd) md_rank2<W>(M, KX, Ji, U, C);
     if (upd) {
         uint64_t D1 = s.D1, D2 = s.D2;
@@ -1157,6 +1173,7 @@ CSIM_HD inline void md_exp_sum(PairRegs& s, const PairMem& M, uint64_t F, bool a
         const W C = Ja ^ (wget<W>(Ja, a) ? U : (W)0);
         const int KX = uniform_max(upd ? KP : 0);
         if (upd && U != (W)0) md_rank2<W>(M, KX, Ja, U, C);
+        if (upd) CSIM_COUNT_ROWS(U != (W)0 ? 1 + KP : 1);
         if (upd) {
             add_D64(D1, D2, (uint64_t)U, getbit(D1, a), getbit(D2, a));
             D2 ^= (uint64_t)(U & Ja);
@@ -1199,6 +1216,7 @@ CSIM_HD inline void md_exp_sum(PairRegs& s, const PairMem& M, uint64_t F, bool a
             const W zm = upd ? (Ep | keep) : (W)0;
             const int lo = zm ? T::ffs(zm) - 1 : T::bits, hi = zm ? T::bits - T::clz(zm) : 0;
             const int X0 = uniform_min(lo) & ~3, X1 = uniform_max(hi);
+            if (live) CSIM_COUNT_ROWS((dimer ? 2 : 1) + (upd ? hi - lo : 0));
             const W rvb = wbrev(vb), rva = wbrev(va), rcb = wbrev(Cb), rca = wbrev(Ca);
             {
                 const int sh = T::bits - 32;
@@ -1335,6 +1353,7 @@ CSIM_HD inline void pair_direct(bool valid, int n, const Canon& cs, const uint64
             v.b = Jc[r + 1];
             *reinterpret_cast<U64x2*>(&R64(r)) = v;
         }
+    CSIM_COUNT_ROWS(KP);
     // the constraints: x's zeros at non-pivot coordinates, descending
     int nz = 0;
     uint64_t hz = 0ull;
@@ -1344,6 +1363,7 @@ CSIM_HD inline void pair_direct(bool valid, int n, const Canon& cs, const uint64
         RG(nz) = acol[c];
         hz |= (uint64_t)getbit(cs.bm, c) << nz;
     }
+    CSIM_COUNT_ROWS(nz);
     s.h = hz;
     eps = 0;
     p = 0;

@@ -154,11 +154,7 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
 // k_canon: one thread per state, theta in pivot coordinates (pc::canon_theta);
 // states whose d = n - k exceeds `dslots` are left to the block-prefix kernel
 // (code_direct < 0), the others to the direct kernel (code_rest < 0).
-struct CanonG {
-    pc::Canon cs;
-    uint64_t Jc[64];
-    uint64_t acol[64];
-};
+using pc::CanonG;
 
 __global__ void __launch_bounds__(64) k_canon(const GState* theta, const int* code, int64_t ntheta, int dslots,
                                                CanonG* out, int* code_direct, int* code_rest) {

@@ -9,11 +9,19 @@ codewords.  Every counted pair is also checked against the dense restatement
 
     python oracle/rowops.py [nstates] [terms_per_state]
 
-Prints one JSON line; the figure is copied into bench.py (ROWOPS_PER_PAIR_T40)
-and profiles/rowops_c2.md.
+The same pairs are also run through the direct-restriction path
+(csim_pair_core.cuh's canon_theta and pair_direct, compiled for the host from
+tests/native/tp_host_check.cpp), which counts the rows of J and constraint
+masks it reads, copies or updates per pair (CSIM_COUNT_ROWS): the work unit of
+the direct kernel.  Its (eps, p, m mod 8) are checked against the oracle too.
+
+Prints one JSON line; the figures are copied into bench.py (ROWOPS_PER_PAIR_T40,
+DIRECT_ROWS_PER_PAIR_T40) and profiles/rowops_c2.md.
 """
+import ctypes as C
 import json
 import os
+import subprocess
 import sys
 
 import numpy as np
@@ -26,6 +34,19 @@ from bench import parse_protocol  # noqa: E402
 from oracle_ffi import Oracle, make_projector  # noqa: E402
 
 
+def direct_counter():
+    """The host build of the pair core with its row counter."""
+    src = os.path.join(ROOT, "tests", "native", "tp_host_check.cpp")
+    so = os.path.join(ROOT, "tests", "native", "_build", "libtphost_rows.so")
+    os.makedirs(os.path.dirname(so), exist_ok=True)
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", src, "-o", so])
+    lib = C.CDLL(so)
+    lib.tp_host_direct.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.tp_host_direct.restype = C.c_int
+    lib.tp_host_rows_take.restype = C.c_int64
+    return lib
+
+
 def main():
     nstates = int(sys.argv[1]) if len(sys.argv) > 1 else 24
     nterms = int(sys.argv[2]) if len(sys.argv) > 2 else 400
@@ -36,7 +57,9 @@ def main():
                                     cfg["k"], O.rng(1))
     rs = np.random.RandomState(3)
     r = O.rng(2024)
-    ops, orth, pairs, per_proj = [], 0, 0, {}
+    dlib = direct_counter()
+    dlib.tp_host_rows_take()
+    ops, orth, pairs, per_proj, drows = [], 0, 0, {}, []
     for pi, (ph, xs, zs, nq) in enumerate(projs):
         P = make_projector(ph, xs, zs, nq)
         got = 0
@@ -45,6 +68,7 @@ def main():
             if O.project(s, P) == 0:
                 continue
             got += 1
+            refs, xs = [], []
             for j in rs.randint(0, 2 ** k, size=nterms):
                 x = O.codeword(int(j), L)
                 res, n_ops = O.pair_rowops(s, x)
@@ -53,10 +77,23 @@ def main():
                 ops.append(n_ops)
                 orth += res[0] == 0
                 pairs += 1
+                refs.append(ref)
+                xs.append(x)
+            xa = np.array(xs, dtype=np.uint64)
+            e, p, m = (np.zeros(len(xs), dtype=np.int32) for _ in range(3))
+            for i in range(len(xs)):  # one pair at a time, so each count is one pair's
+                assert dlib.tp_host_direct(s.ctypes.data, 1, xa[i:].ctypes.data, 1, e[i:].ctypes.data,
+                                           p[i:].ctypes.data, m[i:].ctypes.data) == 0
+                drows.append(dlib.tp_host_rows_take())
+            for i, ref in enumerate(refs):
+                assert (e[i], p[i] if e[i] else 0, (m[i] - ref[2]) % 8 if e[i] else 0) == \
+                    (ref[0], ref[1] if ref[0] else 0, 0), (i, e[i], p[i], m[i], ref)
         per_proj[pi] = float(np.mean(ops[-(nstates // 2) * nterms:]))
     out = {"workload": "c2 (t=40, k=16)", "pairs": pairs, "rowops_per_pair": float(np.mean(ops)),
            "rowops_p50": float(np.median(ops)), "rowops_p95": float(np.percentile(ops, 95)),
-           "orthogonal_fraction": orth / pairs, "per_projector": per_proj}
+           "orthogonal_fraction": orth / pairs, "per_projector": per_proj,
+           "direct_rows_per_pair": float(np.mean(drows)), "direct_rows_p50": float(np.median(drows)),
+           "direct_rows_p95": float(np.percentile(drows, 95))}
     print(json.dumps(out))
 
 

@@ -1,7 +1,12 @@
 // Host build of the thread-per-pair kernel's pair routine
 // (circuitsimulator_gb300/csrc/csim_pair_core.cuh), for CPU tests only: the
 // same source the kernel runs, checked against the oracle without a GPU.
+#include <cstdint>
 #include <cstring>
+
+// rows the direct path touches (the pair core's CSIM_COUNT_ROWS hook)
+static int64_t g_direct_rows = 0;
+#define CSIM_COUNT_ROWS(r) (g_direct_rows += (int64_t)(r))
 
 #include "../../circuitsimulator_gb300/csrc/csim_block_prefix.cuh"
 #include "../../circuitsimulator_gb300/csrc/csim_pair_core.cuh"
@@ -180,4 +185,11 @@ extern "C" int tp_host_direct(const csim_state* theta, int ntheta, const uint64_
         }
     }
     return err;
+}
+
+// Rows the direct path touched since the last call (CSIM_COUNT_ROWS), then 0.
+extern "C" int64_t tp_host_rows_take() {
+    const int64_t r = g_direct_rows;
+    g_direct_rows = 0;
+    return r;
 }

@@ -125,6 +125,31 @@ def test_empty_numerator_projector_seeds_the_denominator(be):
     assert [_key(r) for r in plain_first] == [_key(r) for r in plain_alone] == [_key(r) for r in batched]
 
 
+@pytest.mark.parametrize("kernel,slots", [(2, 0), (5, 0), (5, 1)])
+def test_batched_pair_kernels_agree(kernel, slots):
+    """The engine's block-prefix and direct-restriction launches
+    (CSIM_OPT_PAIR_KERNEL 2 and 5) give bit-identical results, batched and
+    plain.  With one constraint slot (CSIM_OPT_DIRECT_SLOTS 1) most states go
+    on to the block-prefix kernel, so one direct bucket runs both kernels."""
+    qs = mixed_queries(seed=29, count=16)
+    ref_be = backend.Backend(0)
+    ref_be.set_option(backend.OPT_AUTOTUNE, 0)
+    ref_be.set_option(backend.OPT_PAIR_KERNEL, 2)
+    b = backend.Backend(0)
+    b.set_option(backend.OPT_AUTOTUNE, 0)
+    b.set_option(backend.OPT_PAIR_KERNEL, kernel)
+    b.set_option(backend.OPT_DIRECT_SLOTS, slots)
+    try:
+        ref = ref_be.run_queries(qs, batched=False)
+        batched = b.run_queries(qs, batched=True)
+        plain = b.run_queries(qs, batched=False)
+    finally:
+        ref_be.close()
+        b.close()
+    assert [_key(r) for r in batched] == [_key(r) for r in ref]
+    assert [_key(r) for r in plain] == [_key(r) for r in ref]
+
+
 def test_round_splitting_does_not_change_results():
     """Tiny rounds (many per query) give the same results as one big round."""
     qs = mixed_queries(seed=23, count=10)
