@@ -126,20 +126,22 @@ ROWOPS_PER_PAIR_T40 = 2576.0
 DIRECT_ROWS_PER_PAIR_T40 = 265.4
 
 
-# ncu dram__bytes_read.sum + dram__bytes_write.sum of the light pair-kernel
-# launch over 64 projected c2 states (profiles/k_terms_tp_c2_small.md): 657 KB
-# read (the 512 KB codeword table and the states) + 600 KB written (the work
-# items' partial sums).
-MEASURED_TRAFFIC_64_STATES = 657e3 + 600e3
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of one pair-kernel launch over
+# 64 projected c2 states: the light block-prefix launch
+# (profiles/k_terms_tp_c2_small.md: 657 KB read, 600 KB written) and the direct
+# launch (profiles/k_terms_direct_c2_small.md: 658 KB read, 933 KB written).  Reads
+# are the 512 KB codeword table and the states; writes are the partial sums and
+# the write-back of lines the L2 flush left dirty.
+MEASURED_TRAFFIC_64_STATES = {"block prefix": 657e3 + 600e3, "direct": 658e3 + 933e3}
 MEASURED_TRAFFIC_CODEWORDS = 8 * 2 ** 16
 
 
-def dram_bytes_per_launch(states):
+def dram_bytes_per_launch(states, kernel="block prefix"):
     """DRAM bytes of one pair-kernel launch over `states` states, scaled from
     the measured 64-state capture: the codeword table once, the rest in
     proportion to the states (the states read and the partial sums written
     both grow with them)."""
-    per_state = (MEASURED_TRAFFIC_64_STATES - MEASURED_TRAFFIC_CODEWORDS) / 64
+    per_state = (MEASURED_TRAFFIC_64_STATES[kernel] - MEASURED_TRAFFIC_CODEWORDS) / 64
     return MEASURED_TRAFFIC_CODEWORDS + per_state * states
 
 
@@ -299,9 +301,11 @@ def run_ours(args, rank, world, local_rank):
     roofline = {"bound": "alu", "kernel": kname + ": (theta, prepL term) pairs, one thread per pair",
                 "achieved": achieved, "peak": peak, "unit": "G packed row-ops/s",
                 "frac": (achieved / peak) if achieved else None,
-                "traffic": dram_bytes_per_launch(samples * bins / world),
-                "traffic_source": "ncu dram bytes of the 64-state light launch (profiles/k_terms_tp_c2_small.md), "
-                                  "scaled to this launch's states",
+                "traffic": dram_bytes_per_launch(samples * bins / world,
+                                                 "direct" if tuned[3] == 3 else "block prefix"),
+                "traffic_source": "ncu dram bytes of a 64-state launch of this kernel (profiles/%s), scaled to "
+                                  "this launch's states" % ("k_terms_direct_c2_small.md" if tuned[3] == 3
+                                                            else "k_terms_tp_c2_small.md"),
                 "work_unit": "packed row-op of the reference's algorithm (one 64-bit row test/XOR/update of its "
                              "elementary updates), whichever kernel runs",
                 "rowops_per_pair": per_pair,

@@ -13,8 +13,10 @@
 
 #if defined(__CUDACC__)
 #define CSIM_HD __host__ __device__
+#define CSIM_HD_INLINE __host__ __device__ __forceinline__
 #else
 #define CSIM_HD
+#define CSIM_HD_INLINE inline
 #endif
 
 namespace csim {
@@ -1150,6 +1152,102 @@ CSIM_HD inline int md_shrink(PairRegs& s, uint64_t& F, const PairMem& M, int q, 
     }
     return act ? 1 - beta : 1;
 }
+// One step of md_exp_sum's elimination: the monomer or dimer of the highest
+// row in E, its factors folded into W0 (and W1 when sidx >= 0), the rest of E
+// updated.  E and keep are carried in 64-bit words between steps, so the sum
+// can go on in 32-bit words once no lane has a row in play at or above 32.
+template <class W>
+CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64, int sidx, uint64_t& D1,
+                                uint64_t& D2, WAcc& w0, WAcc& w1, int& err) {
+    using T = WordTraits<W>;
+    W E = (W)E64;
+    const W keep = (W)keep64;
+    const bool live = E != (W)0;
+    const int KP = live ? 64 - hd_clz64((uint64_t)(E | keep | (sidx >= 0 ? wbit<W>(sidx) : (W)0))) : 0;
+    const int a = live ? T::bits - 1 - T::clz(E) : 0;
+    const W ra = live ? md_read_row<W>(M, a, KP) : (W)0;
+    const W K = ra & E & ~wbit<W>(a);
+    const bool dimer = K != (W)0;
+    const int b = dimer ? T::bits - 1 - T::clz(K) : 0;
+    const W rb = dimer ? md_read_row<W>(M, b, KP) : (W)0;
+    const int Da = 2 * (2 * getbit(D2, a) + getbit(D1, a));
+    if (live && !dimer) {  // monomer {a}
+        tp_factor_mono(w0, Da, err);
+        if (sidx >= 0) tp_factor_mono(w1, Da + 4 * wget<W>(ra, sidx), err);
+    }
+    if (dimer) {  // dimer {a, b}
+        const int Db = 2 * (2 * getbit(D2, b) + getbit(D1, b));
+        tp_factor_dimer(w0, Da, Db, err);
+        if (sidx >= 0) tp_factor_dimer(w1, Da + 4 * wget<W>(ra, sidx), Db + 4 * wget<W>(rb, sidx), err);
+    }
+    const W Ep = dimer ? (E & ~wbit<W>(a) & ~wbit<W>(b)) : (E & ~wbit<W>(a));
+    const W vb = dimer ? (ra & Ep) : (W)0, va = dimer ? (rb & Ep) : (W)0;
+    const bool upd = (vb | va) != (W)0;
+    const int jaa = wget<W>(ra, a), jbb = wget<W>(rb, b), jab = wget<W>(ra, b);
+    const W Cb = rb ^ (jbb ? vb : (W)0) ^ (jab ? va : (W)0);
+    const W Ca = ra ^ (jab ? vb : (W)0) ^ (jaa ? va : (W)0);
+    {
+        const W zm = upd ? (Ep | keep) : (W)0;
+        const int lo = zm ? T::ffs(zm) - 1 : T::bits, hi = zm ? T::bits - T::clz(zm) : 0;
+        const int X0 = uniform_min(lo) & ~3, X1 = uniform_max(hi);
+        if (live) CSIM_COUNT_ROWS((dimer ? 2 : 1) + (upd ? hi - lo : 0));
+        const W rvb = wbrev(vb), rva = wbrev(va), rcb = wbrev(Cb), rca = wbrev(Ca);
+        {
+            const int sh = T::bits - 32;
+            const int s0 = X0 < 32 ? X0 : 0;
+            const uint32_t rb32 = (uint32_t)rb, ra32 = (uint32_t)ra, vb32 = (uint32_t)vb, va32 = (uint32_t)va;
+            uint32_t cvb = (uint32_t)(rvb >> sh) << s0, cva = (uint32_t)(rva >> sh) << s0,
+                     ccb = (uint32_t)(rcb >> sh) << s0, cca = (uint32_t)(rca >> sh) << s0;
+            const int X1a = X1 < 32 ? X1 : 32;
+            for (int x = X0; x < X1a; x += 4) {
+                U32x4* pr = reinterpret_cast<U32x4*>(&R32(x));
+                U32x4 v = *pr;
+                v.a ^= (rb32 & topmask(cvb)) ^ (ra32 & topmask(cva)) ^ (vb32 & topmask(ccb)) ^
+                       (va32 & topmask(cca));
+                v.b ^= (rb32 & topmask(cvb << 1)) ^ (ra32 & topmask(cva << 1)) ^ (vb32 & topmask(ccb << 1)) ^
+                       (va32 & topmask(cca << 1));
+                v.c ^= (rb32 & topmask(cvb << 2)) ^ (ra32 & topmask(cva << 2)) ^ (vb32 & topmask(ccb << 2)) ^
+                       (va32 & topmask(cca << 2));
+                v.d ^= (rb32 & topmask(cvb << 3)) ^ (ra32 & topmask(cva << 3)) ^ (vb32 & topmask(ccb << 3)) ^
+                       (va32 & topmask(cca << 3));
+                cvb <<= 4;
+                cva <<= 4;
+                ccb <<= 4;
+                cca <<= 4;
+                *pr = v;
+            }
+        }
+        if (sizeof(W) == 8) {
+            const int x0 = X0 > 32 ? (X0 & ~1) : 32;
+            const int s1 = x0 & (T::bits - 1);
+            W cvb = rvb << s1, cva = rva << s1, ccb = rcb << s1, cca = rca << s1;
+            for (int x = x0; x < X1; x += 2) {
+                U64x2* pr = reinterpret_cast<U64x2*>(&R64(x));
+                U64x2 v = *pr;
+                v.a ^= (uint64_t)((rb & topmask(cvb)) ^ (ra & topmask(cva)) ^ (vb & topmask(ccb)) ^
+                                  (va & topmask(cca)));
+                v.b ^= (uint64_t)((rb & topmask((W)(cvb << 1))) ^ (ra & topmask((W)(cva << 1))) ^
+                                  (vb & topmask((W)(ccb << 1))) ^ (va & topmask((W)(cca << 1))));
+                cvb <<= 2;
+                cva <<= 2;
+                ccb <<= 2;
+                cca <<= 2;
+                *pr = v;
+            }
+        }
+    }
+    if (upd) {
+        const int db1 = getbit(D1, b), db2 = getbit(D2, b), da1 = getbit(D1, a), da2 = getbit(D2, a);
+        add_D64(D1, D2, (uint64_t)vb, db1, db2);
+        add_D64(D1, D2, (uint64_t)va, da1, da2);
+        W flip = (vb & rb) ^ (va & ra);
+        if (jab) flip ^= vb & va;
+        D2 ^= (uint64_t)flip;
+    }
+    if (live) E = Ep;
+    E64 = (uint64_t)E;
+}
+
 // exponentialSumExact (stabilizer.c:300-481) of the form over the live
 // variables F (coordinate-indexed rows, nothing compacted): first the
 // substitution that leaves one variable (sidx, the lowest with D odd) with D
@@ -1186,92 +1284,20 @@ CSIM_HD inline void md_exp_sum(PairRegs& s, const PairMem& M, uint64_t F, bool a
     WAcc w0 = {0, 0, 0}, w1 = {0, 0, 0};
     const bool any = E != (W)0;
     const int NE = uniform_max(T::popc(E));
-    for (int it = 0; it < NE; it++) {
-        if (uniform_max(E != (W)0 ? 1 : 0) == 0) break;
-        const bool live = E != (W)0;
-        KP = live ? 64 - hd_clz64((uint64_t)(E | keep | (sidx >= 0 ? wbit<W>(sidx) : (W)0))) : 0;
-        const int a = live ? T::bits - 1 - T::clz(E) : 0;
-        const W ra = live ? md_read_row<W>(M, a, KP) : (W)0;
-        const W K = ra & E & ~wbit<W>(a);
-        const bool dimer = K != (W)0;
-        const int b = dimer ? T::bits - 1 - T::clz(K) : 0;
-        const W rb = dimer ? md_read_row<W>(M, b, KP) : (W)0;
-        const int Da = 2 * (2 * getbit(D2, a) + getbit(D1, a));
-        if (live && !dimer) {  // monomer {a}
-            tp_factor_mono(w0, Da, err);
-            if (sidx >= 0) tp_factor_mono(w1, Da + 4 * wget<W>(ra, sidx), err);
-        }
-        if (dimer) {  // dimer {a, b}
-            const int Db = 2 * (2 * getbit(D2, b) + getbit(D1, b));
-            tp_factor_dimer(w0, Da, Db, err);
-            if (sidx >= 0) tp_factor_dimer(w1, Da + 4 * wget<W>(ra, sidx), Db + 4 * wget<W>(rb, sidx), err);
-        }
-        const W Ep = dimer ? (E & ~wbit<W>(a) & ~wbit<W>(b)) : (E & ~wbit<W>(a));
-        const W vb = dimer ? (ra & Ep) : (W)0, va = dimer ? (rb & Ep) : (W)0;
-        const bool upd = (vb | va) != (W)0;
-        const int jaa = wget<W>(ra, a), jbb = wget<W>(rb, b), jab = wget<W>(ra, b);
-        const W Cb = rb ^ (jbb ? vb : (W)0) ^ (jab ? va : (W)0);
-        const W Ca = ra ^ (jab ? vb : (W)0) ^ (jaa ? va : (W)0);
-        {
-            const W zm = upd ? (Ep | keep) : (W)0;
-            const int lo = zm ? T::ffs(zm) - 1 : T::bits, hi = zm ? T::bits - T::clz(zm) : 0;
-            const int X0 = uniform_min(lo) & ~3, X1 = uniform_max(hi);
-            if (live) CSIM_COUNT_ROWS((dimer ? 2 : 1) + (upd ? hi - lo : 0));
-            const W rvb = wbrev(vb), rva = wbrev(va), rcb = wbrev(Cb), rca = wbrev(Ca);
-            {
-                const int sh = T::bits - 32;
-                const int s0 = X0 < 32 ? X0 : 0;
-                const uint32_t rb32 = (uint32_t)rb, ra32 = (uint32_t)ra, vb32 = (uint32_t)vb, va32 = (uint32_t)va;
-                uint32_t cvb = (uint32_t)(rvb >> sh) << s0, cva = (uint32_t)(rva >> sh) << s0,
-                         ccb = (uint32_t)(rcb >> sh) << s0, cca = (uint32_t)(rca >> sh) << s0;
-                const int X1a = X1 < 32 ? X1 : 32;
-                for (int x = X0; x < X1a; x += 4) {
-                    U32x4* pr = reinterpret_cast<U32x4*>(&R32(x));
-                    U32x4 v = *pr;
-                    v.a ^= (rb32 & topmask(cvb)) ^ (ra32 & topmask(cva)) ^ (vb32 & topmask(ccb)) ^
-                           (va32 & topmask(cca));
-                    v.b ^= (rb32 & topmask(cvb << 1)) ^ (ra32 & topmask(cva << 1)) ^ (vb32 & topmask(ccb << 1)) ^
-                           (va32 & topmask(cca << 1));
-                    v.c ^= (rb32 & topmask(cvb << 2)) ^ (ra32 & topmask(cva << 2)) ^ (vb32 & topmask(ccb << 2)) ^
-                           (va32 & topmask(cca << 2));
-                    v.d ^= (rb32 & topmask(cvb << 3)) ^ (ra32 & topmask(cva << 3)) ^ (vb32 & topmask(ccb << 3)) ^
-                           (va32 & topmask(cca << 3));
-                    cvb <<= 4;
-                    cva <<= 4;
-                    ccb <<= 4;
-                    cca <<= 4;
-                    *pr = v;
-                }
-            }
-            if (sizeof(W) == 8) {
-                const int x0 = X0 > 32 ? (X0 & ~1) : 32;
-                const int s1 = x0 & (T::bits - 1);
-                W cvb = rvb << s1, cva = rva << s1, ccb = rcb << s1, cca = rca << s1;
-                for (int x = x0; x < X1; x += 2) {
-                    U64x2* pr = reinterpret_cast<U64x2*>(&R64(x));
-                    U64x2 v = *pr;
-                    v.a ^= (uint64_t)((rb & topmask(cvb)) ^ (ra & topmask(cva)) ^ (vb & topmask(ccb)) ^
-                                      (va & topmask(cca)));
-                    v.b ^= (uint64_t)((rb & topmask((W)(cvb << 1))) ^ (ra & topmask((W)(cva << 1))) ^
-                                      (vb & topmask((W)(ccb << 1))) ^ (va & topmask((W)(cca << 1))));
-                    cvb <<= 2;
-                    cva <<= 2;
-                    ccb <<= 2;
-                    cca <<= 2;
-                    *pr = v;
-                }
-            }
-        }
-        if (upd) {
-            const int db1 = getbit(D1, b), db2 = getbit(D2, b), da1 = getbit(D1, a), da2 = getbit(D2, a);
-            add_D64(D1, D2, (uint64_t)vb, db1, db2);
-            add_D64(D1, D2, (uint64_t)va, da1, da2);
-            W flip = (vb & rb) ^ (va & ra);
-            if (jab) flip ^= vb & va;
-            D2 ^= (uint64_t)flip;
-        }
-        if (live) E = Ep;
+    uint64_t E64 = (uint64_t)E;
+    int it = 0;
+    for (; it < NE; it++) {
+        if (uniform_max(E64 ? 1 : 0) == 0) break;
+        // rows below 32 alone (and sidx below 32): on in 32-bit words
+        if (sizeof(W) == 8 && uniform_max(64 - hd_clz64(E64 | (sidx >= 0 ? bit1(sidx) : 0ull))) <= CSIM_TP_WIDE_FROM)
+            break;
+        md_exp_step<W>(M, E64, (uint64_t)keep, sidx, D1, D2, w0, w1, err);
     }
+    if (sizeof(W) == 8)
+        for (; it < NE; it++) {
+            if (uniform_max(E64 ? 1 : 0) == 0) break;
+            md_exp_step<uint32_t>(M, E64, 0ull, sidx, D1, D2, w0, w1, err);
+        }
     if (!act) return;
     if (Fw == (W)0) {  // Wsigma's k == 0 case
         eps = 1;
@@ -1372,11 +1398,12 @@ CSIM_HD inline void pair_direct(bool valid, int n, const Canon& cs, const uint64
     const int NZ = uniform_max(nz);
     for (int it = 0; it < NZ; it++) {
         const bool act = alive && it < nz;
-        const bool wide = uniform_max(act && F ? 64 - hd_clz64(F) : 0) > 32;
+        const bool wide = uniform_max(act && F ? 64 - hd_clz64(F) : 0) > CSIM_TP_WIDE_FROM;
         const int r = wide ? md_shrink<uint64_t>(s, F, M, it, nz, act) : md_shrink<uint32_t>(s, F, M, it, nz, act);
         if (act && r == 0) alive = false;
     }
-    if (uniform_max(alive && F ? 64 - hd_clz64(F) : 0) > 32) md_exp_sum<uint64_t>(s, M, F, alive, eps, p, m, err);
+    const int KF = uniform_max(alive && F ? 64 - hd_clz64(F) : 0);  // highest live coordinate of the warp, + 1
+    if (KF > CSIM_TP_WIDE_FROM) md_exp_sum<uint64_t>(s, M, F, alive, eps, p, m, err);
     else md_exp_sum<uint32_t>(s, M, F, alive, eps, p, m, err);
     if (alive) p -= k0 + hd_popc64(x);
     else {
