@@ -947,8 +947,8 @@ CSIM_HD inline void pair_from_run(bool valid, int n, const RunState& rs, const P
 // pivot coordinate: that variable is simply absent.  Only the zeros of x at
 // the d = n - k non-pivot coordinates are constraints (md_shrink), after which
 // the form over the remaining variables goes to the exponential sum
-// (md_exp_sum).  Variables keep their coordinate index (rows of J are indexed
-// by coordinate; a mask F marks the live ones), so nothing is compacted.
+// (md_exp_sum).  Both run on rows indexed by variable under a live mask F;
+// pair_direct first renumbers x's live variables 0..f-1 (direct_compact).
 // The result is the same complex number as innerProductExact's; eps and p are
 // equal, m is equal mod 8 (the reference's unreduced m depends on its basis).
 // CSIM_COUNT_ROWS(r): the direct path touched r rows of J or constraint
@@ -1249,7 +1249,7 @@ CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64
 }
 
 // exponentialSumExact (stabilizer.c:300-481) of the form over the live
-// variables F (coordinate-indexed rows, nothing compacted): first the
+// variables F (rows indexed by variable, F marking the live ones): first the
 // substitution that leaves one variable (sidx, the lowest with D odd) with D
 // odd, then monomers and dimers taken from the highest live row down, so the
 // rows still in play shrink towards row 0.  W0/W1 and their combination as in
@@ -1342,54 +1342,145 @@ CSIM_HD inline void md_exp_sum(PairRegs& s, const PairMem& M, uint64_t F, bool a
     }
 }
 
-// One pair by direct restriction: theta in pivot coordinates (cs, Jc rows,
-// acol non-pivot masks), codeword x; working memory M with at least as many G
-// slots as x has zeros at non-pivot coordinates (dslots).  Same eps and p as
-// pair_l, m equal mod 8.  All lanes of a warp call it together.
-CSIM_HD inline void pair_direct(bool valid, int n, const Canon& cs, const uint64_t* Jc, const uint64_t* acol,
-                                uint64_t x, const PairMem& M, int& eps, int& p, int& m, int& err, int dslots, int k0) {
-    const uint64_t nm = lowmask(n);
-    uint64_t F = x & cs.P;
-    const uint64_t N = ~x & ~cs.P & nm;
-    if (valid && hd_popc64(N) > dslots) {
-        err |= kErrRange;
-        valid = false;
+// The bits of words at the ones of a fixed 32-bit mask m, packed to the low
+// end in order: the parallel-suffix compress of Hacker's Delight (Warren,
+// 2nd ed., section 7-4).  compress_net computes the five move masks of m
+// once; compress32 then moves a word's bits right by 1, 2, 4, 8 and 16.
+struct CompressNet {
+    uint32_t m, mv[5];
+};
+CSIM_HD_INLINE CompressNet compress_net(uint32_t m) {
+    CompressNet c;
+    c.m = m;
+    uint32_t mk = ~m << 1;  // ones where the count of zeros to the right changes parity
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+        uint32_t mp = mk ^ (mk << 1);  // prefix parity of mk: bits that move by 2^i in this round
+        mp ^= mp << 2;
+        mp ^= mp << 4;
+        mp ^= mp << 8;
+        mp ^= mp << 16;
+        const uint32_t mv = mp & m;
+        c.mv[i] = mv;
+        m = (m ^ mv) | (mv >> (1 << i));
+        mk &= ~mp;
     }
-    PairRegs s;
-    s.k = 0;
-    s.Q = cs.Q;
-    s.D1 = cs.D1;
-    s.D2 = cs.D2;
-    // J rows of every coordinate below the highest live one (whole 16-byte units)
-    const int KP = valid && F ? 64 - hd_clz64(F) : 0;
-    const int K = uniform_max(KP);
-    for (int u = 0; 4 * u < (K < 32 ? K : 32); u++)
-        if (4 * u < KP) {
+    return c;
+}
+CSIM_HD_INLINE uint32_t compress32(uint32_t x, const CompressNet& c) {
+    x &= c.m;
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+        const uint32_t t = x & c.mv[i];
+        x = (x ^ t) | (t >> (1 << i));
+    }
+    return x;
+}
+// A word compressed by the live mask: W = uint32_t when the mask has no bit at
+// or above 32 (the low net alone), else each half by its own net, the high
+// half's bits placed after the plo = popc(low half of the mask) low ones.
+template <class W>
+CSIM_HD_INLINE uint64_t compress_w(uint64_t x, const CompressNet& lo, const CompressNet& hi, int plo) {
+    const uint64_t l = compress32((uint32_t)x, lo);
+    if (sizeof(W) == 4) return l;
+    return l | ((uint64_t)compress32((uint32_t)(x >> 32), hi) << plo);
+}
+
+// The compacted form of one pair (pair_direct): live variable i is the i-th
+// coordinate of F0.  Writes J rows 0..f-1 (rows below 32 as their low halves,
+// four to a 16-byte unit; rows from 32 up whole), the constraint masks of the
+// zeros N at non-pivot coordinates (descending) with their right-hand sides
+// in hz, and D.  W = uint32_t when no lane of the warp has a live coordinate
+// at or above 32.
+template <class W>
+CSIM_HD_INLINE void direct_compact(const Canon& cs, const uint64_t* Jc, const uint64_t* acol, uint64_t F0, int f,
+                                   uint64_t N, const PairMem& M, PairRegs& s, int& nz, uint64_t& hz) {
+    using T = WordTraits<W>;
+    const CompressNet nlo = compress_net((uint32_t)F0);
+    CompressNet nhi = nlo;
+    int plo = 0;
+    if (sizeof(W) == 8) {
+        nhi = compress_net((uint32_t)(F0 >> 32));
+        plo = T::popc((W)(F0 & 0xffffffffull));
+    }
+    s.D1 = compress_w<W>(cs.D1, nlo, nhi, plo);
+    s.D2 = compress_w<W>(cs.D2, nlo, nhi, plo);
+    const int fmax = uniform_max(f);
+    W rem = (W)F0;
+    for (int u = 0; 4 * u < (fmax < 32 ? fmax : 32); u++) {
+        uint32_t w[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int c = rem ? T::ffs(rem) - 1 : 0;
+            rem &= rem - (W)1;
+            w[q] = 4 * u + q < f ? (uint32_t)compress_w<W>(Jc[c], nlo, nhi, plo) : 0u;
+        }
+        if (4 * u < f) {
             U32x4 v;
-            v.a = (uint32_t)Jc[4 * u];
-            v.b = (uint32_t)Jc[4 * u + 1];
-            v.c = (uint32_t)Jc[4 * u + 2];
-            v.d = (uint32_t)Jc[4 * u + 3];
+            v.a = w[0];
+            v.b = w[1];
+            v.c = w[2];
+            v.d = w[3];
             *reinterpret_cast<U32x4*>(&R32(4 * u)) = v;
         }
-    for (int r = 32; r < K; r += 2)
-        if (r < KP) {
-            U64x2 v;
-            v.a = Jc[r];
-            v.b = Jc[r + 1];
-            *reinterpret_cast<U64x2*>(&R64(r)) = v;
+    }
+    if (sizeof(W) == 8)
+        for (int r = 32; r < fmax; r += 2) {  // whole rows from 32 up
+            uint64_t w[2];
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const int c = rem ? T::ffs(rem) - 1 : 0;
+                rem &= rem - (W)1;
+                w[q] = r + q < f ? compress_w<W>(Jc[c], nlo, nhi, plo) : 0ull;
+            }
+            if (r < f) {
+                U64x2 v;
+                v.a = w[0];
+                v.b = w[1];
+                *reinterpret_cast<U64x2*>(&R64(r)) = v;
+            }
         }
-    CSIM_COUNT_ROWS(KP);
-    // the constraints: x's zeros at non-pivot coordinates, descending
-    int nz = 0;
-    uint64_t hz = 0ull;
-    for (uint64_t zz = valid ? N : 0ull; zz; nz++) {
+    CSIM_COUNT_ROWS(f);
+    nz = 0;
+    hz = 0ull;
+    for (uint64_t zz = N; zz; nz++) {
         const int c = 63 - hd_clz64(zz);
         zz &= ~bit1(c);
-        RG(nz) = acol[c];
+        RG(nz) = compress_w<W>(acol[c], nlo, nhi, plo);
         hz |= (uint64_t)getbit(cs.bm, c) << nz;
     }
     CSIM_COUNT_ROWS(nz);
+}
+
+// One pair by direct restriction: theta in pivot coordinates (cs, Jc rows,
+// acol non-pivot masks), codeword x; working memory M with at least as many G
+// slots as x has zeros at non-pivot coordinates (dslots).  The live variables
+// F = x & P are renumbered 0..f-1 in coordinate order (rows, their bits, the
+// constraint masks and D compressed by F), so the constraints and the
+// exponential sum run on f rows with nothing dead in between, in 32-bit words
+// while the warp's f stays at or below 32.  The renumbering keeps the order of
+// the variables, so each step eliminates the same variable as on coordinate
+// indices.  Same eps and p as pair_l, m equal mod 8.  All lanes of a warp call
+// it together.
+CSIM_HD inline void pair_direct(bool valid, int n, const Canon& cs, const uint64_t* Jc, const uint64_t* acol,
+                                uint64_t x, const PairMem& M, int& eps, int& p, int& m, int& err, int dslots, int k0) {
+    const uint64_t nm = lowmask(n);
+    const uint64_t N0 = ~x & ~cs.P & nm;
+    if (valid && hd_popc64(N0) > dslots) {
+        err |= kErrRange;
+        valid = false;
+    }
+    const uint64_t F0 = valid ? x & cs.P : 0ull;
+    const uint64_t N = valid ? N0 : 0ull;
+    const int f = hd_popc64(F0);
+    PairRegs s;
+    s.k = 0;
+    s.Q = cs.Q;
+    int nz;
+    uint64_t hz;
+    if (uniform_max((F0 >> 32) != 0ull ? 1 : 0)) direct_compact<uint64_t>(cs, Jc, acol, F0, f, N, M, s, nz, hz);
+    else direct_compact<uint32_t>(cs, Jc, acol, F0, f, N, M, s, nz, hz);
+    uint64_t F = lowmask(f);
     s.h = hz;
     eps = 0;
     p = 0;
