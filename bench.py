@@ -123,7 +123,7 @@ class ClockSampler:
 ROWOPS_PER_PAIR_T40 = 2576.0
 # Rows of J and constraint masks the direct-restriction path reads, copies or
 # updates per c2 pair (the same 9600 pairs, CSIM_COUNT_ROWS hook of the host build).
-DIRECT_ROWS_PER_PAIR_T40 = 265.4
+DIRECT_ROWS_PER_PAIR_T40 = 151.1
 
 
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one pair-kernel launch over
