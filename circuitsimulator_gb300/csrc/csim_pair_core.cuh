@@ -443,7 +443,9 @@ CSIM_HD inline void tp_factor_mono(WAcc& w, int A, int& err) {
 // one dimer factor Gamma(A, B), A and B even and non-negative (kGammaCodes)
 CSIM_HD inline void tp_factor_dimer(WAcc& w, int A, int B, int& err) {
     if (((A | B) & 1) || A < 0 || B < 0) err |= kErrGamma;
-    const int code = (int)((kGammaCodes >> (4 * (4 * ((A & 7) >> 1) + ((B & 7) >> 1)))) & 15);
+    const int idx = 4 * ((A & 7) >> 1) + ((B & 7) >> 1);
+    const uint32_t half = (idx & 8) ? (uint32_t)(kGammaCodes >> 32) : (uint32_t)kGammaCodes;
+    const int code = (int)((half >> (4 * (idx & 7))) & 15u);
     const int z = code >> 3;
     w.zero |= z;
     w.p += z ? 0 : 2;
@@ -979,6 +981,13 @@ CSIM_HD inline void add_D64(uint64_t& D1, uint64_t& D2, uint64_t u, int d1, int 
     D1 ^= a1;
     D2 ^= a2 ^ c;
 }
+// the same in the words of the exponential sum's mode
+template <class W>
+CSIM_HD_INLINE void add_Dw(W& D1, W& D2, W u, int d1, int d2) {
+    const W a1 = d1 ? u : (W)0, a2 = d2 ? u : (W)0, c = D1 & a1;
+    D1 ^= a1;
+    D2 ^= a2 ^ c;
+}
 
 // theta (n qubits, k, Q, h, D1, D2, G rows, J rows as in csim_state) in pivot
 // coordinates.  Jc[c], acol[c] for c < n: J row of variable c (0 for a
@@ -1157,8 +1166,8 @@ CSIM_HD inline int md_shrink(PairRegs& s, uint64_t& F, const PairMem& M, int q, 
 // updated.  E and keep are carried in 64-bit words between steps, so the sum
 // can go on in 32-bit words once no lane has a row in play at or above 32.
 template <class W>
-CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64, int sidx, uint64_t& D1,
-                                uint64_t& D2, WAcc& w0, WAcc& w1, int& err) {
+CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64, int sidx, W& D1, W& D2, WAcc& w0,
+                                WAcc& w1, int& err) {
     using T = WordTraits<W>;
     W E = (W)E64;
     const W keep = (W)keep64;
@@ -1170,13 +1179,13 @@ CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64
     const bool dimer = K != (W)0;
     const int b = dimer ? T::bits - 1 - T::clz(K) : 0;
     const W rb = dimer ? md_read_row<W>(M, b, KP) : (W)0;
-    const int Da = 2 * (2 * getbit(D2, a) + getbit(D1, a));
+    const int Da = 2 * (2 * wget<W>(D2, a) + wget<W>(D1, a));
     if (live && !dimer) {  // monomer {a}
         tp_factor_mono(w0, Da, err);
         if (sidx >= 0) tp_factor_mono(w1, Da + 4 * wget<W>(ra, sidx), err);
     }
     if (dimer) {  // dimer {a, b}
-        const int Db = 2 * (2 * getbit(D2, b) + getbit(D1, b));
+        const int Db = 2 * (2 * wget<W>(D2, b) + wget<W>(D1, b));
         tp_factor_dimer(w0, Da, Db, err);
         if (sidx >= 0) tp_factor_dimer(w1, Da + 4 * wget<W>(ra, sidx), Db + 4 * wget<W>(rb, sidx), err);
     }
@@ -1237,12 +1246,12 @@ CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64
         }
     }
     if (upd) {
-        const int db1 = getbit(D1, b), db2 = getbit(D2, b), da1 = getbit(D1, a), da2 = getbit(D2, a);
-        add_D64(D1, D2, (uint64_t)vb, db1, db2);
-        add_D64(D1, D2, (uint64_t)va, da1, da2);
+        const int db1 = wget<W>(D1, b), db2 = wget<W>(D2, b), da1 = wget<W>(D1, a), da2 = wget<W>(D2, a);
+        add_Dw<W>(D1, D2, vb, db1, db2);
+        add_Dw<W>(D1, D2, va, da1, da2);
         W flip = (vb & rb) ^ (va & ra);
         if (jab) flip ^= vb & va;
-        D2 ^= (uint64_t)flip;
+        D2 ^= flip;
     }
     if (live) E = Ep;
     E64 = (uint64_t)E;
@@ -1259,8 +1268,8 @@ CSIM_HD inline void md_exp_sum(PairRegs& s, const PairMem& M, uint64_t F, bool a
                                int& err) {
     using T = WordTraits<W>;
     const W Fw = act ? (W)F : (W)0;
-    uint64_t D1 = s.D1, D2 = s.D2;
-    const W Sm = (W)D1 & Fw;
+    W D1 = (W)s.D1, D2 = (W)s.D2;  // bits of live variables only (all below 32 in 32-bit mode)
+    const W Sm = D1 & Fw;
     int sidx = -1;
     int KP = Fw ? 64 - hd_clz64((uint64_t)Fw) : 0;
     {
@@ -1273,8 +1282,8 @@ CSIM_HD inline void md_exp_sum(PairRegs& s, const PairMem& M, uint64_t F, bool a
         if (upd && U != (W)0) md_rank2<W>(M, KX, Ja, U, C);
         if (upd) CSIM_COUNT_ROWS(U != (W)0 ? 1 + KP : 1);
         if (upd) {
-            add_D64(D1, D2, (uint64_t)U, getbit(D1, a), getbit(D2, a));
-            D2 ^= (uint64_t)(U & Ja);
+            add_Dw<W>(D1, D2, U, wget<W>(D1, a), wget<W>(D2, a));
+            D2 ^= U & Ja;
             sidx = a;
         }
     }
@@ -1293,11 +1302,15 @@ CSIM_HD inline void md_exp_sum(PairRegs& s, const PairMem& M, uint64_t F, bool a
             break;
         md_exp_step<W>(M, E64, (uint64_t)keep, sidx, D1, D2, w0, w1, err);
     }
-    if (sizeof(W) == 8)
+    if (sizeof(W) == 8 && it < NE) {
+        uint32_t d1 = (uint32_t)D1, d2 = (uint32_t)D2;  // the rest of E and sidx lie below 32
         for (; it < NE; it++) {
             if (uniform_max(E64 ? 1 : 0) == 0) break;
-            md_exp_step<uint32_t>(M, E64, 0ull, sidx, D1, D2, w0, w1, err);
+            md_exp_step<uint32_t>(M, E64, 0ull, sidx, d1, d2, w0, w1, err);
         }
+        D1 = (W)d1;
+        D2 = (W)d2;
+    }
     if (!act) return;
     if (Fw == (W)0) {  // Wsigma's k == 0 case
         eps = 1;
@@ -1305,7 +1318,7 @@ CSIM_HD inline void md_exp_sum(PairRegs& s, const PairMem& M, uint64_t F, bool a
         m = s.Q;
         return;
     }
-    const int tM0 = s.Q, tM1 = s.Q + (sidx >= 0 ? 2 * (2 * getbit(D2, sidx) + getbit(D1, sidx)) : 0);
+    const int tM0 = s.Q, tM1 = s.Q + (sidx >= 0 ? 2 * (2 * wget<W>(D2, sidx) + wget<W>(D1, sidx)) : 0);
     const int e0 = !w0.zero, p0 = w0.zero ? 0 : w0.p, m0 = w0.zero ? 0 : (any ? (tM0 + w0.m) % 8 : tM0);
     if (sidx < 0) {
         eps = e0;
@@ -1344,22 +1357,22 @@ CSIM_HD inline void md_exp_sum(PairRegs& s, const PairMem& M, uint64_t F, bool a
 
 // The bits of words at the ones of a fixed 32-bit mask m, packed to the low
 // end in order: the parallel-suffix compress of Hacker's Delight (Warren,
-// 2nd ed., section 7-4).  compress_net computes the five move masks of m
-// once; compress32 then moves a word's bits right by 1, 2, 4, 8 and 16.
+// 2nd ed., section 7-4).  compress_net computes the move masks of m once;
+// compress32 then moves a word's bits right by 1, 2, 4, ...  R rounds move a
+// bit by up to 2^R - 1, which is enough when m has no bit at or above 2^R.
 struct CompressNet {
     uint32_t m, mv[5];
 };
+template <int R>
 CSIM_HD_INLINE CompressNet compress_net(uint32_t m) {
     CompressNet c;
     c.m = m;
     uint32_t mk = ~m << 1;  // ones where the count of zeros to the right changes parity
 #pragma unroll
-    for (int i = 0; i < 5; i++) {
-        uint32_t mp = mk ^ (mk << 1);  // prefix parity of mk: bits that move by 2^i in this round
-        mp ^= mp << 2;
-        mp ^= mp << 4;
-        mp ^= mp << 8;
-        mp ^= mp << 16;
+    for (int i = 0; i < R; i++) {
+        uint32_t mp = mk ^ (mk << 1);  // prefix parity of mk: the bits that move by 2^i this round
+#pragma unroll
+        for (int j = 1; j < R; j++) mp ^= mp << (1 << j);
         const uint32_t mv = mp & m;
         c.mv[i] = mv;
         m = (m ^ mv) | (mv >> (1 << i));
@@ -1367,53 +1380,67 @@ CSIM_HD_INLINE CompressNet compress_net(uint32_t m) {
     }
     return c;
 }
+template <int R>
 CSIM_HD_INLINE uint32_t compress32(uint32_t x, const CompressNet& c) {
     x &= c.m;
 #pragma unroll
-    for (int i = 0; i < 5; i++) {
+    for (int i = 0; i < R; i++) {
         const uint32_t t = x & c.mv[i];
         x = (x ^ t) | (t >> (1 << i));
     }
     return x;
 }
-// A word compressed by the live mask: W = uint32_t when the mask has no bit at
-// or above 32 (the low net alone), else each half by its own net, the high
-// half's bits placed after the plo = popc(low half of the mask) low ones.
-template <class W>
-CSIM_HD_INLINE uint64_t compress_w(uint64_t x, const CompressNet& lo, const CompressNet& hi, int plo) {
-    const uint64_t l = compress32((uint32_t)x, lo);
-    if (sizeof(W) == 4) return l;
-    return l | ((uint64_t)compress32((uint32_t)(x >> 32), hi) << plo);
+// x << s within 32 bits, 0 for s == 32
+CSIM_HD_INLINE uint32_t shl32_upto32(uint32_t x, int s) {
+#if defined(__CUDA_ARCH__)
+    return __funnelshift_lc(0u, x, (unsigned)s);
+#else
+    return s >= 32 ? 0u : x << s;
+#endif
+}
+
+// How pair_direct compresses a pair's words, by the warp's live coordinates:
+// all below 32 (kCompactLow); some at or above 32 but at most 32 live
+// variables in every lane, so every compressed word fits 32 bits
+// (kCompactSplit: each half by its own net, the high net with RHI rounds for
+// coordinates below 32 + 2^RHI); more than 32 live variables in some lane
+// (kCompactWide: 64-bit words, rows from 32 up whole).
+enum { kCompactLow = 0, kCompactSplit = 1, kCompactWide = 2 };
+
+template <int MODE, int RHI>
+CSIM_HD_INLINE uint64_t compress_word(uint64_t x, const CompressNet& lo, const CompressNet& hi, int plo) {
+    const uint32_t l = compress32<5>((uint32_t)x, lo);
+    if (MODE == kCompactLow) return l;
+    const uint32_t h = compress32<RHI>((uint32_t)(x >> 32), hi);
+    if (MODE == kCompactSplit) return l | shl32_upto32(h, plo);
+    return l | ((uint64_t)h << plo);
 }
 
 // The compacted form of one pair (pair_direct): live variable i is the i-th
 // coordinate of F0.  Writes J rows 0..f-1 (rows below 32 as their low halves,
-// four to a 16-byte unit; rows from 32 up whole), the constraint masks of the
-// zeros N at non-pivot coordinates (descending) with their right-hand sides
-// in hz, and D.  W = uint32_t when no lane of the warp has a live coordinate
-// at or above 32.
-template <class W>
+// four to a 16-byte unit; rows from 32 up whole, kCompactWide only), the
+// constraint masks of the zeros N at non-pivot coordinates (descending) with
+// their right-hand sides in hz, and D.  Rows from f up to the warp's largest
+// f, within the last 16-byte unit, get words that no step reads.
+template <int MODE, int RHI>
 CSIM_HD_INLINE void direct_compact(const Canon& cs, const uint64_t* Jc, const uint64_t* acol, uint64_t F0, int f,
                                    uint64_t N, const PairMem& M, PairRegs& s, int& nz, uint64_t& hz) {
-    using T = WordTraits<W>;
-    const CompressNet nlo = compress_net((uint32_t)F0);
-    CompressNet nhi = nlo;
-    int plo = 0;
-    if (sizeof(W) == 8) {
-        nhi = compress_net((uint32_t)(F0 >> 32));
-        plo = T::popc((W)(F0 & 0xffffffffull));
-    }
-    s.D1 = compress_w<W>(cs.D1, nlo, nhi, plo);
-    s.D2 = compress_w<W>(cs.D2, nlo, nhi, plo);
+    const CompressNet nlo = compress_net<5>((uint32_t)F0);
+    const CompressNet nhi = MODE == kCompactLow ? nlo : compress_net<RHI>((uint32_t)(F0 >> 32));
+    const int plo = MODE == kCompactLow ? 0 : WordTraits<uint32_t>::popc((uint32_t)F0);
+    s.D1 = compress_word<MODE, RHI>(cs.D1, nlo, nhi, plo);
+    s.D2 = compress_word<MODE, RHI>(cs.D2, nlo, nhi, plo);
     const int fmax = uniform_max(f);
-    W rem = (W)F0;
+    uint32_t rl = (uint32_t)F0, rh = (uint32_t)(F0 >> 32);  // live coordinates not yet taken
     for (int u = 0; 4 * u < (fmax < 32 ? fmax : 32); u++) {
         uint32_t w[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            const int c = rem ? T::ffs(rem) - 1 : 0;
-            rem &= rem - (W)1;
-            w[q] = 4 * u + q < f ? (uint32_t)compress_w<W>(Jc[c], nlo, nhi, plo) : 0u;
+            const bool inlo = MODE == kCompactLow || rl != 0u;
+            const int c = inlo ? WordTraits<uint32_t>::ffs(rl) - 1 : 31 + WordTraits<uint32_t>::ffs(rh);
+            if (inlo) rl &= rl - 1u;
+            else rh &= rh - 1u;
+            w[q] = (uint32_t)compress_word<MODE, RHI>(Jc[c & 63], nlo, nhi, plo);
         }
         if (4 * u < f) {
             U32x4 v;
@@ -1424,14 +1451,16 @@ CSIM_HD_INLINE void direct_compact(const Canon& cs, const uint64_t* Jc, const ui
             *reinterpret_cast<U32x4*>(&R32(4 * u)) = v;
         }
     }
-    if (sizeof(W) == 8)
+    if (MODE == kCompactWide)
         for (int r = 32; r < fmax; r += 2) {  // whole rows from 32 up
             uint64_t w[2];
 #pragma unroll
             for (int q = 0; q < 2; q++) {
-                const int c = rem ? T::ffs(rem) - 1 : 0;
-                rem &= rem - (W)1;
-                w[q] = r + q < f ? compress_w<W>(Jc[c], nlo, nhi, plo) : 0ull;
+                const bool inlo = rl != 0u;
+                const int c = inlo ? WordTraits<uint32_t>::ffs(rl) - 1 : 31 + WordTraits<uint32_t>::ffs(rh);
+                if (inlo) rl &= rl - 1u;
+                else rh &= rh - 1u;
+                w[q] = compress_word<MODE, RHI>(Jc[c & 63], nlo, nhi, plo);
             }
             if (r < f) {
                 U64x2 v;
@@ -1446,7 +1475,7 @@ CSIM_HD_INLINE void direct_compact(const Canon& cs, const uint64_t* Jc, const ui
     for (uint64_t zz = N; zz; nz++) {
         const int c = 63 - hd_clz64(zz);
         zz &= ~bit1(c);
-        RG(nz) = compress_w<W>(acol[c], nlo, nhi, plo);
+        RG(nz) = compress_word<MODE, RHI>(acol[c], nlo, nhi, plo);
         hz |= (uint64_t)getbit(cs.bm, c) << nz;
     }
     CSIM_COUNT_ROWS(nz);
@@ -1478,8 +1507,13 @@ CSIM_HD inline void pair_direct(bool valid, int n, const Canon& cs, const uint64
     s.Q = cs.Q;
     int nz;
     uint64_t hz;
-    if (uniform_max((F0 >> 32) != 0ull ? 1 : 0)) direct_compact<uint64_t>(cs, Jc, acol, F0, f, N, M, s, nz, hz);
-    else direct_compact<uint32_t>(cs, Jc, acol, F0, f, N, M, s, nz, hz);
+    // the warp's highest live coordinate (+ 1) and largest live count choose the compress
+    const int top = uniform_max(F0 ? 64 - hd_clz64(F0) : 0);
+    if (top <= 32) direct_compact<kCompactLow, 0>(cs, Jc, acol, F0, f, N, M, s, nz, hz);
+    else if (uniform_max(f) > 32) direct_compact<kCompactWide, 5>(cs, Jc, acol, F0, f, N, M, s, nz, hz);
+    else if (top <= 40) direct_compact<kCompactSplit, 3>(cs, Jc, acol, F0, f, N, M, s, nz, hz);
+    else if (top <= 48) direct_compact<kCompactSplit, 4>(cs, Jc, acol, F0, f, N, M, s, nz, hz);
+    else direct_compact<kCompactSplit, 5>(cs, Jc, acol, F0, f, N, M, s, nz, hz);
     uint64_t F = lowmask(f);
     s.h = hz;
     eps = 0;
