@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(kTPB) k_items_direct(const PairItem* items, in
                     if (__all_sync(kFull, !valid)) break;  // warp-uniform exit
                     const uint64_t x = valid ? it.cw[j] : 0ull;
                     int eps = 0, pp = 0, mm = 0;
-                    pc::pair_direct(valid, n, sh.cs, sJ, sA, x, mem, eps, pp, mm, e, dslots, sh.cs.k);
+                    pc::pair_direct(valid, n, sh.cs, sJ, sA, x, mem, eps, pp, mm, e, dslots, sh.cs.k, nmax);
                     if (!valid) continue;
                     pc::zacc(z, eps, pp, mm, P, e);
                     if (j == it.diag) {

@@ -667,9 +667,18 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
                 // direct kernel: every term of the states it takes; the rest (or all, for kernel 0) below
                 const int* rcode = scode;
                 if (tn.kernel == 3) {
-                    rc |= csim::launch_terms_direct(launch_of(ctx), t, dsl, dcw,
-                                                    (const unsigned char*)dcanon + (size_t)s0 * csim::canon_bytes(),
-                                                    dcode_dir + s0, cs, 0, chi, pt, P2, spart, nchunks, 0);
+                    // above 32 qubits the table's heavy part [0, cw_split) holds the codewords of at most 32
+                    // ones (direct_light), whose pairs need 32 J rows: a launch of its own with smaller
+                    // per-pair memory; the rest (from its first whole item) with rows for every coordinate
+                    const unsigned char* cb = (const unsigned char*)dcanon + (size_t)s0 * csim::canon_bytes();
+                    const int64_t span = 64 * (int64_t)pt;
+                    const int64_t jn = t > 32 ? std::min(chi, ctx->cw_split / span * span) : 0;
+                    if (jn > 0)
+                        rc |= csim::launch_terms_direct(launch_of(ctx), t, 32, dsl, dcw, cb, dcode_dir + s0, cs, 0,
+                                                        jn, pt, P2, spart, nchunks, 0);
+                    if (jn < chi)
+                        rc |= csim::launch_terms_direct(launch_of(ctx), t, t, dsl, dcw + jn, cb, dcode_dir + s0, cs,
+                                                        jn, chi - jn, pt, P2, spart, nchunks, jn / span);
                     rcode = dcode_rest + s0;
                 }
                 // terms [0, jb): every zero count; terms [jb, chi): at most tn.light zeros
@@ -852,6 +861,7 @@ int tune_for(csim_ctx* ctx, int t, TpTune* out, const csim_projector* P, const u
     if (t < 1 || t > CSIM_MAX_QUBITS) return fail(ctx, CSIM_ERR_ARG, "t=%d outside 1..64", t);
     if (ctx->tuning) {
         *out = ctx->trial;
+        if (out->kernel == 3) out->light = direct_light(t);
         return 0;
     }
     TpTune r = default_tune(t);
@@ -873,6 +883,7 @@ int tune_for(csim_ctx* ctx, int t, TpTune* out, const csim_projector* P, const u
         r.light = light_zeros(t);
     }
     if (ctx->per_thread > 0) r.per_thread = ctx->per_thread;
+    if (r.kernel == 3) r.light = direct_light(t);
     *out = r;
     return 0;
 }
@@ -891,6 +902,7 @@ extern "C" int csim_autotune(csim_ctx* ctx, int32_t t, const csim_projector* P, 
         CKR(tune_run(ctx, t, P, L, k));
         if (!tuned_get(ctx->device, t, &tn, &ms)) return fail(ctx, CSIM_ERR_CUDA, "tuning left no result");
     }
+    if (tn.kernel == 3) tn.light = direct_light(t);
     if (kernel) *kernel = tn.kernel;
     if (per_thread) *per_thread = tn.per_thread;
     if (light_zeros_out) *light_zeros_out = tn.light;

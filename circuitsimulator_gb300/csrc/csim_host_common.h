@@ -170,6 +170,11 @@ struct TpTune {
 // constraint slots per pair of the direct kernel: states with more non-pivot
 // coordinates (n - k) than this go to the block-prefix kernel
 inline int direct_slots(int t) { return std::min(t, 8); }
+// The direct kernel's light bound: above 32 qubits the table's heavy part
+// (more than t - 33 zeros) holds the codewords of at most 32 ones, whose pairs
+// have at most 32 live variables; the block-prefix launches of the states
+// left to them use the same bound.
+inline int direct_light(int t) { return t > 32 ? t - 33 : light_zeros(t); }
 inline TpTune default_tune(int t) {
     TpTune r;
     r.per_thread = auto_per_thread(t);

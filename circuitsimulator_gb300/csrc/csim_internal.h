@@ -61,13 +61,15 @@ int terms_tp_occupancy(int nmax, int gmax);
 // dslots get code_direct = -1 and keep their code in code_rest (for the
 // block-prefix kernel), the others the reverse.  launch_terms_direct: all pairs
 // of the states with code >= 0 against codewords [j0, j0 + nj), partial sums as
-// launch_terms_tp's (only live states write theirs).
+// launch_terms_tp's (only live states write theirs); `rows` (<= nmax) bounds the
+// ones of every codeword in the range, which sizes the per-pair rows (a pair
+// with more live variables sets the range error).
 size_t canon_bytes();
 int launch_canon(const Launch& L, const GState* theta, const int* code, int64_t ntheta, int dslots, void* canon,
                  int* code_direct, int* code_rest);
-int launch_terms_direct(const Launch& L, int nmax, int dslots, const uint64_t* codewords, const void* canon,
-                        const int* code, int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P,
-                        __int128* part, int64_t part_stride, int64_t part_base);
+int launch_terms_direct(const Launch& L, int nmax, int rows, int dslots, const uint64_t* codewords,
+                        const void* canon, const int* code, int64_t ntheta, int64_t j0, int64_t nj, int per_thread,
+                        int P, __int128* part, int64_t part_stride, int64_t part_base);
 
 // the run kernel (csim_terms_tp.cu): codewords [j0, j0 + nj) in run order
 // (csim_host::run_ordered_codewords), runs of per_thread codewords, partial

@@ -1482,8 +1482,9 @@ CSIM_HD_INLINE void direct_compact(const Canon& cs, const uint64_t* Jc, const ui
 }
 
 // One pair by direct restriction: theta in pivot coordinates (cs, Jc rows,
-// acol non-pivot masks), codeword x; working memory M with at least as many G
-// slots as x has zeros at non-pivot coordinates (dslots).  The live variables
+// acol non-pivot masks), codeword x; working memory M with `rows` J rows (at
+// least x's live variables) and at least as many G slots as x has zeros at
+// non-pivot coordinates (dslots).  The live variables
 // F = x & P are renumbered 0..f-1 in coordinate order (rows, their bits, the
 // constraint masks and D compressed by F), so the constraints and the
 // exponential sum run on f rows with nothing dead in between, in 32-bit words
@@ -1492,10 +1493,11 @@ CSIM_HD_INLINE void direct_compact(const Canon& cs, const uint64_t* Jc, const ui
 // indices.  Same eps and p as pair_l, m equal mod 8.  All lanes of a warp call
 // it together.
 CSIM_HD inline void pair_direct(bool valid, int n, const Canon& cs, const uint64_t* Jc, const uint64_t* acol,
-                                uint64_t x, const PairMem& M, int& eps, int& p, int& m, int& err, int dslots, int k0) {
+                                uint64_t x, const PairMem& M, int& eps, int& p, int& m, int& err, int dslots, int k0,
+                                int rows) {
     const uint64_t nm = lowmask(n);
     const uint64_t N0 = ~x & ~cs.P & nm;
-    if (valid && hd_popc64(N0) > dslots) {
+    if (valid && (hd_popc64(N0) > dslots || hd_popc64(x & cs.P) > rows)) {
         err |= kErrRange;
         valid = false;
     }

@@ -187,8 +187,8 @@ struct DirectShared {
 
 __global__ void __launch_bounds__(kTP) k_terms_direct(const uint64_t* codewords, const CanonG* canon, const int* code,
                                                       int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P,
-                                                      int nmax, int dslots, __int128* part, int64_t part_stride,
-                                                      int64_t part_base, int* err) {
+                                                      int nmax, int rows, int dslots, __int128* part,
+                                                      int64_t part_stride, int64_t part_base, int* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     DirectShared& sh = *reinterpret_cast<DirectShared*>(smem_raw);
     uint64_t* const sJ = reinterpret_cast<uint64_t*>(smem_raw + sizeof(DirectShared));  // 64 rows, then 64 masks
@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(kTP) k_terms_direct(const uint64_t* codewords,
     unsigned char* const pair_base = smem_raw + sizeof(DirectShared) + 2 * 64 * 8;
     const int tid = threadIdx.x;
     int e = 0;
-    const pc::PairMem mem = pc::pair_mem(pair_base, nmax, kTP, tid);
+    const pc::PairMem mem = pc::pair_mem(pair_base, rows, kTP, tid);
     const int64_t span = (int64_t)kTP * per_thread;
     const int64_t nblk = (nj + span - 1) / span;
     const int64_t items = ntheta * nblk;
@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(kTP) k_terms_direct(const uint64_t* codewords,
                 if (__all_sync(kFull, !valid)) break;  // warp-uniform exit
                 const uint64_t x = valid ? codewords[j - j0] : 0ull;
                 int eps = 0, pp = 0, mm = 0;
-                pc::pair_direct(valid, n, sh.cs, sJ, sA, x, mem, eps, pp, mm, e, dslots, sh.cs.k);
+                pc::pair_direct(valid, n, sh.cs, sJ, sA, x, mem, eps, pp, mm, e, dslots, sh.cs.k, rows);
                 if (valid) pc::zacc(z, eps, pp, mm, P, e);
             }
         }
@@ -259,11 +259,12 @@ size_t terms_direct_smem(int nmax, int dslots) {
 }
 }  // namespace
 
-int launch_terms_direct(const Launch& L, int nmax, int dslots, const uint64_t* codewords, const void* canon,
-                        const int* code, int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P,
-                        __int128* part, int64_t part_stride, int64_t part_base) {
+int launch_terms_direct(const Launch& L, int nmax, int rows, int dslots, const uint64_t* codewords,
+                        const void* canon, const int* code, int64_t ntheta, int64_t j0, int64_t nj, int per_thread,
+                        int P, __int128* part, int64_t part_stride, int64_t part_base) {
     if (ntheta <= 0 || nj <= 0) return 0;
-    if (nmax < 1 || nmax > 64 || dslots < 0 || dslots > nmax || per_thread < 1 || !part || !canon || !code)
+    if (nmax < 1 || nmax > 64 || rows < 1 || rows > nmax || dslots < 0 || dslots > nmax || per_thread < 1 || !part ||
+        !canon || !code)
         return -1;
     const int64_t span = (int64_t)kTP * per_thread;
     const int64_t nblk = (nj + span - 1) / span;
@@ -271,15 +272,15 @@ int launch_terms_direct(const Launch& L, int nmax, int dslots, const uint64_t* c
     if (cudaFuncSetAttribute(k_terms_direct, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)terms_direct_smem(64, 64)) != cudaSuccess)
         return -1;
-    const size_t smem = terms_direct_smem(nmax, dslots);
+    const size_t smem = terms_direct_smem(rows, dslots);
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_terms_direct, kTP, smem) != cudaSuccess || per_sm < 1)
         per_sm = 1;
     int64_t grid = (int64_t)L.num_sms * per_sm;
     if (grid > ntheta * nblk) grid = ntheta * nblk;
     k_terms_direct<<<(int)grid, kTP, smem, L.stream>>>(codewords, (const CanonG*)canon, code, ntheta, j0, nj,
-                                                        per_thread, P, nmax, dslots, part, part_stride, part_base,
-                                                        L.d_err);
+                                                        per_thread, P, nmax, rows, dslots, part, part_stride,
+                                                        part_base, L.d_err);
     (*L.launches)++;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -181,7 +181,7 @@ extern "C" int tp_host_direct(const csim_state* theta, int ntheta, const uint64_
         canon_theta(th.n, th.k, th.Q, th.h, th.D1, th.D2, th.G, th.J, Jc, acol, cs);
         for (int j = 0; j < nx; j++) {
             const int w = a * nx + j;
-            pair_direct(true, th.n, cs, Jc, acol, xs[j], mem, eps[w], p[w], m[w], err, 64, th.k);
+            pair_direct(true, th.n, cs, Jc, acol, xs[j], mem, eps[w], p[w], m[w], err, 64, th.k, 64);
         }
     }
     return err;

@@ -225,7 +225,10 @@ def test_autotuner_leaves_results_and_streams_unchanged():
         for t in (22, 45):
             pt, lz, ms, kern = a.autotune(t)
             assert pt in (16, 32) and kern in (0, 1, 2, 3) and ms > 0, (t, pt, lz, kern)
-            assert kern == 2 or lz in {min(t, (f * t + 99) // 100) for f in (50, 55, 60, 70)}, (t, lz)
+            if kern == 3:  # the direct kernel's own bound: t - 33 above 32 qubits, else ceil(0.6 t)
+                assert lz == (t - 33 if t > 32 else min(t, (3 * t + 4) // 5)), (t, lz)
+            else:
+                assert kern == 2 or lz in {min(t, (f * t + 99) // 100) for f in (50, 55, 60, 70)}, (t, lz)
         pt, lz, ms, kern = b.autotune(60)  # explicit tuning works with the automatic one off
         assert pt in (16, 32) and ms > 0
     finally:
@@ -239,9 +242,10 @@ def test_run_kernel_equals_block_kernel(gpu, t, k, pt):
     """The sampler through the run kernel (codewords in per-thread runs that
     share their top-bit shrinks), through the block-prefix kernel with heavy and
     light launches, with one launch per occupancy class, and through the
-    direct kernel (alone, and split with the block-prefix kernel by each
-    state's number of non-pivot coordinates): identical values for every state
-    (the sums are exact), on the same counter-based draws."""
+    direct kernel (alone, with its launch split by codeword weight above 32
+    qubits, and split with the block-prefix kernel by each state's number of
+    non-pivot coordinates): identical values for every state (the sums are
+    exact), on the same counter-based draws."""
     rs = np.random.RandomState(4000 + t + k)
     L = [rand_word(rs, t) for _ in range(k)]
     rows = random_projector_rows(rs, t, int(0.7 * t))
