@@ -48,8 +48,9 @@ int launch_items_tp(const Launch& L, const PairItem* items, int64_t nitems, cons
 // the direct kernel over the items; canon, code_direct, code_rest as launch_canon
 // wrote them for the items' states.  Writes every item's partial sums except
 // those of states with code_rest >= 0 (launch_items_tp with code_rest, only_live).
+// `rows` (<= nmax) bounds the ones of every item's codewords.
 int launch_items_direct(const Launch& L, const PairItem* items, int64_t nitems, const void* canon,
-                        const int* code_direct, const int* code_rest, int per_thread, int nmax, int dslots,
+                        const int* code_direct, const int* code_rest, int per_thread, int nmax, int rows, int dslots,
                         __int128* part, __int128* part_diag, unsigned long long* queue);
 int launch_items_warp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,
                       __int128* part, __int128* part_diag);

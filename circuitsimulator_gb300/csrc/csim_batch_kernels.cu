@@ -229,8 +229,8 @@ static_assert(kTPB == 64, "one thread per row of the 64-row pivot form");
 
 __global__ void __launch_bounds__(kTPB) k_items_direct(const PairItem* items, int64_t nitems,
                                                        const pc::CanonG* canon, const int* code_direct,
-                                                       const int* code_rest, int per_thread, int nmax, int dslots,
-                                                       __int128* part, __int128* part_diag,
+                                                       const int* code_rest, int per_thread, int nmax, int rows,
+                                                       int dslots, __int128* part, __int128* part_diag,
                                                        unsigned long long* queue, int* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     DirectItemShared& sh = *reinterpret_cast<DirectItemShared*>(smem_raw);
@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(kTPB) k_items_direct(const PairItem* items, in
     unsigned char* const pair_base = smem_raw + sizeof(DirectItemShared) + 2 * 64 * 8;
     const int tid = threadIdx.x;
     int e = 0;
-    const pc::PairMem mem = pc::pair_mem(pair_base, nmax, kTPB, tid);
+    const pc::PairMem mem = pc::pair_mem(pair_base, rows, kTPB, tid);
     if (tid == 0) sh.next = (long long)atomicAdd(queue, 1ull);
     __syncthreads();
     for (int64_t w = sh.next; w < nitems;) {
@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(kTPB) k_items_direct(const PairItem* items, in
                     if (__all_sync(kFull, !valid)) break;  // warp-uniform exit
                     const uint64_t x = valid ? it.cw[j] : 0ull;
                     int eps = 0, pp = 0, mm = 0;
-                    pc::pair_direct(valid, n, sh.cs, sJ, sA, x, mem, eps, pp, mm, e, dslots, sh.cs.k, nmax);
+                    pc::pair_direct(valid, n, sh.cs, sJ, sA, x, mem, eps, pp, mm, e, dslots, sh.cs.k, rows);
                     if (!valid) continue;
                     pc::zacc(z, eps, pp, mm, P, e);
                     if (j == it.diag) {
@@ -417,15 +417,17 @@ size_t items_direct_smem(int nmax, int dslots) {
 }  // namespace
 
 int launch_items_direct(const Launch& L, const PairItem* items, int64_t nitems, const void* canon,
-                        const int* code_direct, const int* code_rest, int per_thread, int nmax, int dslots,
+                        const int* code_direct, const int* code_rest, int per_thread, int nmax, int rows, int dslots,
                         __int128* part, __int128* part_diag, unsigned long long* queue) {
     if (nitems <= 0) return 0;
-    if (nmax < 1 || nmax > 64 || dslots < 0 || dslots > nmax || per_thread < 1 || !queue || !canon) return -1;
+    if (nmax < 1 || nmax > 64 || rows < 1 || rows > nmax || dslots < 0 || dslots > nmax || per_thread < 1 || !queue ||
+        !canon)
+        return -1;
     if (cudaMemsetAsync(queue, 0, sizeof(unsigned long long), L.stream) != cudaSuccess) return -1;
     if (cudaFuncSetAttribute(k_items_direct, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)items_direct_smem(64, 64)) != cudaSuccess)
         return -1;
-    const size_t smem = items_direct_smem(nmax, dslots);
+    const size_t smem = items_direct_smem(rows, dslots);
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_items_direct, kTPB, smem) != cudaSuccess ||
         per_sm < 1)
@@ -433,8 +435,8 @@ int launch_items_direct(const Launch& L, const PairItem* items, int64_t nitems, 
     int64_t grid = (int64_t)L.num_sms * per_sm;
     if (grid > nitems) grid = nitems;
     k_items_direct<<<(int)grid, kTPB, smem, L.stream>>>(items, nitems, (const pc::CanonG*)canon, code_direct,
-                                                        code_rest, per_thread, nmax, dslots, part, part_diag, queue,
-                                                        L.d_err);
+                                                        code_rest, per_thread, nmax, rows, dslots, part, part_diag,
+                                                        queue, L.d_err);
     (*L.launches)++;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -51,10 +51,11 @@ using Clock = std::chrono::steady_clock;
 constexpr size_t kAlign = 256;
 inline size_t align_up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
 
-// thread-per-pair launches: three per occupancy class of t (heavy, light,
-// direct); a light launch takes codewords of at most the light bound's zeros,
-// a direct launch the evaluations the tuner gave the direct kernel (tune_for)
-constexpr int kBuckets = 3 * CSIM_MAX_QUBITS;
+// thread-per-pair launches: four per occupancy class of t (heavy, light,
+// direct narrow, direct wide); a light launch takes codewords of at most the
+// light bound's zeros, the direct launches the evaluations the tuner gave the
+// direct kernel (tune_for), narrow for the codewords of at most 32 ones
+constexpr int kBuckets = 4 * CSIM_MAX_QUBITS;
 
 // device memory that grows on demand (contents are not kept)
 struct DevBuf {
@@ -409,7 +410,8 @@ int Engine::ensure_decomp(QueryRec* r, bool need_phis, bool force, Decomp** out)
             }
             d->pt = tn.per_thread;
             d->kern = tn.kernel;
-            d->lz = tn.kernel == 0 ? tn.light : light_zeros(d->t);  // the items kernel shares top bits per block
+            // the items kernel shares top bits per block; the direct kernel's bound splits narrow from wide
+            d->lz = (tn.kernel == 0 || tn.kernel == 3) ? tn.light : light_zeros(d->t);
             std::vector<uint64_t> ordered;
             ordered_codewords(d->L.data(), d->k, d->t, d->lz, ordered);
             d->light = light_split(ordered, d->t, d->lz);
@@ -510,6 +512,14 @@ static int64_t light_first_item(const Eval* e, int64_t span) {
     return std::min((e->chi + span - 1) / span, (e->q->dec->light + span - 1) / span);
 }
 
+// Items of a direct-kernel evaluation whose codewords all have at most 32 ones
+// (the ordered table's heavy part above 32 qubits, whole items only); the
+// exactProjector's rows walk the table in term order and take none.
+static int64_t direct_narrow_items(const Eval* e, int64_t span) {
+    if (e->kind != 1 || e->t <= 32) return 0;
+    return std::min((e->chi + span - 1) / span, e->q->dec->light / span);
+}
+
 bool Engine::eval_ready(const Eval* e) const {
     if (e->next >= e->ns) return false;
     // rand() draws: H' continues G''s stream, so its states are drawn after all of G''s
@@ -588,11 +598,13 @@ int Engine::launch_round() {
         const int64_t jb = e->kind == 2 ? rs.slots[i].s : 0;
         const int64_t nj = e->chi - jb;
         if (!e->q->exact) {
-            const int b = 3 * bucket_of_[e->t];
+            const int b = 4 * bucket_of_[e->t];
             const int64_t span_tp = span_tp_of(e);
             const int64_t nall = (nj + span_tp - 1) / span_tp;
             if (e->q->dec->kern == 3) {
-                nbucket[b + 2] += nall;
+                const int64_t nn = direct_narrow_items(e, span_tp);
+                nbucket[b + 2] += nn;
+                nbucket[b + 3] += nall - nn;
                 continue;
             }
             const int64_t nlight = e->kind == 1 ? nall - light_first_item(e, span_tp) : 0;
@@ -617,7 +629,7 @@ int Engine::launch_round() {
     const size_t o_range2 = align_up(o_range + (size_t)ns * 16);
     const size_t up_bytes = align_up(o_range2 + (size_t)ns * 16);
     bool any_direct = false;
-    for (int b = 2; b < kBuckets; b += 3) any_direct |= nbucket[b] > 0;
+    for (int b = 0; b < kBuckets; b++) any_direct |= b % 4 >= 2 && nbucket[b] > 0;
     // work block: states | parts | parts diag | pivot forms | direct and rest codes (direct launches)
     const size_t w_states = 0;
     const size_t w_part = align_up((size_t)ns * sizeof(csim_state));
@@ -688,19 +700,25 @@ int Engine::launch_round() {
         const int64_t jb = e->kind == 2 ? s : 0;
         const int64_t diag = e->kind == 2 ? s : -1;
         if (!r->exact && r->dec->kern == 3) {
-            // all of a slot's items in its bucket's direct launch
+            // a slot's items in its bucket's direct launches: narrow ones, then wide ones
             const int64_t span_tp = span_tp_of(e);
-            int64_t& cd = cur[3 * bucket_of_[e->t] + 2];
-            hrange[2 * i] = cd;
-            for (int64_t j = jb; j < e->chi; j += span_tp)
-                hitems[cd++] = csim::PairItem{i, j, std::min(span_tp, e->chi - j), diag,
-                                              e->kind == 1 ? r->dec->cws : r->dec->cw, nullptr};
-            hrange[2 * i + 1] = cd;
-            hrange2[2 * i] = hrange2[2 * i + 1] = 0;
+            const int b = 4 * bucket_of_[e->t];
+            const int64_t jn = jb + direct_narrow_items(e, span_tp) * span_tp;
+            const uint64_t* cw = e->kind == 1 ? r->dec->cws : r->dec->cw;
+            int64_t& cn = cur[b + 2];
+            int64_t& cd = cur[b + 3];
+            hrange[2 * i] = cn;
+            for (int64_t j = jb; j < jn; j += span_tp)
+                hitems[cn++] = csim::PairItem{i, j, std::min(span_tp, e->chi - j), diag, cw, nullptr};
+            hrange[2 * i + 1] = cn;
+            hrange2[2 * i] = cd;
+            for (int64_t j = jn; j < e->chi; j += span_tp)
+                hitems[cd++] = csim::PairItem{i, j, std::min(span_tp, e->chi - j), diag, cw, nullptr};
+            hrange2[2 * i + 1] = cd;
         } else if (!r->exact) {
             // heavy items first, then light ones; a slot's items may sit in two
             // launches, so its range is kept per slot in each (see below)
-            const int b = 3 * bucket_of_[e->t];
+            const int b = 4 * bucket_of_[e->t];
             const int64_t span_tp = span_tp_of(e);
             const int64_t jl = e->kind == 1 ? light_first_item(e, span_tp) * span_tp : e->chi;
             int64_t& ch = cur[b];
@@ -744,19 +762,23 @@ int Engine::launch_round() {
     int* const crest = (int*)(wb + w_crest);
     if (any_direct && csim::launch_canon(L, dstates, dcode, ns, dslots_max, canon, cdir, crest))
         return fail(ctx_, CSIM_ERR_CUDA, "pivot form launch failed");
-    for (int b = 0; b < 3 * nbuckets_; b++) {
-        if (!nbucket[b]) continue;
-        const int nmax = bucket_hi_[b / 3];
+    for (int b = 0; b < 4 * nbuckets_; b++) {
+        const int nmax = bucket_hi_[b / 4];
         const csim::PairItem* it = ditems + bstart[b];
         int rc = 0;
-        if (b % 3 == 2) {
-            rc = csim::launch_items_direct(L, it, nbucket[b], canon, cdir, crest, launch_pt, nmax,
-                                           std::min(nmax, dslots_max), part + 4 * bstart[b], partd + 4 * bstart[b],
-                                           queue) ||
-                 csim::launch_items_tp(L, it, nbucket[b], dstates, crest, launch_pt, nmax, nmax, part + 4 * bstart[b],
-                                       partd + 4 * bstart[b], queue, true);
-        } else {
-            const int gmax = b % 3 == 1 ? std::min(nmax, lzmax[b]) : nmax;
+        if (b % 4 >= 2) {
+            // narrow items take 32 J rows per pair; after the wide launch, the states left to the
+            // block-prefix kernel over both (adjacent in the table)
+            if (nbucket[b])
+                rc = csim::launch_items_direct(L, it, nbucket[b], canon, cdir, crest, launch_pt, nmax,
+                                               b % 4 == 2 ? std::min(nmax, 32) : nmax, std::min(nmax, dslots_max),
+                                               part + 4 * bstart[b], partd + 4 * bstart[b], queue);
+            const int64_t nd = nbucket[b - 1] + nbucket[b];
+            if (!rc && b % 4 == 3 && nd)
+                rc = csim::launch_items_tp(L, ditems + bstart[b - 1], nd, dstates, crest, launch_pt, nmax, nmax,
+                                           part + 4 * bstart[b - 1], partd + 4 * bstart[b - 1], queue, true);
+        } else if (nbucket[b]) {
+            const int gmax = b % 4 == 1 ? std::min(nmax, lzmax[b]) : nmax;
             rc = csim::launch_items_tp(L, it, nbucket[b], dstates, dcode, launch_pt, nmax, gmax, part + 4 * bstart[b],
                                        partd + 4 * bstart[b], queue);
         }
