@@ -1193,56 +1193,53 @@ CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64
     const W vb = dimer ? (ra & Ep) : (W)0, va = dimer ? (rb & Ep) : (W)0;
     const bool upd = (vb | va) != (W)0;
     const int jaa = wget<W>(ra, a), jbb = wget<W>(rb, b), jab = wget<W>(ra, b);
-    const W Cb = rb ^ (jbb ? vb : (W)0) ^ (jab ? va : (W)0);
-    const W Ca = ra ^ (jab ? vb : (W)0) ^ (jaa ? va : (W)0);
+    // Rows a and b are not read again, so only rows x of Ep change, and only in the columns still
+    // read (Ep and sidx).  Since J_ab = 1 for a dimer, R J R^T there is the symmetric rank-two
+    // update x ^= (vb_x ? Pm : 0) ^ (va_x ? Qm : 0) (vb_x = J_ax, va_x = J_bx), column sidx
+    // included through bit sidx of rows a and b.
+    const W es = sidx >= 0 ? wbit<W>(sidx) : (W)0;
+    const W Pm = va ^ (jbb ? vb : (W)0) ^ (rb & es);
+    const W Qm = vb ^ (jaa ? va : (W)0) ^ (ra & es);
     {
-        const W zm = upd ? (Ep | keep) : (W)0;
+        const W zm = upd ? Ep : (W)0;
         const int lo = zm ? T::ffs(zm) - 1 : T::bits, hi = zm ? T::bits - T::clz(zm) : 0;
         const int X0 = uniform_min(lo) & ~3, X1 = uniform_max(hi);
         if (live) CSIM_COUNT_ROWS((dimer ? 2 : 1) + (upd ? hi - lo : 0));
-        const W rvb = wbrev(vb), rva = wbrev(va), rcb = wbrev(Cb), rca = wbrev(Ca);
+        const W rvb = wbrev(vb), rva = wbrev(va);
         {
             const int sh = T::bits - 32;
             const int s0 = X0 < 32 ? X0 : 0;
-            const uint32_t rb32 = (uint32_t)rb, ra32 = (uint32_t)ra, vb32 = (uint32_t)vb, va32 = (uint32_t)va;
-            uint32_t cvb = (uint32_t)(rvb >> sh) << s0, cva = (uint32_t)(rva >> sh) << s0,
-                     ccb = (uint32_t)(rcb >> sh) << s0, cca = (uint32_t)(rca >> sh) << s0;
+            const uint32_t P32 = (uint32_t)Pm, Q32 = (uint32_t)Qm;
+            uint32_t cvb = (uint32_t)(rvb >> sh) << s0, cva = (uint32_t)(rva >> sh) << s0;
             const int X1a = X1 < 32 ? X1 : 32;
             for (int x = X0; x < X1a; x += 4) {
                 U32x4* pr = reinterpret_cast<U32x4*>(&R32(x));
                 U32x4 v = *pr;
-                v.a ^= (rb32 & topmask(cvb)) ^ (ra32 & topmask(cva)) ^ (vb32 & topmask(ccb)) ^
-                       (va32 & topmask(cca));
-                v.b ^= (rb32 & topmask(cvb << 1)) ^ (ra32 & topmask(cva << 1)) ^ (vb32 & topmask(ccb << 1)) ^
-                       (va32 & topmask(cca << 1));
-                v.c ^= (rb32 & topmask(cvb << 2)) ^ (ra32 & topmask(cva << 2)) ^ (vb32 & topmask(ccb << 2)) ^
-                       (va32 & topmask(cca << 2));
-                v.d ^= (rb32 & topmask(cvb << 3)) ^ (ra32 & topmask(cva << 3)) ^ (vb32 & topmask(ccb << 3)) ^
-                       (va32 & topmask(cca << 3));
+                v.a ^= (P32 & topmask(cvb)) ^ (Q32 & topmask(cva));
+                v.b ^= (P32 & topmask(cvb << 1)) ^ (Q32 & topmask(cva << 1));
+                v.c ^= (P32 & topmask(cvb << 2)) ^ (Q32 & topmask(cva << 2));
+                v.d ^= (P32 & topmask(cvb << 3)) ^ (Q32 & topmask(cva << 3));
                 cvb <<= 4;
                 cva <<= 4;
-                ccb <<= 4;
-                cca <<= 4;
                 *pr = v;
             }
         }
         if (sizeof(W) == 8) {
             const int x0 = X0 > 32 ? (X0 & ~1) : 32;
             const int s1 = x0 & (T::bits - 1);
-            W cvb = rvb << s1, cva = rva << s1, ccb = rcb << s1, cca = rca << s1;
+            W cvb = rvb << s1, cva = rva << s1;
             for (int x = x0; x < X1; x += 2) {
                 U64x2* pr = reinterpret_cast<U64x2*>(&R64(x));
                 U64x2 v = *pr;
-                v.a ^= (uint64_t)((rb & topmask(cvb)) ^ (ra & topmask(cva)) ^ (vb & topmask(ccb)) ^
-                                  (va & topmask(cca)));
-                v.b ^= (uint64_t)((rb & topmask((W)(cvb << 1))) ^ (ra & topmask((W)(cva << 1))) ^
-                                  (vb & topmask((W)(ccb << 1))) ^ (va & topmask((W)(cca << 1))));
+                v.a ^= (uint64_t)((Pm & topmask(cvb)) ^ (Qm & topmask(cva)));
+                v.b ^= (uint64_t)((Pm & topmask((W)(cvb << 1))) ^ (Qm & topmask((W)(cva << 1))));
                 cvb <<= 2;
                 cva <<= 2;
-                ccb <<= 2;
-                cca <<= 2;
                 *pr = v;
             }
+            // a row sidx >= 32 holds column sidx of the rows below 32
+            if (keep && upd)
+                R64(sidx) ^= (uint64_t)((wget<W>(rb, sidx) ? vb : (W)0) ^ (wget<W>(ra, sidx) ? va : (W)0));
         }
     }
     if (upd) {
@@ -1303,13 +1300,15 @@ CSIM_HD inline void md_exp_sum(PairRegs& s, const PairMem& M, uint64_t F, bool a
         md_exp_step<W>(M, E64, (uint64_t)keep, sidx, D1, D2, w0, w1, err);
     }
     if (sizeof(W) == 8 && it < NE) {
-        uint32_t d1 = (uint32_t)D1, d2 = (uint32_t)D2;  // the rest of E and sidx lie below 32
+        // the rest of E and sidx lie below 32 (or E is empty): steps in 32-bit words, which leave
+        // the D bits from 32 up as they are
+        uint32_t d1 = (uint32_t)D1, d2 = (uint32_t)D2;
         for (; it < NE; it++) {
             if (uniform_max(E64 ? 1 : 0) == 0) break;
             md_exp_step<uint32_t>(M, E64, 0ull, sidx, d1, d2, w0, w1, err);
         }
-        D1 = (W)d1;
-        D2 = (W)d2;
+        D1 = (D1 & ~(W)0xffffffffu) | (W)d1;
+        D2 = (D2 & ~(W)0xffffffffu) | (W)d2;
     }
     if (!act) return;
     if (Fw == (W)0) {  // Wsigma's k == 0 case

@@ -205,3 +205,48 @@ def test_direct_vs_oracle(tp, oracle, t, k, nshrink):
     eo, po, mo = oracle.term_products(t, 0, L, k, thetas, 0, 2 ** k, threads=os.cpu_count() or 1)
     ok = (e == eo) & ((e == 0) | ((p == po) & ((m % 8) == (mo % 8))))
     assert ok.all(), (t, k, nshrink, int((~ok).sum()))
+
+
+def test_direct_odd_variable_above_32(tp, oracle):
+    """Pairs whose exponential sum keeps its one odd-D variable (sidx) at a live
+    index >= 32, with more than 32 live variables: in 64-bit mode the row of
+    sidx stores column sidx of the rows below 32 and is updated apart from the
+    row passes.  Every coordinate is a pivot (G = I), odd D only on coordinates
+    56..63, J random symmetric with diagonal D1, codewords of about 45 ones."""
+    rs = np.random.RandomState(77)
+    t = 64
+    thetas = []
+    for _ in range(3):
+        th = oracle.state(t, t)[0]
+        hi = np.uint64(0xFF00000000000000)
+        d1 = np.uint64(rand_word(rs, t)) & hi
+        th["D1"] = d1
+        th["D2"] = np.uint64(rand_word(rs, t))
+        th["Q"] = int(rs.randint(8)) & 6
+        J = np.zeros(t, dtype=np.uint64)
+        for a in range(t):
+            for b in range(a + 1, t):
+                if rs.randint(2):
+                    J[a] |= np.uint64(1 << b)
+                    J[b] |= np.uint64(1 << a)
+            if (int(d1) >> a) & 1:
+                J[a] |= np.uint64(1 << a)
+        th["J"] = J
+        thetas.append(th)
+    thetas = np.array(thetas)
+    # codewords: random words of about 0.7 t ones, closed under XOR of a small code
+    L = np.array([int("".join("1" if rs.rand() < 0.7 else "0" for _ in range(t)), 2) for _ in range(6)],
+                 dtype=np.uint64)
+    xs = [oracle.codeword(int(j), L) for j in range(2 ** len(L))]
+    xs = [x for x in xs if bin(x).count("1") > 36]
+    assert len(xs) >= 8
+    err, e, p, m = tp(thetas, xs, run_len=-1)
+    assert err == 0
+    eo, po, mo = oracle.term_products(t, 0, L, len(L), thetas, 0, 2 ** len(L), threads=os.cpu_count() or 1)
+    idx = [j for j in range(2 ** len(L)) if bin(oracle.codeword(j, L)).count("1") > 36]
+    eo = eo.reshape(len(thetas), -1)[:, idx].reshape(-1)
+    po = po.reshape(len(thetas), -1)[:, idx].reshape(-1)
+    mo = mo.reshape(len(thetas), -1)[:, idx].reshape(-1)
+    ok = (e == eo) & ((e == 0) | ((p == po) & ((m % 8) == (mo % 8))))
+    assert ok.all(), int((~ok).sum())
+    assert (e != 0).any()
