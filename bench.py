@@ -129,10 +129,10 @@ DIRECT_ROWS_PER_PAIR_T40 = 151.1
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one pair-kernel launch over
 # 64 projected c2 states: the light block-prefix launch
 # (profiles/k_terms_tp_c2_small.md: 657 KB read, 600 KB written) and the direct
-# launch (profiles/k_terms_direct_c2_small.md: 658 KB read, 933 KB written).  Reads
+# launch (profiles/k_terms_direct_c2_small.md: 673 KB read, 1071 KB written).  Reads
 # are the 512 KB codeword table and the states; writes are the partial sums and
 # the write-back of lines the L2 flush left dirty.
-MEASURED_TRAFFIC_64_STATES = {"block prefix": 657e3 + 600e3, "direct": 658e3 + 933e3}
+MEASURED_TRAFFIC_64_STATES = {"block prefix": 657e3 + 600e3, "direct": 673e3 + 1071e3}
 MEASURED_TRAFFIC_CODEWORDS = 8 * 2 ** 16
 
 

@@ -452,6 +452,22 @@ CSIM_HD inline void tp_factor_dimer(WAcc& w, int A, int B, int& err) {
     w.m += z ? 0 : (code & 7);
 }
 
+// One monomer factor partialGamma(A) (dimer = false) or dimer factor Gamma(A, B)
+// folded into w, A and B even and non-negative, without a branch on which:
+// both codes come from 4-bit tables (bit 3 zero, bits 0..2 the power of w);
+// the power of sqrt2 is 2 unless a monomer's power of w is odd.
+constexpr uint32_t kMonoCodes = 0x7810u;  // A/2 mod 4 = 0, 1, 2, 3: w^0 (p 2), w^1 (p 1), zero, w^7 (p 1)
+CSIM_HD inline void fold_factor(WAcc& w, bool dimer, int A, int B, int& err) {
+    if ((A | B) & 1) err |= kErrGamma;
+    const int ia = (A >> 1) & 3, idx = 4 * ia + ((B >> 1) & 3);
+    const uint32_t half = (idx & 8) ? (uint32_t)(kGammaCodes >> 32) : (uint32_t)kGammaCodes;
+    const int code = dimer ? (int)((half >> (4 * (idx & 7))) & 15u) : (int)((kMonoCodes >> (4 * ia)) & 15u);
+    const int z = code >> 3, m = code & 7;
+    w.zero |= z;
+    w.p += z ? 0 : ((dimer || m == 0) ? 2 : 1);
+    w.m += z ? 0 : m;
+}
+
 // exponentialSumExact (stabilizer.c:300-481), symmetric J; `act` as for tp_shrink.
 template <class W>
 CSIM_HD inline void tp_exp_sum(PairRegs& s, const PairMem& M, bool act, int& eps, int& p, int& m, int& err) {
@@ -1179,20 +1195,17 @@ CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64
     const bool dimer = K != (W)0;
     const int b = dimer ? T::bits - 1 - T::clz(K) : 0;
     const W rb = dimer ? md_read_row<W>(M, b, KP) : (W)0;
+    // the monomer {a} or dimer {a, b} factor of W0, and of W1 (D + 4 J at sidx)
     const int Da = 2 * (2 * wget<W>(D2, a) + wget<W>(D1, a));
-    if (live && !dimer) {  // monomer {a}
-        tp_factor_mono(w0, Da, err);
-        if (sidx >= 0) tp_factor_mono(w1, Da + 4 * wget<W>(ra, sidx), err);
-    }
-    if (dimer) {  // dimer {a, b}
-        const int Db = 2 * (2 * wget<W>(D2, b) + wget<W>(D1, b));
-        tp_factor_dimer(w0, Da, Db, err);
-        if (sidx >= 0) tp_factor_dimer(w1, Da + 4 * wget<W>(ra, sidx), Db + 4 * wget<W>(rb, sidx), err);
+    const int Db = dimer ? 2 * (2 * wget<W>(D2, b) + wget<W>(D1, b)) : 0;
+    if (live) {
+        fold_factor(w0, dimer, Da, Db, err);
+        if (sidx >= 0) fold_factor(w1, dimer, Da + 4 * wget<W>(ra, sidx), Db + 4 * wget<W>(rb, sidx), err);
     }
     const W Ep = dimer ? (E & ~wbit<W>(a) & ~wbit<W>(b)) : (E & ~wbit<W>(a));
     const W vb = dimer ? (ra & Ep) : (W)0, va = dimer ? (rb & Ep) : (W)0;
     const bool upd = (vb | va) != (W)0;
-    const int jaa = wget<W>(ra, a), jbb = wget<W>(rb, b), jab = wget<W>(ra, b);
+    const int jaa = wget<W>(ra, a), jbb = wget<W>(rb, b);
     // Rows a and b are not read again, so only rows x of Ep change, and only in the columns still
     // read (Ep and sidx).  Since J_ab = 1 for a dimer, R J R^T there is the symmetric rank-two
     // update x ^= (vb_x ? Pm : 0) ^ (va_x ? Qm : 0) (vb_x = J_ax, va_x = J_bx), column sidx
@@ -1246,9 +1259,7 @@ CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64
         const int db1 = wget<W>(D1, b), db2 = wget<W>(D2, b), da1 = wget<W>(D1, a), da2 = wget<W>(D2, a);
         add_Dw<W>(D1, D2, vb, db1, db2);
         add_Dw<W>(D1, D2, va, da1, da2);
-        W flip = (vb & rb) ^ (va & ra);
-        if (jab) flip ^= vb & va;
-        D2 ^= flip;
+        D2 ^= (vb & rb) ^ (va & ra) ^ (vb & va);  // J_ab = 1 for a dimer, the only step that updates
     }
     if (live) E = Ep;
     E64 = (uint64_t)E;
