@@ -560,7 +560,7 @@ def serve_compare(rate, count, seed=5, c5=False):
 C4_WORKLOAD = os.path.join(ROOT, "tests", "golden", "workload_c4.json")
 
 
-def chain_compare(shots, nbits, samples=None):
+def chain_compare(shots, nbits, samples=None, groups=2):
     """sampleQubits chains on the c4 circuit (tests/golden/workload_c4.json:
     n=32, t=64, k=14 code, L=2048 states per conditional): `shots` chains of
     `nbits` sampled qubits, plain (one shot after another, one query at a
@@ -581,14 +581,20 @@ def chain_compare(shots, nbits, samples=None):
              for s in seeds]
     t1 = time.perf_counter()
     st = {}
-    batched = sample.sample_qubits_batch(w["circ"], {}, list(bits), dict(cfg), seeds, backend=gpu, stats=st)
+    batched = sample.sample_qubits_batch(w["circ"], {}, list(bits), dict(cfg), seeds, backend=gpu, stats=st,
+                                         groups=groups)
     t2 = time.perf_counter()
     queries = sum(st["queries_per_step"])
     return {"workload": "c4 chain: %d shots x %d sampled qubits, n=32, t=64, k=%d, L=%d per conditional"
                         % (shots, nbits, cfg["k"], cfg["samples"]),
             "metric": "queries/s", "queries": queries, "plain": queries / (t1 - t0), "batched": queries / (t2 - t1),
             "speedup": (t1 - t0) / (t2 - t1), "identical_outputs": plain == batched, "steps": st["steps"],
-            "plain_s": t1 - t0, "batched_s": t2 - t1}
+            "plain_s": t1 - t0, "batched_s": t2 - t1,
+            "batched_split": {"gpu_calls_s": st["gpu_s"], "device_s": st["device_s"],
+                              "pair_kernel_s": st["pair_kernel_s"], "front_ends_s": st["host_s"],
+                              "groups": groups,
+                              "note": "shot groups: one group's front ends run while another's queries are on "
+                                      "the GPU"}}
 
 
 def c3_rates(ts=(28, 41, 47, 57), count=2000):
@@ -767,6 +773,8 @@ def main():
     ap.add_argument("--chain", default=None, metavar="SHOTSxBITS",
                     help="only time sampleQubits chains on the c4 circuit, plain vs batched (e.g. 16x4)")
     ap.add_argument("--chain-samples", type=int, default=None, help="L per conditional for --chain")
+    ap.add_argument("--chain-groups", type=int, default=2,
+                    help="shot groups of the batched --chain arm (1: one csim_run_queries call per step)")
     ap.add_argument("--serve", default=None, metavar="RATES",
                     help="only time serving under Poisson arrivals at these rates (queries/s, comma separated)")
     ap.add_argument("--serve-count", type=int, default=300, help="queries per rate for --serve")
@@ -795,7 +803,7 @@ def main():
         return
     if args.chain:
         shots, nbits = (int(v) for v in args.chain.lower().split("x"))
-        print(json.dumps(chain_compare(shots, nbits, args.chain_samples)))
+        print(json.dumps(chain_compare(shots, nbits, args.chain_samples, args.chain_groups)))
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

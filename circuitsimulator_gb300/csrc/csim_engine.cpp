@@ -564,9 +564,58 @@ int Engine::launch_round() {
     const int64_t ns = (int64_t)rs.slots.size();
     if (ns == 0) return 0;
 
-    // rand() words of the sampled states, drawn in each query's own order
-    std::vector<uint32_t> words;
+    // rand() words of the sampled states with the C library's draws, each query's states in its own
+    // stream order (G' then H'); queries are independent streams, so they are drawn on host threads
+    // of their own (at t = 64 a state takes about 2000 words)
     std::vector<std::pair<int64_t, int64_t>> wr(ns, {0, 0});
+    struct WordJob {
+        QueryRec* q;
+        int t;
+        std::vector<int64_t> slots;
+        std::vector<uint32_t> words;
+        std::vector<int64_t> ends;
+    };
+    std::vector<WordJob> jobs;
+    {
+        std::map<QueryRec*, size_t> jix;
+        for (int64_t i = 0; i < ns; i++) {
+            Eval* e = rs.slots[i].e;
+            if (e->kind != 1 || e->q->q.rng != CSIM_RNG_LIBC) continue;
+            auto it = jix.find(e->q);
+            if (it == jix.end()) {
+                it = jix.emplace(e->q, jobs.size()).first;
+                jobs.push_back(WordJob{e->q, e->t, {}, {}, {}});
+            }
+            jobs[it->second].slots.push_back(i);
+        }
+        auto run_job = [](WordJob& j) {
+            double cum[CSIM_MAX_QUBITS + 1];
+            cum_table(j.t, cum);
+            j.ends.reserve(j.slots.size());
+            for (size_t k = 0; k < j.slots.size(); k++) {
+                draw_state_words(j.q->lr, j.t, cum, j.words);
+                j.ends.push_back((int64_t)j.words.size());
+            }
+        };
+        const int nthreads = (int)std::min<size_t>(jobs.size(), std::max(1u, std::thread::hardware_concurrency()));
+        if (nthreads <= 1) {
+            for (auto& j : jobs) run_job(j);
+        } else {
+            std::atomic<size_t> next{0};
+            std::vector<std::thread> pool;
+            for (int w = 0; w < nthreads; w++)
+                pool.emplace_back([&] {
+                    for (size_t j; (j = next.fetch_add(1)) < jobs.size();) run_job(jobs[j]);
+                });
+            for (auto& th : pool) th.join();
+        }
+    }
+    int64_t nwords = 0;
+    for (auto& j : jobs) {
+        for (size_t k = 0; k < j.slots.size(); k++)
+            wr[j.slots[k]] = {nwords + (k ? j.ends[k - 1] : 0), nwords + j.ends[k]};
+        nwords += (int64_t)j.words.size();
+    }
     std::map<Eval*, int> evix;  // evaluations in this round -> projector block
     // thread-per-pair items are grouped by t bucket: each bucket's launch sizes
     // its shared memory for that bucket's largest t, not the round's
@@ -578,22 +627,11 @@ int Engine::launch_round() {
     const int launch_pt = per_thread_ > 0 ? per_thread_ : 32;  // the largest item any t is tuned to
     int lzmax[kBuckets] = {0};  // per light launch: the largest light bound of its items
     const int64_t span_w = 64;
-    double hcum[CSIM_MAX_QUBITS + 1];
-    int hcum_t = -1;
     for (int64_t i = 0; i < ns; i++) {
         Eval* e = rs.slots[i].e;
         if (!evix.count(e)) {
             const int ix = (int)evix.size();
             evix[e] = ix;
-        }
-        if (e->kind == 1 && e->q->q.rng == CSIM_RNG_LIBC) {
-            if (hcum_t != e->t) {
-                cum_table(e->t, hcum);
-                hcum_t = e->t;
-            }
-            wr[i].first = (int64_t)words.size();
-            draw_state_words(e->q->lr, e->t, hcum, words);
-            wr[i].second = (int64_t)words.size();
         }
         const int64_t jb = e->kind == 2 ? rs.slots[i].s : 0;
         const int64_t nj = e->chi - jb;
@@ -624,7 +662,7 @@ int Engine::launch_round() {
     const size_t o_desc = 0;
     const size_t o_proj = align_up(o_desc + (size_t)ns * sizeof(csim::DrawDesc));
     const size_t o_words = align_up(o_proj + evix.size() * 192 * 8);
-    const size_t o_items = align_up(o_words + words.size() * 4);
+    const size_t o_items = align_up(o_words + (size_t)nwords * 4);
     const size_t o_range = align_up(o_items + (size_t)nitems * sizeof(csim::PairItem));
     const size_t o_range2 = align_up(o_range + (size_t)ns * 16);
     const size_t up_bytes = align_up(o_range2 + (size_t)ns * 16);
@@ -659,7 +697,13 @@ int Engine::launch_round() {
         memcpy(blk + 64, kv.first->pz, 8 * kv.first->nstabs);
         memcpy(blk + 128, kv.first->px, 8 * kv.first->nstabs);
     }
-    if (!words.empty()) memcpy(hb + o_words, words.data(), words.size() * 4);
+    {
+        size_t o = 0;
+        for (auto& j : jobs) {
+            if (!j.words.empty()) memcpy(hb + o_words + 4 * o, j.words.data(), j.words.size() * 4);
+            o += j.words.size();
+        }
+    }
     const uint64_t* dproj = (const uint64_t*)(db + o_proj);
     const uint32_t* dwords = (const uint32_t*)(db + o_words);
     csim::DrawDesc* hdesc = (csim::DrawDesc*)(hb + o_desc);

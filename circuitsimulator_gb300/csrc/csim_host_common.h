@@ -34,9 +34,10 @@ struct LibcRand {
     LibcRand() { seed(1); }  // rand() before any srand() is seeded with 1
 
     uint32_t step() {
-        const uint32_t v = ring[(idx + 31) % 34] + ring[(idx + 3) % 34];
+        const int i31 = idx + 31 >= 34 ? idx - 3 : idx + 31, i3 = idx + 3 >= 34 ? idx - 31 : idx + 3;
+        const uint32_t v = ring[i31] + ring[i3];
         ring[idx] = v;
-        idx = (idx + 1) % 34;
+        idx = idx == 33 ? 0 : idx + 1;
         return v;
     }
     void seed(uint32_t s) {
@@ -139,7 +140,9 @@ inline void draw_state_words(LibcRand& lr, int n, const double* cum, std::vector
         k--;
     }
     const int64_t rest = 3 * bytes + (int64_t)k * (k - 1) / 2;
-    for (int64_t i = 0; i < rest; i++) words.push_back((uint32_t)lr.next());
+    const size_t w0 = words.size();
+    words.resize(w0 + (size_t)rest);
+    for (int64_t i = 0; i < rest; i++) words[w0 + (size_t)i] = (uint32_t)lr.next();
 }
 
 // Zero bound of the "light" part of an ordered codeword table: codewords with

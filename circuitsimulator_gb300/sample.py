@@ -218,16 +218,24 @@ def sampleQubits(circ, measure, sample, config=None, rng=None, backend=None):
                   backend or default_backend())
 
 
-def sample_qubits_batch(circ, measure, sample, config, seeds, backend=None, stats=None):
+def sample_qubits_batch(circ, measure, sample, config, seeds, backend=None, stats=None, groups=2):
     """Many independent sampleQubits shots in lockstep.  Shot s has its own
     numpy RandomState(seeds[s]) for the front end and the bit draws, and its
-    own copies of `measure` and `config`.  At every step the pending queries
-    of all shots go to the GPU in one csim_run_queries call.  Shot s returns
-    the same bits as sampleQubits run alone with that random state.  Returns
-    the list of output strings; `stats`, when a dict, gets the step count and
-    queries per step."""
+    own copies of `measure` and `config`.  The shots are split into `groups`
+    interleaved groups; each group's pending queries go to the GPU in one
+    csim_run_queries call, made on a worker thread, while this thread runs
+    the other groups' front ends (the call releases the GIL).  Shot s returns
+    the same bits as sampleQubits run alone with that random state, whatever
+    the grouping.  Returns the list of output strings; `stats`, when a dict,
+    gets the number of calls, the queries per call, and the seconds spent in
+    the calls (`gpu_s`; of it `device_s` on the GPU, `pair_kernel_s` in the
+    pair kernels) and in the front ends between them (`host_s`)."""
+    import time
+    from concurrent.futures import ThreadPoolExecutor
+
     be = backend or default_backend()
     gens, pending, out = [], [], [None] * len(seeds)
+    t0 = time.perf_counter()
     for s, seed in enumerate(seeds):
         g = sample_steps(circ, dict(measure), sample, dict(config), np.random.RandomState(seed))
         gens.append(g)
@@ -236,19 +244,48 @@ def sample_qubits_batch(circ, measure, sample, config, seeds, backend=None, stat
         except StopIteration as e:
             out[s] = e.value
             pending.append(None)
-    steps, per_step = 0, []
-    while any(q is not None for q in pending):
-        live = [s for s, q in enumerate(pending) if q is not None]
-        res = be.run_queries([pending[s] for s in live], batched=True)
-        steps += 1
-        per_step.append(len(live))
-        for s, r in zip(live, res):
-            try:
-                pending[s] = gens[s].send((r["numerator"], r["denominator"]))
-            except StopIteration as e:
-                out[s] = e.value
-                pending[s] = None
+    host_s = time.perf_counter() - t0
+    groups = max(1, min(groups, len(seeds)))
+    members = [list(range(g, len(seeds), groups)) for g in range(groups)]
+    steps, per_step, gpu_s = 0, [], [0.0, 0.0, 0.0]
+
+    def answer(qs):
+        t = time.perf_counter()
+        r = be.run_queries(qs, batched=True)
+        gpu_s[0] += time.perf_counter() - t
+        st = be.last_stats()  # this call's device time and pair-kernel time
+        gpu_s[1] += st.device_ms / 1e3
+        gpu_s[2] += st.pair_kernel_ms / 1e3
+        return r
+
+    with ThreadPoolExecutor(max_workers=1) as worker:
+        def submit(g):
+            live = [s for s in members[g] if pending[s] is not None]
+            return (live, worker.submit(answer, [pending[s] for s in live])) if live else None
+
+        inflight = [submit(g) for g in range(groups)]  # the worker runs them in this order
+        while any(f is not None for f in inflight):
+            for g in range(groups):
+                if inflight[g] is None:
+                    continue
+                live, fut = inflight[g]
+                res = fut.result()
+                steps += 1
+                per_step.append(len(live))
+                t = time.perf_counter()
+                for s, r in zip(live, res):
+                    try:
+                        pending[s] = gens[s].send((r["numerator"], r["denominator"]))
+                    except StopIteration as e:
+                        out[s] = e.value
+                        pending[s] = None
+                host_s += time.perf_counter() - t
+                inflight[g] = submit(g)
     if isinstance(stats, dict):
         stats["steps"] = steps
         stats["queries_per_step"] = per_step
+        stats["gpu_s"] = gpu_s[0]
+        stats["device_s"] = gpu_s[1]
+        stats["pair_kernel_s"] = gpu_s[2]
+        stats["host_s"] = host_s
     return out

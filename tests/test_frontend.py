@@ -128,8 +128,10 @@ def test_sample_batch_equals_shots_alone(cases):
     c = next(c for c in cases["sample"] if c["name"] == "controlledT.circ")  # two queries per shot
     cfg = dict(c["config"], quiet=True, seed=c["backend_seed"])
     seeds = [11, 12, 13, 14, 15, 16]
-    stats = {}
-    batch = sample.sample_qubits_batch(c["circ"], {}, [0, 1, 2], cfg, seeds, stats=stats)
     alone = [sample.sampleQubits(c["circ"], {}, [0, 1, 2], dict(cfg), rng=np.random.RandomState(s)) for s in seeds]
-    assert batch == alone
-    assert stats["steps"] >= 1 and max(stats["queries_per_step"]) >= 2
+    for groups in (1, 2, 3):  # one call per step, or groups pipelined with the front ends
+        stats = {}
+        batch = sample.sample_qubits_batch(c["circ"], {}, [0, 1, 2], cfg, seeds, stats=stats, groups=groups)
+        assert batch == alone, groups
+        assert stats["steps"] >= 1 and max(stats["queries_per_step"]) >= 2
+        assert stats["gpu_s"] > 0 and stats["host_s"] > 0
