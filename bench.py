@@ -446,7 +446,7 @@ def c5_stream(count, seed=505, max_pairs=1 << 30):
     else a code of k = min(18, the fidelity-0.02 rule of probability.c:330)
     rows; L from eps and failure probability 0.05 by probability.py:150-167.
     Draws whose inner products exceed max_pairs are skipped (a c5 query at
-    eps = 0.02 and t = 60 takes 2.6e10 pairs, about a minute of GPU time), so
+    eps = 0.02 and t = 60 takes 2.6e10 pairs, about 10 s of GPU time), so
     the kept stream still spans t = 8..64 and every eps.  Returns (queries,
     draws, [(t, eps, pairs)])."""
     import math
