@@ -41,10 +41,11 @@ int launch_draw_project(const Launch& L, const DrawDesc* desc, int64_t count, GS
 // and codewords of up to gmax zeros
 int items_tp_occupancy(int nmax, int gmax);
 // queue: one device counter, zeroed by the launch (stream-ordered) and drawn from by the blocks.
-// only_live: write the partial sums of live states' items only (the other items are another launch's)
+// only_live: write the partial sums of live states' items only (the other items are another launch's).
+// gate (optional, device): when *gate is 0 no item has a live state and the blocks return at once.
 int launch_items_tp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,
                     int per_thread, int nmax, int gmax, __int128* part, __int128* part_diag,
-                    unsigned long long* queue, bool only_live = false);
+                    unsigned long long* queue, bool only_live = false, const int* gate = nullptr);
 // the direct kernel over the items; canon, code_direct, code_rest as launch_canon
 // wrote them for the items' states.  Writes every item's partial sums except
 // those of states with code_rest >= 0 (launch_items_tp with code_rest, only_live).

@@ -110,7 +110,9 @@ __device__ __forceinline__ __int128 shfl_xor_128(__int128 v, int m) {
 __global__ void __launch_bounds__(kTPB) k_items_tp(const PairItem* items, int64_t nitems, const GState* states,
                                                    const int* codes, int per_thread, int nmax, int gmax,
                                                    __int128* part, __int128* part_diag,
-                                                   unsigned long long* queue, int only_live, int* err) {
+                                                   unsigned long long* queue, int only_live, const int* gate,
+                                                   int* err) {
+    if (gate && *gate == 0) return;  // no live state (block-uniform)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ItemShared& sh = *reinterpret_cast<ItemShared*>(smem_raw);
     uint64_t* const sa = reinterpret_cast<uint64_t*>(smem_raw + sizeof(ItemShared));
@@ -391,7 +393,7 @@ int items_tp_occupancy(int nmax, int gmax) {
 
 int launch_items_tp(const Launch& L, const PairItem* items, int64_t nitems, const GState* states, const int* codes,
                     int per_thread, int nmax, int gmax, __int128* part, __int128* part_diag,
-                    unsigned long long* queue, bool only_live) {
+                    unsigned long long* queue, bool only_live, const int* gate) {
     if (nitems <= 0) return 0;
     if (nmax < 1 || nmax > 64 || gmax < 0 || gmax > nmax || !queue) return -1;
     if (cudaMemsetAsync(queue, 0, sizeof(unsigned long long), L.stream) != cudaSuccess) return -1;
@@ -405,7 +407,7 @@ int launch_items_tp(const Launch& L, const PairItem* items, int64_t nitems, cons
     int64_t grid = (int64_t)L.num_sms * per_sm;
     if (grid > nitems) grid = nitems;
     k_items_tp<<<(int)grid, kTPB, smem, L.stream>>>(items, nitems, states, codes, per_thread, nmax, gmax, part,
-                                                    part_diag, queue, only_live ? 1 : 0, L.d_err);
+                                                    part_diag, queue, only_live ? 1 : 0, gate, L.d_err);
     (*L.launches)++;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

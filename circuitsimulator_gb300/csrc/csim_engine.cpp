@@ -40,8 +40,10 @@
 using namespace csim_host;
 
 namespace {
-// byte offset of the thread-per-pair launches' work-queue counter in a round's download block
+// byte offsets in a round's download block: the thread-per-pair launches' work-queue counter,
+// and the count of live states the direct launches leave to the block-prefix kernel
 constexpr size_t kQueueOffset = 64;
+constexpr size_t kRestCountOffset = 128;
 }  // namespace
 
 namespace {
@@ -804,8 +806,12 @@ int Engine::launch_round() {
     void* const canon = wb + w_canon;
     int* const cdir = (int*)(wb + w_cdir);
     int* const crest = (int*)(wb + w_crest);
-    if (any_direct && csim::launch_canon(L, dstates, dcode, ns, dslots_max, canon, cdir, crest))
-        return fail(ctx_, CSIM_ERR_CUDA, "pivot form launch failed");
+    int* const rest_count = (int*)(dd + kRestCountOffset);
+    if (any_direct) {
+        CK(cudaMemsetAsync(rest_count, 0, 4, ctx_->stream));
+        if (csim::launch_canon(L, dstates, dcode, ns, dslots_max, canon, cdir, crest, rest_count))
+            return fail(ctx_, CSIM_ERR_CUDA, "pivot form launch failed");
+    }
     for (int b = 0; b < 4 * nbuckets_; b++) {
         const int nmax = bucket_hi_[b / 4];
         const csim::PairItem* it = ditems + bstart[b];
@@ -820,7 +826,8 @@ int Engine::launch_round() {
             const int64_t nd = nbucket[b - 1] + nbucket[b];
             if (!rc && b % 4 == 3 && nd)
                 rc = csim::launch_items_tp(L, ditems + bstart[b - 1], nd, dstates, crest, launch_pt, nmax, nmax,
-                                           part + 4 * bstart[b - 1], partd + 4 * bstart[b - 1], queue, true);
+                                           part + 4 * bstart[b - 1], partd + 4 * bstart[b - 1], queue, true,
+                                           rest_count);
         } else if (nbucket[b]) {
             const int gmax = b % 4 == 1 ? std::min(nmax, lzmax[b]) : nmax;
             rc = csim::launch_items_tp(L, it, nbucket[b], dstates, dcode, launch_pt, nmax, gmax, part + 4 * bstart[b],

@@ -585,13 +585,15 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
         CKR(dbuf(ctx, kBufCode, c * 4, &v));
         int* dcode = (int*)v;
         void* dcanon = nullptr;
-        int *dcode_dir = nullptr, *dcode_rest = nullptr;
+        int *dcode_dir = nullptr, *dcode_rest = nullptr, *drest = nullptr;
         if (tp && tn.kernel == 3) {
             CKR(dbuf(ctx, kBufCanon, (size_t)c * csim::canon_bytes(), &dcanon));
             CKR(dbuf(ctx, kBufCodeDirect, c * 4, &v));
             dcode_dir = (int*)v;
             CKR(dbuf(ctx, kBufCodeRest, c * 4, &v));
             dcode_rest = (int*)v;
+            CKR(dbuf(ctx, kBufRestCount, 4, &v));  // live states of a sub-batch left to the block-prefix kernel
+            drest = (int*)v;
         }
         const size_t nparts = (size_t)c * nchunks * 4;
         CKR(dbuf(ctx, kBufParts, nparts * sizeof(__int128), &v));
@@ -630,11 +632,13 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
             }
             if (csim::launch_project(launch_of(ctx), nr, sth, cs, P->nstabs, dpm, dpz, dpx, scode))
                 return fail(ctx, CSIM_ERR_CUDA, "projection launch failed");
-            if (tp && tn.kernel == 3 &&
-                csim::launch_canon(launch_of(ctx), sth, scode, cs, dsl,
-                                   (unsigned char*)dcanon + (size_t)s0 * csim::canon_bytes(), dcode_dir + s0,
-                                   dcode_rest + s0))
-                return fail(ctx, CSIM_ERR_CUDA, "pivot-form launch failed");
+            if (tp && tn.kernel == 3) {
+                CK(cudaMemsetAsync(drest, 0, 4, ctx->stream));
+                if (csim::launch_canon(launch_of(ctx), sth, scode, cs, dsl,
+                                       (unsigned char*)dcanon + (size_t)s0 * csim::canon_bytes(), dcode_dir + s0,
+                                       dcode_rest + s0, drest))
+                    return fail(ctx, CSIM_ERR_CUDA, "pivot-form launch failed");
+            }
             if (first) CK(cudaEventRecord(ctx->ev[1], ctx->stream));
             first = false;
             __int128* spart = dpart + (size_t)s0 * nchunks * 4;
@@ -681,16 +685,17 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
                                                         jn, chi - jn, pt, P2, spart, nchunks, jn / span);
                     rcode = dcode_rest + s0;
                 }
-                // terms [0, jb): every zero count; terms [jb, chi): at most tn.light zeros
+                // terms [0, jb): every zero count; terms [jb, chi): at most tn.light zeros (for the direct
+                // kernel's fallback, gated on the sub-batch having a state left to it)
                 const int64_t span = 64 * (int64_t)pt;
                 const int64_t jb = std::min(chi, (ctx->cw_split + span - 1) / span * span);
                 if (jb > 0)
                     rc |= csim::launch_terms_tp(launch_of(ctx), t, t, dcw, sth, rcode, cs, 0, jb, pt, P2, spart,
-                                                nchunks, 0, nullptr, nullptr, nullptr);
+                                                nchunks, 0, nullptr, nullptr, nullptr, drest);
                 if (jb < chi)
                     rc |= csim::launch_terms_tp(launch_of(ctx), t, tn.light, dcw + jb, sth, rcode, cs, jb,
                                                 chi - jb, pt, P2, spart, nchunks, jb / span, nullptr, nullptr,
-                                                nullptr);
+                                                nullptr, drest);
             } else {
                 rc = csim::launch_terms(launch_of(ctx), nr, exact ? 1 : 0, dcw, (const csim::GState*)dphis, sth,
                                         scode, cs, 0, chi, (int)chunk, P2, spart, nullptr, nullptr, nullptr, nullptr);

@@ -371,7 +371,7 @@ enum BufId {
     kBufA, kBufB, kBufEps, kBufP, kBufM, kBufXi, kBufZeta, kBufAlpha, kBufCode, kBufWords, kBufOffsets,
     kBufCum, kBufCodewords, kBufAcc, kBufAccDiag, kBufPhis, kBufIdx, kBufConsumed, kBufPm, kBufPz, kBufPx,
     kBufL, kBufParts, kBufPartsDiag, kBufCwOrdered, kBufRunScratch, kBufCanon, kBufCodeDirect, kBufCodeRest,
-    kNumBufs
+    kBufRestCount, kNumBufs
 };
 
 class Engine;                     // csim_engine.cpp: the batched query engine

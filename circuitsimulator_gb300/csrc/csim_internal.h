@@ -47,10 +47,12 @@ int launch_reduce_parts(const Launch& L, const __int128* part, int64_t ntheta, i
 // gmax >= the zeros of every codeword in [j0, j0 + nj) (gmax = nmax always holds).
 // codewords[0] is term j0's codeword.
 // Work item = (theta a, block cb of 64 * per_thread terms): 4 int128 partial sums at
-// part[4 * (a * part_stride + part_base + cb)].
+// part[4 * (a * part_stride + part_base + cb)].  gate (optional, device): when *gate is 0
+// the launch has no live state and its blocks return at once (the direct kernel's fallback).
 int launch_terms_tp(const Launch& L, int nmax, int gmax, const uint64_t* codewords, const GState* theta,
                     const int* code, int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P, __int128* part,
-                    int64_t part_stride, int64_t part_base, int* eps_o, int* p_o, int* m_o);
+                    int64_t part_stride, int64_t part_base, int* eps_o, int* p_o, int* m_o,
+                    const int* gate = nullptr);
 int64_t terms_tp_blocks(int64_t nj, int per_thread);
 // resident blocks per SM of the thread-per-pair kernel for states of up to nmax
 // qubits and codewords of up to gmax zeros (-1 if the query fails)
@@ -65,8 +67,10 @@ int terms_tp_occupancy(int nmax, int gmax);
 // ones of every codeword in the range, which sizes the per-pair rows (a pair
 // with more live variables sets the range error).
 size_t canon_bytes();
+// rest_count (optional): the number of live states left to the block-prefix
+// kernel is added to *rest_count (zero it before the first launch)
 int launch_canon(const Launch& L, const GState* theta, const int* code, int64_t ntheta, int dslots, void* canon,
-                 int* code_direct, int* code_rest);
+                 int* code_direct, int* code_rest, int* rest_count = nullptr);
 int launch_terms_direct(const Launch& L, int nmax, int rows, int dslots, const uint64_t* codewords,
                         const void* canon, const int* code, int64_t ntheta, int64_t j0, int64_t nj, int per_thread,
                         int P, __int128* part, int64_t part_stride, int64_t part_base);

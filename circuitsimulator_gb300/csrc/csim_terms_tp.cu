@@ -56,7 +56,9 @@ __device__ __forceinline__ __int128 shfl_xor_i128(__int128 v, int m) {
 __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, const GState* theta, const int* code,
                                                   int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P,
                                                   int nmax, int gmax, __int128* part, int64_t part_stride,
-                                                  int64_t part_base, int* eps_o, int* p_o, int* m_o, int* err) {
+                                                  int64_t part_base, int* eps_o, int* p_o, int* m_o,
+                                                  const int* gate, int* err) {
+    if (gate && *gate == 0) return;  // no live state (block-uniform)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TPShared& sh = *reinterpret_cast<TPShared*>(smem_raw);
     uint64_t* const sa = reinterpret_cast<uint64_t*>(smem_raw + sizeof(TPShared));
@@ -157,7 +159,7 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
 using pc::CanonG;
 
 __global__ void __launch_bounds__(64) k_canon(const GState* theta, const int* code, int64_t ntheta, int dslots,
-                                               CanonG* out, int* code_direct, int* code_rest) {
+                                               CanonG* out, int* code_direct, int* code_rest, int* rest_count) {
     const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= ntheta) return;
     const GState* g = theta + a;
@@ -166,6 +168,7 @@ __global__ void __launch_bounds__(64) k_canon(const GState* theta, const int* co
     const bool direct = c >= 0 && n - k <= dslots && n >= 1 && n <= 64 && k >= 0 && k <= n;
     code_direct[a] = direct ? c : -1;
     code_rest[a] = direct ? -1 : c;
+    if (rest_count && !direct && c >= 0) atomicAdd(rest_count, 1);
     if (!direct) return;
     uint64_t G[64], J[64];
     for (int r = 0; r < k; r++) {
@@ -245,10 +248,11 @@ __global__ void __launch_bounds__(kTP) k_terms_direct(const uint64_t* codewords,
 size_t canon_bytes() { return sizeof(CanonG); }
 
 int launch_canon(const Launch& L, const GState* theta, const int* code, int64_t ntheta, int dslots, void* canon,
-                 int* code_direct, int* code_rest) {
+                 int* code_direct, int* code_rest, int* rest_count) {
     if (ntheta <= 0) return 0;
     const int64_t blocks = (ntheta + 63) / 64;
-    k_canon<<<(int)blocks, 64, 0, L.stream>>>(theta, code, ntheta, dslots, (CanonG*)canon, code_direct, code_rest);
+    k_canon<<<(int)blocks, 64, 0, L.stream>>>(theta, code, ntheta, dslots, (CanonG*)canon, code_direct, code_rest,
+                                               rest_count);
     (*L.launches)++;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
@@ -440,7 +444,7 @@ size_t terms_tp_smem(int nmax, int gmax) {
 
 int launch_terms_tp(const Launch& L, int nmax, int gmax, const uint64_t* codewords, const GState* theta,
                     const int* code, int64_t ntheta, int64_t j0, int64_t nj, int per_thread, int P, __int128* part,
-                    int64_t part_stride, int64_t part_base, int* eps_o, int* p_o, int* m_o) {
+                    int64_t part_stride, int64_t part_base, int* eps_o, int* p_o, int* m_o, const int* gate) {
     if (ntheta <= 0 || nj <= 0) return 0;
     if (nmax < 1 || nmax > 64 || gmax < 0 || gmax > nmax) return -1;
     const int64_t span = (int64_t)kTP * per_thread;
@@ -457,7 +461,7 @@ int launch_terms_tp(const Launch& L, int nmax, int gmax, const uint64_t* codewor
     int64_t grid = (int64_t)L.num_sms * per_sm;
     if (grid > items) grid = items;
     k_terms_tp<<<(int)grid, kTP, smem, L.stream>>>(codewords, theta, code, ntheta, j0, nj, per_thread, P, nmax, gmax,
-                                                    part, part_stride, part_base, eps_o, p_o, m_o, L.d_err);
+                                                    part, part_stride, part_base, eps_o, p_o, m_o, gate, L.d_err);
     (*L.launches)++;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
