@@ -809,9 +809,10 @@ int tune_run(csim_ctx* ctx, int t, const csim_projector* Pw, const uint64_t* Lw,
     struct Cand {
         int kernel, pt, pct;
     };
-    static const Cand cands[] = {{0, 16, 50}, {0, 16, 60}, {0, 16, 70}, {0, 32, 50}, {0, 32, 60}, {0, 32, 70},
-                                 {1, 16, 50}, {1, 16, 55}, {1, 16, 60}, {1, 32, 50}, {1, 32, 55}, {1, 32, 60},
-                                 {2, 16, 60}, {2, 32, 60}, {3, 16, 60}, {3, 32, 60}};
+    // the direct kernel won at every t measured (by 2.5x to 6.5x); the block-prefix kernel stays
+    // as the one alternative (the run kernel and the occupancy classes are kept for
+    // CSIM_OPT_PAIR_KERNEL 3 and 4, but no longer tried)
+    static const Cand cands[] = {{0, 16, 60}, {0, 32, 60}, {3, 16, 60}, {3, 32, 60}};
     for (const Cand& c : cands) {
         if (rc) break;
         if (c.kernel == 1 && chi % (64 * (int64_t)c.pt) != 0) continue;

@@ -134,11 +134,11 @@ int csim_set_option(csim_ctx *ctx, int32_t option, int64_t value);
 
 /* The autotuner of the thread-per-pair launches (no counterpart in the
  * reference).  For the t bucket of t ([4b, 4b+3]) it times the sampler's own
- * launches with each candidate -- terms per thread per work item 16 or 32
- * (items of 1024 or 2048 pairs; 32 pairs per warp per step) and a
- * light-launch bound of ceil(0.5 t), ceil(0.6 t) or ceil(0.7 t) zeros -- and
- * keeps the fastest for every t of the bucket, for every context on this
- * device in this process.  The trials run projector P and the k-row code L
+ * launches with each candidate -- the direct kernel or the block-prefix
+ * kernel (light launch bound ceil(0.6 t) zeros), each with 16 or 32 terms per
+ * thread per work item (items of 1024 or 2048 pairs; 32 pairs per warp per
+ * step) -- and keeps the fastest for every t of the bucket, for every context
+ * on this device in this process.  The trials run projector P and the k-row code L
  * (the workload about to run; P->nqubits == t) on the tuner's own
  * counter-based states, about 2^25 pairs per trial; with P null they run a
  * synthetic workload (ceil(0.7 t) random Pauli rows, a random min(t, 14)-row
@@ -146,8 +146,10 @@ int csim_set_option(csim_ctx *ctx, int32_t option, int64_t value);
  * first sampler call or batched query at a new t tunes it on its own
  * workload.  The caller's random streams and last statistics are unchanged.
  * Returns the chosen kernel (0 block-prefix with heavy and light launches,
- * 1 per-thread runs, 2 block-prefix with one launch per occupancy class), terms
- * per thread, light bound and the pair-kernel milliseconds of the winning trial.
+ * 3 direct restriction; 1 per-thread runs and 2 block-prefix with one launch
+ * per occupancy class are not tried, only forced), terms per thread, light
+ * bound (t - 33 above 32 qubits for the direct kernel, its narrow/wide split)
+ * and the pair-kernel milliseconds of the winning trial.
  * Any output pointer may be NULL. */
 int csim_autotune(csim_ctx *ctx, int32_t t, const csim_projector *P, const uint64_t *L, int32_t k,
                   int32_t *kernel, int32_t *per_thread, int32_t *light_zeros, double *pair_ms);
