@@ -153,29 +153,134 @@ __global__ void __launch_bounds__(kTP) k_terms_tp(const uint64_t* codewords, con
 }
 
 // ---------------------------------------------------------------- direct restriction
-// k_canon: one thread per state, theta in pivot coordinates (pc::canon_theta);
-// states whose d = n - k exceeds `dslots` are left to the block-prefix kernel
-// (code_direct < 0), the others to the direct kernel (code_rest < 0).
+// k_canon: one warp per state, theta in pivot coordinates: pc::canon_theta's
+// steps with lane l holding variables l and l + 32 (rows of G and J), the
+// pivot step's row set B a ballot and its rank-two update done by every lane
+// on its own rows; states whose d = n - k exceeds `dslots` are left to the
+// block-prefix kernel (code_direct < 0), the others to the direct kernel
+// (code_rest < 0).
 using pc::CanonG;
+
+namespace {
+__device__ __forceinline__ uint64_t shfl_xor_u64(uint64_t v, int m) {
+    const uint32_t lo = __shfl_xor_sync(kFull, (uint32_t)v, m), hi = __shfl_xor_sync(kFull, (uint32_t)(v >> 32), m);
+    return ((uint64_t)hi << 32) | lo;
+}
+__device__ __forceinline__ uint64_t ballot64(bool lo, bool hi) {
+    return (uint64_t)__ballot_sync(kFull, lo) | ((uint64_t)__ballot_sync(kFull, hi) << 32);
+}
+__device__ __forceinline__ uint64_t xor_reduce64(uint64_t v) {
+    for (int o = 16; o > 0; o >>= 1) v ^= shfl_xor_u64(v, o);
+    return v;
+}
+__device__ __forceinline__ uint64_t or_reduce64(uint64_t v) {
+    for (int o = 16; o > 0; o >>= 1) v |= shfl_xor_u64(v, o);
+    return v;
+}
+// coordinate-indexed mask of a variable-indexed one (variable a -> its pivot coordinate)
+__device__ __forceinline__ uint64_t to_coords(uint64_t v, const unsigned char* piv) {
+    uint64_t r = 0ull;
+    while (v) {
+        const int a = __ffsll((long long)v) - 1;
+        v &= v - 1ull;
+        r |= 1ull << piv[a];
+    }
+    return r;
+}
+}  // namespace
 
 __global__ void __launch_bounds__(64) k_canon(const GState* theta, const int* code, int64_t ntheta, int dslots,
                                                CanonG* out, int* code_direct, int* code_rest, int* rest_count) {
-    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= ntheta) return;
-    const GState* g = theta + a;
-    const int c = code ? code[a] : 0;
+    __shared__ unsigned char piv_s[2][64];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    unsigned char* const piv = piv_s[wib];
+    const int64_t a0 = (int64_t)blockIdx.x * 2 + wib;  // this warp's state
+    if (a0 >= ntheta) return;                          // warp-uniform
+    const GState* g = theta + a0;
+    const int c = code ? code[a0] : 0;
     const int n = g->n, k = g->k;
     const bool direct = c >= 0 && n - k <= dslots && n >= 1 && n <= 64 && k >= 0 && k <= n;
-    code_direct[a] = direct ? c : -1;
-    code_rest[a] = direct ? -1 : c;
-    if (rest_count && !direct && c >= 0) atomicAdd(rest_count, 1);
-    if (!direct) return;
-    uint64_t G[64], J[64];
-    for (int r = 0; r < k; r++) {
-        G[r] = g->G[r];
-        J[r] = g->J[r];
+    if (lane == 0) {
+        code_direct[a0] = direct ? c : -1;
+        code_rest[a0] = direct ? -1 : c;
+        if (rest_count && !direct && c >= 0) atomicAdd(rest_count, 1);
     }
-    pc::canon_theta(n, k, g->Q, g->h, g->D1, g->D2, G, J, out[a].Jc, out[a].acol, out[a].cs);
+    if (!direct) return;  // warp-uniform
+    CanonG& o = out[a0];
+    const uint64_t nm = pc::lowmask(n), km = pc::lowmask(k);
+    const int r0 = lane, r1 = lane + 32;  // this lane's variables
+    uint64_t g0 = r0 < k ? g->G[r0] & nm : 0ull, g1 = r1 < k ? g->G[r1] & nm : 0ull;
+    uint64_t j0 = r0 < k ? g->J[r0] & km : 0ull, j1 = r1 < k ? g->J[r1] & km : 0ull;
+    uint64_t D1 = g->D1 & km, D2 = g->D2 & km;
+    int p0 = 0, p1 = 0;
+    // Gauss-Jordan on the rows of G: rows b of B += row a (u_a = u'_a + u'_b), J <- R J R^T with
+    // rows in B getting J_a and rows in C getting B, D_b += D_a + 4 J_ab (pc::canon_theta)
+    for (int a = 0; a < k; a++) {
+        const int src = a & 31;
+        const bool up = a >= 32;
+        const uint64_t ga = shfl64(up ? g1 : g0, src);
+        const int pcol = ga ? __ffsll((long long)ga) - 1 : 0;
+        if (lane == src) {
+            if (up) p1 = pcol;
+            else p0 = pcol;
+        }
+        const bool in0 = r0 < k && r0 != a && ((g0 >> pcol) & 1ull), in1 = r1 < k && r1 != a && ((g1 >> pcol) & 1ull);
+        const uint64_t B = ballot64(in0, in1);
+        if (!B) continue;  // warp-uniform
+        if (in0) g0 ^= ga;
+        if (in1) g1 ^= ga;
+        const uint64_t Ja = shfl64(up ? j1 : j0, src);
+        const uint64_t C = Ja ^ (((Ja >> a) & 1ull) ? B : 0ull);
+        j0 ^= (((B >> r0) & 1ull) ? Ja : 0ull) ^ (((C >> r0) & 1ull) ? B : 0ull);
+        j1 ^= (((B >> r1) & 1ull) ? Ja : 0ull) ^ (((C >> r1) & 1ull) ? B : 0ull);
+        pc::add_D64(D1, D2, B, (int)((D1 >> a) & 1ull), (int)((D2 >> a) & 1ull));
+        D2 ^= B & Ja;
+    }
+    // shift v = u + w, w_a = h at a's pivot: in order of a, Q += D_a and D_a -> -D_a, D_b += 4 J_ab;
+    // D_a as read at step a carries the earlier steps' flips J_{a'a}, a' < a in w
+    const bool w0 = r0 < k && ((g->h >> p0) & 1ull), w1 = r1 < k && ((g->h >> p1) & 1ull);
+    const uint64_t wv = ballot64(w0, w1);
+    int dq = 0;
+    if (w0) dq += 2 * (2 * (int)(((D2 >> r0) ^ (uint64_t)__popcll(j0 & wv & pc::lowmask(r0))) & 1ull) +
+                       (int)((D1 >> r0) & 1ull));
+    if (w1) dq += 2 * (2 * (int)(((D2 >> r1) ^ (uint64_t)__popcll(j1 & wv & pc::lowmask(r1))) & 1ull) +
+                       (int)((D1 >> r1) & 1ull));
+    dq = (int)__reduce_add_sync(kFull, (unsigned)dq);
+    const uint64_t flips = xor_reduce64((w0 ? j0 & ~(1ull << r0) : 0ull) ^ (w1 ? j1 & ~(1ull << r1) : 0ull));
+    D2 ^= (D1 & wv) ^ (flips & km);
+    // to coordinate indexing
+    piv[r0] = (unsigned char)(r0 < k ? p0 : 0);
+    piv[r1] = (unsigned char)(r1 < k ? p1 : 0);
+    __syncwarp();
+    const uint64_t P = or_reduce64((r0 < k ? 1ull << p0 : 0ull) | (r1 < k ? 1ull << p1 : 0ull));
+    o.Jc[r0] = 0ull;
+    o.Jc[r1] = 0ull;
+    o.acol[r0] = 0ull;
+    o.acol[r1] = 0ull;
+    __syncwarp();
+    if (r0 < k) o.Jc[p0] = to_coords(j0, piv);
+    if (r1 < k) o.Jc[p1] = to_coords(j1, piv);
+    // each non-pivot coordinate: the variables its coordinate depends on, and the constraint's bit
+    uint64_t bm = 0ull;
+    for (uint64_t np = ~P & nm; np;) {
+        const int cc = __ffsll((long long)np) - 1;
+        np &= np - 1ull;
+        const uint64_t av = ballot64(r0 < k && ((g0 >> cc) & 1ull), r1 < k && ((g1 >> cc) & 1ull));
+        if (lane == (cc & 31)) o.acol[cc] = to_coords(av, piv);
+        if ((((g->h >> cc) & 1ull) ^ (uint64_t)(__popcll(wv & av) & 1)) != 0ull) bm |= 1ull << cc;
+    }
+    if (lane == 0) {
+        pc::Canon cs;
+        cs.P = P;
+        cs.D1 = to_coords(D1, piv);
+        cs.D2 = to_coords(D2, piv);
+        cs.bm = bm;
+        cs.Q = (g->Q + dq) & 7;
+        cs.k = k;
+        cs.n = n;
+        cs.pad = 0;
+        o.cs = cs;
+    }
 }
 
 // The direct kernel: one thread per (theta, term) pair like k_terms_tp, each
@@ -250,7 +355,7 @@ size_t canon_bytes() { return sizeof(CanonG); }
 int launch_canon(const Launch& L, const GState* theta, const int* code, int64_t ntheta, int dslots, void* canon,
                  int* code_direct, int* code_rest, int* rest_count) {
     if (ntheta <= 0) return 0;
-    const int64_t blocks = (ntheta + 63) / 64;
+    const int64_t blocks = (ntheta + 1) / 2;  // a warp per state
     k_canon<<<(int)blocks, 64, 0, L.stream>>>(theta, code, ntheta, dslots, (CanonG*)canon, code_direct, code_rest,
                                                rest_count);
     (*L.launches)++;
