@@ -126,22 +126,26 @@ ROWOPS_PER_PAIR_T40 = 2576.0
 DIRECT_ROWS_PER_PAIR_T40 = 151.1
 
 
-# ncu dram__bytes_read.sum + dram__bytes_write.sum of one pair-kernel launch over
-# 64 projected c2 states: the light block-prefix launch
-# (profiles/k_terms_tp_c2_small.md: 657 KB read, 600 KB written) and the direct
-# launch (profiles/k_terms_direct_c2_small.md: 673 KB read, 1071 KB written).  Reads
-# are the 512 KB codeword table and the states; writes are the partial sums and
-# the write-back of lines the L2 flush left dirty.
-MEASURED_TRAFFIC_64_STATES = {"block prefix": 657e3 + 600e3, "direct": 673e3 + 1071e3}
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of pair-kernel launches over
+# projected c2 states.  The block-prefix kernel: the light launch over 64 states
+# (profiles/k_terms_tp_c2_small.md: 657 KB read, 600 KB written), the codeword
+# table once and the rest in proportion to the states.  The direct kernel: its
+# H' launch over 64 and over 256 states (profiles/k_terms_direct_c2_small.md:
+# 1.52 MB and 2.62 MB), a line through the two; per state 1.08 KB is read (the
+# pivot form) and 4.66 KB written (the partial sums, and the write-back of the
+# states and pivot forms the launches before it left in L2).
+MEASURED_TRAFFIC_64_STATES = 657e3 + 600e3
 MEASURED_TRAFFIC_CODEWORDS = 8 * 2 ** 16
+DIRECT_TRAFFIC = ((64, 677888 + 843264), (256, 884736 + 1737472))
 
 
 def dram_bytes_per_launch(states, kernel="block prefix"):
-    """DRAM bytes of one pair-kernel launch over `states` states, scaled from
-    the measured 64-state capture: the codeword table once, the rest in
-    proportion to the states (the states read and the partial sums written
-    both grow with them)."""
-    per_state = (MEASURED_TRAFFIC_64_STATES[kernel] - MEASURED_TRAFFIC_CODEWORDS) / 64
+    """DRAM bytes of one pair-kernel launch over `states` states, from the
+    measured captures above."""
+    if kernel == "direct":
+        (s0, b0), (s1, b1) = DIRECT_TRAFFIC
+        return b0 + (b1 - b0) / (s1 - s0) * (states - s0)
+    per_state = (MEASURED_TRAFFIC_64_STATES - MEASURED_TRAFFIC_CODEWORDS) / 64
     return MEASURED_TRAFFIC_CODEWORDS + per_state * states
 
 
@@ -303,9 +307,11 @@ def run_ours(args, rank, world, local_rank):
                 "frac": (achieved / peak) if achieved else None,
                 "traffic": dram_bytes_per_launch(samples * bins / world,
                                                  "direct" if tuned[3] == 3 else "block prefix"),
-                "traffic_source": "ncu dram bytes of a 64-state launch of this kernel (profiles/%s), scaled to "
-                                  "this launch's states" % ("k_terms_direct_c2_small.md" if tuned[3] == 3
-                                                            else "k_terms_tp_c2_small.md"),
+                "traffic_source": ("ncu dram bytes (read + write) of this kernel's launches over 64 and 256 states "
+                                   "(profiles/k_terms_direct_c2_small.md), on the line through them"
+                                   if tuned[3] == 3 else
+                                   "ncu dram bytes (read + write) of a 64-state launch of this kernel "
+                                   "(profiles/k_terms_tp_c2_small.md), scaled to this launch's states"),
                 "work_unit": "packed row-op of the reference's algorithm (one 64-bit row test/XOR/update of its "
                              "elementary updates), whichever kernel runs",
                 "rowops_per_pair": per_pair,
