@@ -1442,15 +1442,36 @@ CSIM_HD_INLINE void direct_compact(const Canon& cs, const uint64_t* Jc, const ui
     s.D2 = compress_word<MODE, RHI>(cs.D2, nlo, nhi, plo);
     const int fmax = uniform_max(f);
     uint32_t rl = (uint32_t)F0, rh = (uint32_t)(F0 >> 32);  // live coordinates not yet taken
+    // with at most 8 live high coordinates (RHI 3), the high bytes of a unit's four rows go
+    // through one compress: the move masks repeated in each byte move every byte's bits within it
+    const bool pack = MODE == kCompactSplit && RHI == 3;
+    CompressNet n4 = nhi;
+    if (pack) {
+        n4.m = (nhi.m & 0xFFu) * 0x01010101u;
+#pragma unroll
+        for (int i = 0; i < 3; i++) n4.mv[i] = (nhi.mv[i] & 0xFFu) * 0x01010101u;
+    }
     for (int u = 0; 4 * u < (fmax < 32 ? fmax : 32); u++) {
         uint32_t w[4];
+        uint32_t hb = 0u;
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const bool inlo = MODE == kCompactLow || rl != 0u;
             const int c = inlo ? WordTraits<uint32_t>::ffs(rl) - 1 : 31 + WordTraits<uint32_t>::ffs(rh);
             if (inlo) rl &= rl - 1u;
             else rh &= rh - 1u;
-            w[q] = (uint32_t)compress_word<MODE, RHI>(Jc[c & 63], nlo, nhi, plo);
+            const uint64_t row = Jc[c & 63];
+            if (pack) {
+                w[q] = compress32<5>((uint32_t)row, nlo);
+                hb |= ((uint32_t)(row >> 32) & 0xFFu) << (8 * q);
+            } else {
+                w[q] = (uint32_t)compress_word<MODE, RHI>(row, nlo, nhi, plo);
+            }
+        }
+        if (pack) {
+            const uint32_t hc = compress32<3>(hb, n4);
+#pragma unroll
+            for (int q = 0; q < 4; q++) w[q] |= shl32_upto32((hc >> (8 * q)) & 0xFFu, plo);
         }
         if (4 * u < f) {
             U32x4 v;
