@@ -1442,18 +1442,23 @@ CSIM_HD_INLINE void direct_compact(const Canon& cs, const uint64_t* Jc, const ui
     s.D2 = compress_word<MODE, RHI>(cs.D2, nlo, nhi, plo);
     const int fmax = uniform_max(f);
     uint32_t rl = (uint32_t)F0, rh = (uint32_t)(F0 >> 32);  // live coordinates not yet taken
-    // with at most 8 live high coordinates (RHI 3), the high bytes of a unit's four rows go
-    // through one compress: the move masks repeated in each byte move every byte's bits within it
-    const bool pack = MODE == kCompactSplit && RHI == 3;
-    CompressNet n4 = nhi;
+    // with at most 8 (RHI 3) or 16 (RHI 4) live high coordinates, the high parts of a unit's
+    // rows share compresses, four bytes or two 16-bit halves to a word: the move masks repeated
+    // in each lane move every lane's bits within it
+    constexpr int kLanes = RHI == 3 ? 4 : (RHI == 4 ? 2 : 1);
+    constexpr int kLaneBits = 32 / kLanes;
+    constexpr uint32_t kLaneMask = kLanes == 4 ? 0xFFu : 0xFFFFu;
+    constexpr uint32_t kRepeat = kLanes == 4 ? 0x01010101u : 0x00010001u;
+    const bool pack = MODE == kCompactSplit && kLanes > 1;
+    CompressNet nrep = nhi;
     if (pack) {
-        n4.m = (nhi.m & 0xFFu) * 0x01010101u;
+        nrep.m = (nhi.m & kLaneMask) * kRepeat;
 #pragma unroll
-        for (int i = 0; i < 3; i++) n4.mv[i] = (nhi.mv[i] & 0xFFu) * 0x01010101u;
+        for (int i = 0; i < RHI && i < 5; i++) nrep.mv[i] = (nhi.mv[i] & kLaneMask) * kRepeat;
     }
     for (int u = 0; 4 * u < (fmax < 32 ? fmax : 32); u++) {
         uint32_t w[4];
-        uint32_t hb = 0u;
+        uint32_t hb[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const bool inlo = MODE == kCompactLow || rl != 0u;
@@ -1463,15 +1468,18 @@ CSIM_HD_INLINE void direct_compact(const Canon& cs, const uint64_t* Jc, const ui
             const uint64_t row = Jc[c & 63];
             if (pack) {
                 w[q] = compress32<5>((uint32_t)row, nlo);
-                hb |= ((uint32_t)(row >> 32) & 0xFFu) << (8 * q);
+                hb[q / kLanes] |= ((uint32_t)(row >> 32) & kLaneMask) << (kLaneBits * (q % kLanes));
             } else {
                 w[q] = (uint32_t)compress_word<MODE, RHI>(row, nlo, nhi, plo);
             }
         }
         if (pack) {
-            const uint32_t hc = compress32<3>(hb, n4);
+            uint32_t hc[4];
 #pragma unroll
-            for (int q = 0; q < 4; q++) w[q] |= shl32_upto32((hc >> (8 * q)) & 0xFFu, plo);
+            for (int g = 0; g < 4 / kLanes; g++) hc[g] = compress32<RHI>(hb[g], nrep);
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                w[q] |= shl32_upto32((hc[q / kLanes] >> (kLaneBits * (q % kLanes))) & kLaneMask, plo);
         }
         if (4 * u < f) {
             U32x4 v;

@@ -182,7 +182,8 @@ def test_runs_vs_oracle(tp, oracle, t, k, run_len):
 
 
 @pytest.mark.parametrize("t,k,nshrink", [(1, 1, 0), (3, 3, 0), (8, 4, 0), (12, 6, 4), (24, 8, 0), (33, 8, 0),
-                                         (40, 10, 0), (40, 10, 20), (57, 8, 0), (64, 9, 0), (64, 8, 40)])
+                                         (40, 10, 0), (40, 10, 20), (44, 9, 0), (48, 9, 6), (57, 8, 0), (64, 9, 0),
+                                         (64, 8, 40)])
 def test_direct_vs_oracle(tp, oracle, t, k, nshrink):
     """The direct kernel's path: theta once in pivot coordinates
     (canon_theta), each pair by removing the variables at x's zero pivot
