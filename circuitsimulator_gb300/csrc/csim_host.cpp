@@ -64,8 +64,11 @@ extern "C" void csim_ctx_destroy(csim_ctx* ctx) {
     for (int i = 0; i < kNumBufs + 32; i++)
         if (ctx->buf[i]) cudaFree(ctx->buf[i]);
     if (ctx->d_err) cudaFree(ctx->d_err);
-    for (int i = 0; i < 4; i++)
+    for (int i = 0; i < 4; i++) {
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+        if (ctx->pin_ev[i]) cudaEventDestroy(ctx->pin_ev[i]);
+        if (ctx->pin[i]) cudaFreeHost(ctx->pin[i]);
+    }
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -607,7 +610,7 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
         const int64_t sub = rng == CSIM_RNG_LIBC ? std::min<int64_t>(c, 1024) : c;
         const int64_t sub0 = rng == CSIM_RNG_LIBC ? std::min<int64_t>(c, 256) : c;
         bool first = true;
-        for (int64_t s0 = 0; s0 < c;) {
+        for (int64_t s0 = 0, sb = 0; s0 < c; sb++) {
             const int64_t cs = std::min(first ? sub0 : sub, c - s0);
             csim::GState* sth = (csim::GState*)((csim_state*)dth + s0);
             int* scode = dcode + s0;
@@ -618,10 +621,12 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
                     draw_state_words(ctx->lr, t, hcum, words);
                     offs.push_back((int64_t)words.size());
                 }
+                // pinned staging, alternating slot pairs: the upload does not wait for the sub-batch
+                // before it, so the host goes on to draw the next one
                 uint32_t* dw;
                 int64_t* doff;
-                CKR(dput(ctx, kBufWords, words.data(), words.size(), &dw));
-                CKR(dput(ctx, kBufOffsets, offs.data(), offs.size(), &doff));
+                CKR(staged_put(ctx, 2 * (sb & 1), kBufWords, words.data(), words.size(), &dw));
+                CKR(staged_put(ctx, 2 * (sb & 1) + 1, kBufOffsets, offs.data(), offs.size(), &doff));
                 if (csim::launch_random_states(launch_of(ctx), t, cs, 1, 0, 0, dw, doff, dcum, sth, nullptr))
                     return fail(ctx, CSIM_ERR_CUDA, "random state launch failed");
             } else {

@@ -394,6 +394,10 @@ struct csim_ctx {
     int pair_kernel = 0;  // CSIM_OPT_PAIR_KERNEL
     int per_thread = 0;  // CSIM_OPT_PER_THREAD; 0 = auto_per_thread(t)
     cudaEvent_t ev[4] = {};
+    // pinned staging of host-made uploads (staged_put): four slots, each with the event of its last copy
+    void* pin[4] = {};
+    size_t pin_cap[4] = {};
+    cudaEvent_t pin_ev[4] = {};
     Engine* engine = nullptr;  // created by the first batched csim_run_queries
     std::vector<uint64_t> cw_key;  // (k, rows of L, t, light bound) of the ordered codeword table in kBufCwOrdered
     int64_t cw_split = 0;          // first index of that table whose codewords have <= the light bound's zeros
@@ -466,6 +470,38 @@ inline int dput(csim_ctx* ctx, int id, const T* src, size_t count, T** out) {
     CKR(dbuf(ctx, id, count * sizeof(T), &p));
     if (count) CK(cudaMemcpyAsync(p, src, count * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
     ctx->stats.h2d_bytes += (int64_t)(count * sizeof(T));
+    *out = (T*)p;
+    return 0;
+}
+
+// dput through pinned staging slot `slot`: an upload from pageable memory first waits for the
+// stream, one from pinned memory returns at once, so the host can prepare the next upload
+// while the GPU works.  The slot's previous copy must have run before the slot is rewritten;
+// alternating slots makes that wait rare.
+template <class T>
+inline int staged_put(csim_ctx* ctx, int slot, int id, const T* src, size_t count, T** out) {
+    void* p;
+    const size_t bytes = count * sizeof(T);
+    CKR(dbuf(ctx, id, bytes, &p));
+    if (ctx->pin_ev[slot]) CK(cudaEventSynchronize(ctx->pin_ev[slot]));
+    else CK(cudaEventCreateWithFlags(&ctx->pin_ev[slot], cudaEventDisableTiming));
+    if (ctx->pin_cap[slot] < bytes) {
+        if (ctx->pin[slot]) cudaFreeHost(ctx->pin[slot]);
+        ctx->pin[slot] = nullptr;
+        ctx->pin_cap[slot] = 0;
+        const size_t c = bytes + bytes / 4;
+        if (cudaMallocHost(&ctx->pin[slot], c) != cudaSuccess) {
+            ctx->pin[slot] = nullptr;
+            return fail(ctx, CSIM_ERR_NOMEM, "cudaMallocHost of %zu bytes failed", c);
+        }
+        ctx->pin_cap[slot] = c;
+    }
+    if (count) {
+        memcpy(ctx->pin[slot], src, bytes);
+        CK(cudaMemcpyAsync(p, ctx->pin[slot], bytes, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    CK(cudaEventRecord(ctx->pin_ev[slot], ctx->stream));
+    ctx->stats.h2d_bytes += (int64_t)bytes;
     *out = (T*)p;
     return 0;
 }
