@@ -452,22 +452,6 @@ CSIM_HD inline void tp_factor_dimer(WAcc& w, int A, int B, int& err) {
     w.m += z ? 0 : (code & 7);
 }
 
-// One monomer factor partialGamma(A) (dimer = false) or dimer factor Gamma(A, B)
-// folded into w, A and B even and non-negative, without a branch on which:
-// both codes come from 4-bit tables (bit 3 zero, bits 0..2 the power of w);
-// the power of sqrt2 is 2 unless a monomer's power of w is odd.
-constexpr uint32_t kMonoCodes = 0x7810u;  // A/2 mod 4 = 0, 1, 2, 3: w^0 (p 2), w^1 (p 1), zero, w^7 (p 1)
-CSIM_HD inline void fold_factor(WAcc& w, bool dimer, int A, int B, int& err) {
-    if ((A | B) & 1) err |= kErrGamma;
-    const int ia = (A >> 1) & 3, idx = 4 * ia + ((B >> 1) & 3);
-    const uint32_t half = (idx & 8) ? (uint32_t)(kGammaCodes >> 32) : (uint32_t)kGammaCodes;
-    const int code = dimer ? (int)((half >> (4 * (idx & 7))) & 15u) : (int)((kMonoCodes >> (4 * ia)) & 15u);
-    const int z = code >> 3, m = code & 7;
-    w.zero |= z;
-    w.p += z ? 0 : ((dimer || m == 0) ? 2 : 1);
-    w.m += z ? 0 : m;
-}
-
 // exponentialSumExact (stabilizer.c:300-481), symmetric J; `act` as for tp_shrink.
 template <class W>
 CSIM_HD inline void tp_exp_sum(PairRegs& s, const PairMem& M, bool act, int& eps, int& p, int& m, int& err) {
@@ -1177,30 +1161,43 @@ CSIM_HD inline int md_shrink(PairRegs& s, uint64_t& F, const PairMem& M, int q, 
     }
     return act ? 1 - beta : 1;
 }
+// The factors md_exp_sum's elimination has folded into W0 and W1 (bit 0 and
+// bit 1 of `zero` and `m4`).  Every variable it eliminates has D/2 even (the
+// first substitution leaves D1 only at sidx, and no step changes D1), so D is
+// 4 D2 there, and 4 (D2 ^ J_x,sidx) in W1's form.  A monomer factor
+// 1 + w^D is then 2 or 0 and a dimer factor Gamma is 2 or -2: each step adds
+// 2 to p, a monomer with D = 4 makes the sum zero and a dimer with both D = 4
+// adds 4 to m.
+struct MdAcc {
+    int zero, m4, steps;
+};
+
 // One step of md_exp_sum's elimination: the monomer or dimer of the highest
-// row in E, its factors folded into W0 (and W1 when sidx >= 0), the rest of E
-// updated.  E and keep are carried in 64-bit words between steps, so the sum
-// can go on in 32-bit words once no lane has a row in play at or above 32.
+// row in E, its factors folded into w, the rest of E updated.  E and keep are
+// carried in 64-bit words between steps, so the sum can go on in 32-bit words
+// once no lane has a row in play at or above 32.
 template <class W>
-CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64, int sidx, W& D1, W& D2, WAcc& w0,
-                                WAcc& w1, int& err) {
+CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64, int sidx, W& D2, MdAcc& w) {
     using T = WordTraits<W>;
     W E = (W)E64;
     const W keep = (W)keep64;
     const bool live = E != (W)0;
-    const int KP = live ? 64 - hd_clz64((uint64_t)(E | keep | (sidx >= 0 ? wbit<W>(sidx) : (W)0))) : 0;
+    const W es = sidx >= 0 ? wbit<W>(sidx) : (W)0;
+    const int KP = live ? 64 - hd_clz64((uint64_t)(E | keep | es)) : 0;
     const int a = live ? T::bits - 1 - T::clz(E) : 0;
     const W ra = live ? md_read_row<W>(M, a, KP) : (W)0;
     const W K = ra & E & ~wbit<W>(a);
     const bool dimer = K != (W)0;
     const int b = dimer ? T::bits - 1 - T::clz(K) : 0;
     const W rb = dimer ? md_read_row<W>(M, b, KP) : (W)0;
-    // the monomer {a} or dimer {a, b} factor of W0, and of W1 (D + 4 J at sidx)
-    const int Da = 2 * (2 * wget<W>(D2, a) + wget<W>(D1, a));
-    const int Db = dimer ? 2 * (2 * wget<W>(D2, b) + wget<W>(D1, b)) : 0;
+    // D2 of a and b in W0's form (bit 0) and W1's (bit 1)
+    const int da2 = wget<W>(D2, a), db2 = dimer ? wget<W>(D2, b) : 0;
+    const int fa = (da2 ? 3 : 0) ^ ((ra & es) != (W)0 ? 2 : 0);
+    const int fb = (db2 ? 3 : 0) ^ ((rb & es) != (W)0 ? 2 : 0);
     if (live) {
-        fold_factor(w0, dimer, Da, Db, err);
-        if (sidx >= 0) fold_factor(w1, dimer, Da + 4 * wget<W>(ra, sidx), Db + 4 * wget<W>(rb, sidx), err);
+        w.steps++;
+        if (dimer) w.m4 ^= fa & fb;
+        else w.zero |= fa;
     }
     const W Ep = dimer ? (E & ~wbit<W>(a) & ~wbit<W>(b)) : (E & ~wbit<W>(a));
     const W vb = dimer ? (ra & Ep) : (W)0, va = dimer ? (rb & Ep) : (W)0;
@@ -1210,7 +1207,6 @@ CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64
     // read (Ep and sidx).  Since J_ab = 1 for a dimer, R J R^T there is the symmetric rank-two
     // update x ^= (vb_x ? Pm : 0) ^ (va_x ? Qm : 0) (vb_x = J_ax, va_x = J_bx), column sidx
     // included through bit sidx of rows a and b.
-    const W es = sidx >= 0 ? wbit<W>(sidx) : (W)0;
     const W Pm = va ^ (jbb ? vb : (W)0) ^ (rb & es);
     const W Qm = vb ^ (jaa ? va : (W)0) ^ (ra & es);
     {
@@ -1255,12 +1251,8 @@ CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64
                 R64(sidx) ^= (uint64_t)((wget<W>(rb, sidx) ? vb : (W)0) ^ (wget<W>(ra, sidx) ? va : (W)0));
         }
     }
-    if (upd) {
-        const int db1 = wget<W>(D1, b), db2 = wget<W>(D2, b), da1 = wget<W>(D1, a), da2 = wget<W>(D2, a);
-        add_Dw<W>(D1, D2, vb, db1, db2);
-        add_Dw<W>(D1, D2, va, da1, da2);
-        D2 ^= (vb & rb) ^ (va & ra) ^ (vb & va);  // J_ab = 1 for a dimer, the only step that updates
-    }
+    if (upd)  // the dimer's D update of the rows in Ep; D1 is zero at a and b, so only D2 changes
+        D2 ^= (db2 ? vb : (W)0) ^ (da2 ? va : (W)0) ^ (vb & rb) ^ (va & ra) ^ (vb & va);
     if (live) E = Ep;
     E64 = (uint64_t)E;
 }
@@ -1296,9 +1288,10 @@ CSIM_HD inline void md_exp_sum(PairRegs& s, const PairMem& M, uint64_t F, bool a
         }
     }
     W E = Fw & ~(sidx >= 0 ? wbit<W>(sidx) : (W)0);
+    if ((D1 & E) != (W)0) err |= kErrGamma;  // MdAcc's premise
     // in 64-bit mode the row sidx >= 32 stays updated: its bits are bit sidx of the rows below 32
     const W keep = (sizeof(W) == 8 && sidx >= 32) ? wbit<W>(sidx) : (W)0;
-    WAcc w0 = {0, 0, 0}, w1 = {0, 0, 0};
+    MdAcc acc = {0, 0, 0};
     const bool any = E != (W)0;
     const int NE = uniform_max(T::popc(E));
     uint64_t E64 = (uint64_t)E;
@@ -1308,20 +1301,21 @@ CSIM_HD inline void md_exp_sum(PairRegs& s, const PairMem& M, uint64_t F, bool a
         // rows below 32 alone (and sidx below 32): on in 32-bit words
         if (sizeof(W) == 8 && uniform_max(64 - hd_clz64(E64 | (sidx >= 0 ? bit1(sidx) : 0ull))) <= CSIM_TP_WIDE_FROM)
             break;
-        md_exp_step<W>(M, E64, (uint64_t)keep, sidx, D1, D2, w0, w1, err);
+        md_exp_step<W>(M, E64, (uint64_t)keep, sidx, D2, acc);
     }
     if (sizeof(W) == 8 && it < NE) {
         // the rest of E and sidx lie below 32 (or E is empty): steps in 32-bit words, which leave
         // the D bits from 32 up as they are
-        uint32_t d1 = (uint32_t)D1, d2 = (uint32_t)D2;
+        uint32_t d2 = (uint32_t)D2;
         for (; it < NE; it++) {
             if (uniform_max(E64 ? 1 : 0) == 0) break;
-            md_exp_step<uint32_t>(M, E64, 0ull, sidx, d1, d2, w0, w1, err);
+            md_exp_step<uint32_t>(M, E64, 0ull, sidx, d2, acc);
         }
-        D1 = (D1 & ~(W)0xffffffffu) | (W)d1;
         D2 = (D2 & ~(W)0xffffffffu) | (W)d2;
     }
     if (!act) return;
+    const WAcc w0 = {acc.zero & 1, 2 * acc.steps, 4 * (acc.m4 & 1)};
+    const WAcc w1 = {(acc.zero >> 1) & 1, 2 * acc.steps, 4 * ((acc.m4 >> 1) & 1)};
     if (Fw == (W)0) {  // Wsigma's k == 0 case
         eps = 1;
         p = 0;
