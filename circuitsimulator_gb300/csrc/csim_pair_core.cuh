@@ -226,6 +226,13 @@ CSIM_HD inline int uniform_max(int v) {
     return v;
 #endif
 }
+CSIM_HD inline bool uniform_any(bool v) {
+#if defined(__CUDA_ARCH__)
+    return __any_sync(0xffffffffu, v) != 0;
+#else
+    return v;
+#endif
+}
 CSIM_HD inline int uniform_min(int v) {
 #if defined(__CUDA_ARCH__)
     return (int)__reduce_min_sync(0xffffffffu, (unsigned)v);
@@ -1210,10 +1217,12 @@ CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64
     const W Pm = va ^ (jbb ? vb : (W)0) ^ (rb & es);
     const W Qm = vb ^ (jaa ? va : (W)0) ^ (ra & es);
     {
+        // rows from 0: the warp's lowest row in play is nearly always 0 after the renumbering,
+        // and finding it costs more than the rows it would skip
         const W zm = upd ? Ep : (W)0;
-        const int lo = zm ? T::ffs(zm) - 1 : T::bits, hi = zm ? T::bits - T::clz(zm) : 0;
-        const int X0 = uniform_min(lo) & ~3, X1 = uniform_max(hi);
-        if (live) CSIM_COUNT_ROWS((dimer ? 2 : 1) + (upd ? hi - lo : 0));
+        const int hi = zm ? T::bits - T::clz(zm) : 0;
+        const int X0 = 0, X1 = uniform_max(hi);
+        if (live) CSIM_COUNT_ROWS((dimer ? 2 : 1) + (upd ? hi - (T::ffs(zm) - 1) : 0));
         const W rvb = wbrev(vb), rva = wbrev(va);
         {
             const int sh = T::bits - 32;
@@ -1297,7 +1306,7 @@ CSIM_HD inline void md_exp_sum(PairRegs& s, const PairMem& M, uint64_t F, bool a
     uint64_t E64 = (uint64_t)E;
     int it = 0;
     for (; it < NE; it++) {
-        if (uniform_max(E64 ? 1 : 0) == 0) break;
+        if (!uniform_any(E64 != 0ull)) break;
         // rows below 32 alone (and sidx below 32): on in 32-bit words
         if (sizeof(W) == 8 && uniform_max(64 - hd_clz64(E64 | (sidx >= 0 ? bit1(sidx) : 0ull))) <= CSIM_TP_WIDE_FROM)
             break;
@@ -1308,7 +1317,7 @@ CSIM_HD inline void md_exp_sum(PairRegs& s, const PairMem& M, uint64_t F, bool a
         // the D bits from 32 up as they are
         uint32_t d2 = (uint32_t)D2;
         for (; it < NE; it++) {
-            if (uniform_max(E64 ? 1 : 0) == 0) break;
+            if (!uniform_any(E64 != 0ull)) break;
             md_exp_step<uint32_t>(M, E64, 0ull, sidx, d2, acc);
         }
         D2 = (D2 & ~(W)0xffffffffu) | (W)d2;
