@@ -1209,13 +1209,14 @@ CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64
     const W Ep = dimer ? (E & ~wbit<W>(a) & ~wbit<W>(b)) : (E & ~wbit<W>(a));
     const W vb = dimer ? (ra & Ep) : (W)0, va = dimer ? (rb & Ep) : (W)0;
     const bool upd = (vb | va) != (W)0;
-    const int jaa = wget<W>(ra, a), jbb = wget<W>(rb, b);
     // Rows a and b are not read again, so only rows x of Ep change, and only in the columns still
     // read (Ep and sidx).  Since J_ab = 1 for a dimer, R J R^T there is the symmetric rank-two
     // update x ^= (vb_x ? Pm : 0) ^ (va_x ? Qm : 0) (vb_x = J_ax, va_x = J_bx), column sidx
-    // included through bit sidx of rows a and b.
-    const W Pm = va ^ (jbb ? vb : (W)0) ^ (rb & es);
-    const W Qm = vb ^ (jaa ? va : (W)0) ^ (ra & es);
+    // included through bit sidx of rows a and b.  The full update also adds J_bb vb to Pm and
+    // J_aa va to Qm; J's diagonal is D1 (J_xx = D/2 mod 2, kept so by every substitution), which
+    // is 0 at a and b.
+    const W Pm = va ^ (rb & es);
+    const W Qm = vb ^ (ra & es);
     {
         // rows from 0: the warp's lowest row in play is nearly always 0 after the renumbering,
         // and finding it costs more than the rows it would skip
@@ -1261,7 +1262,7 @@ CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64
         }
     }
     if (upd)  // the dimer's D update of the rows in Ep; D1 is zero at a and b, so only D2 changes
-        D2 ^= (db2 ? vb : (W)0) ^ (da2 ? va : (W)0) ^ (vb & rb) ^ (va & ra) ^ (vb & va);
+        D2 ^= (db2 ? vb : (W)0) ^ (da2 ? va : (W)0) ^ (vb & va);  // (vb & rb) = (va & ra) cancel
     if (live) E = Ep;
     E64 = (uint64_t)E;
 }
