@@ -606,12 +606,13 @@ int sample_values(csim_ctx* ctx, const csim_projector* P, const uint64_t* L, int
         // With the C library's draws the host makes every state's rand() words.
         // The batch goes in sub-batches: the host draws sub-batch s+1 while the
         // GPU works on sub-batch s, all launches queued on the stream.  The
-        // first sub-batch is small, so the GPU starts after a short draw.
-        const int64_t sub = rng == CSIM_RNG_LIBC ? std::min<int64_t>(c, 1024) : c;
-        const int64_t sub0 = rng == CSIM_RNG_LIBC ? std::min<int64_t>(c, 256) : c;
+        // sub-batches grow 64, 256, 1024 states, so the GPU starts after a short
+        // draw and each draw stays shorter than the GPU's work on the one before.
+        int64_t ramp = rng == CSIM_RNG_LIBC ? 64 : c;
         bool first = true;
         for (int64_t s0 = 0, sb = 0; s0 < c; sb++) {
-            const int64_t cs = std::min(first ? sub0 : sub, c - s0);
+            const int64_t cs = std::min(ramp, c - s0);
+            ramp = std::min<int64_t>(4 * ramp, rng == CSIM_RNG_LIBC ? 1024 : c);
             csim::GState* sth = (csim::GState*)((csim_state*)dth + s0);
             int* scode = dcode + s0;
             if (rng == CSIM_RNG_LIBC) {

@@ -2,8 +2,8 @@
 benchmark workloads, against the oracle and the reference backend.
 
 * The reference-draw sampler (CSIM_RNG_LIBC) at counts that cross every
-  hand-off of the host sampler: the first sub-batch of 256 states, sub-batches
-  of 1024, and batches of 16384 states, with bins > 1.  Values within 1e-12
+  hand-off of the host sampler: sub-batches of 64, 256, then 1024 states, and
+  batches of 16384 states, with bins > 1.  Values within 1e-12
   relative of the oracle's multiSampledProjector on the same seed
   (libcirc/innerprod.c:23-84).
 * workload_c1.txt (the c1 query: t = 12, exact decomposition chi = 2^6,
@@ -53,11 +53,12 @@ def _projectors(t, rows):
 
 
 # ---------------------------------------------------------------- the libc-draw sampler at realistic L
-@pytest.mark.parametrize("t,k,samples,bins", [(40, 3, 257, 1), (40, 3, 2000, 1), (40, 2, 5900, 3), (24, 6, 1500, 2)])
+@pytest.mark.parametrize("t,k,samples,bins", [(40, 3, 65, 1), (40, 3, 321, 1), (40, 3, 2000, 1), (40, 2, 5900, 3),
+                                               (24, 6, 1500, 2)])
 def test_libc_sampler_at_realistic_counts(gpu, oracle, t, k, samples, bins):
-    """257 states: one past the first sub-batch; 2000: the reference's default
-    L, two sub-batch boundaries; 3 x 5900 = 17700: past the 16384-state batch
-    boundary, with a median over three bins."""
+    """65 and 321 states: one past the first (64) and second (256) sub-batch;
+    2000: the reference's default L, three sub-batch boundaries; 3 x 5900 =
+    17700: past the 16384-state batch boundary, with a median over three bins."""
     rs = np.random.RandomState(500 + samples)
     L = [rand_word(rs, t) for _ in range(k)]
     rows = random_projector_rows(rs, t, max(2, t // 6))
