@@ -208,6 +208,21 @@ CSIM_HD inline uint64_t wbrev(uint64_t x) {
 // all ones if the top bit of x is set (an arithmetic shift)
 CSIM_HD inline uint32_t topmask(uint32_t x) { return (uint32_t)((int32_t)x >> 31); }
 CSIM_HD inline uint64_t topmask(uint64_t x) { return (uint64_t)((int64_t)x >> 63); }
+// The row masks of a 16-byte unit of four rows: m[i] = topmask(c << i), i < 4.  On the
+// GPU one multiply puts bit 31 - i of c at the sign bit of byte 3 - i (copies of the top
+// nibble at bits 7, 14, 21, 28, which do not overlap), and one prmt per row replicates
+// that byte's sign over the word: one logic op per row instead of two shifts.
+CSIM_HD inline void unit_masks(uint32_t c, uint32_t (&m)[4]) {
+#ifdef __CUDA_ARCH__
+    const uint32_t s = (c >> 28) * 0x10204080u;
+    asm("prmt.b32 %0, %1, 0, 0xBBBB;" : "=r"(m[0]) : "r"(s));
+    asm("prmt.b32 %0, %1, 0, 0xAAAA;" : "=r"(m[1]) : "r"(s));
+    asm("prmt.b32 %0, %1, 0, 0x9999;" : "=r"(m[2]) : "r"(s));
+    asm("prmt.b32 %0, %1, 0, 0x8888;" : "=r"(m[3]) : "r"(s));
+#else
+    for (int i = 0; i < 4; i++) m[i] = topmask(c << i);
+#endif
+}
 
 struct PairRegs {
     int k, Q;
@@ -1094,10 +1109,13 @@ CSIM_HD inline void md_rank2(const PairMem& M, int KX, W Ji, W U, W C) {
         for (int x = 0; x < K32; x += 4) {
             U32x4* pr = reinterpret_cast<U32x4*>(&R32(x));
             U32x4 v = *pr;
-            v.a ^= (Ji32 & topmask(cu)) ^ (U32 & topmask(cc));
-            v.b ^= (Ji32 & topmask(cu << 1)) ^ (U32 & topmask(cc << 1));
-            v.c ^= (Ji32 & topmask(cu << 2)) ^ (U32 & topmask(cc << 2));
-            v.d ^= (Ji32 & topmask(cu << 3)) ^ (U32 & topmask(cc << 3));
+            uint32_t mu[4], mc[4];
+            unit_masks(cu, mu);
+            unit_masks(cc, mc);
+            v.a ^= (Ji32 & mu[0]) ^ (U32 & mc[0]);
+            v.b ^= (Ji32 & mu[1]) ^ (U32 & mc[1]);
+            v.c ^= (Ji32 & mu[2]) ^ (U32 & mc[2]);
+            v.d ^= (Ji32 & mu[3]) ^ (U32 & mc[3]);
             cu <<= 4;
             cc <<= 4;
             *pr = v;
@@ -1234,10 +1252,13 @@ CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64
             for (int x = X0; x < X1a; x += 4) {
                 U32x4* pr = reinterpret_cast<U32x4*>(&R32(x));
                 U32x4 v = *pr;
-                v.a ^= (P32 & topmask(cvb)) ^ (Q32 & topmask(cva));
-                v.b ^= (P32 & topmask(cvb << 1)) ^ (Q32 & topmask(cva << 1));
-                v.c ^= (P32 & topmask(cvb << 2)) ^ (Q32 & topmask(cva << 2));
-                v.d ^= (P32 & topmask(cvb << 3)) ^ (Q32 & topmask(cva << 3));
+                uint32_t mb[4], ma[4];
+                unit_masks(cvb, mb);
+                unit_masks(cva, ma);
+                v.a ^= (P32 & mb[0]) ^ (Q32 & ma[0]);
+                v.b ^= (P32 & mb[1]) ^ (Q32 & ma[1]);
+                v.c ^= (P32 & mb[2]) ^ (Q32 & ma[2]);
+                v.d ^= (P32 & mb[3]) ^ (Q32 & ma[3]);
                 cvb <<= 4;
                 cva <<= 4;
                 *pr = v;
