@@ -1240,16 +1240,15 @@ CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64
         // and finding it costs more than the rows it would skip
         const W zm = upd ? Ep : (W)0;
         const int hi = zm ? T::bits - T::clz(zm) : 0;
-        const int X0 = 0, X1 = uniform_max(hi);
+        const int X1 = uniform_max(hi);
         if (live) CSIM_COUNT_ROWS((dimer ? 2 : 1) + (upd ? hi - (T::ffs(zm) - 1) : 0));
-        const W rvb = wbrev(vb), rva = wbrev(va);
+        const W rvb = wbrev(vb), rva = wbrev(va);  // row x's bits at bit T::bits - 1 - x
         {
             const int sh = T::bits - 32;
-            const int s0 = X0 < 32 ? X0 : 0;
             const uint32_t P32 = (uint32_t)Pm, Q32 = (uint32_t)Qm;
-            uint32_t cvb = (uint32_t)(rvb >> sh) << s0, cva = (uint32_t)(rva >> sh) << s0;
+            uint32_t cvb = (uint32_t)(rvb >> sh), cva = (uint32_t)(rva >> sh);
             const int X1a = X1 < 32 ? X1 : 32;
-            for (int x = X0; x < X1a; x += 4) {
+            for (int x = 0; x < X1a; x += 4) {
                 U32x4* pr = reinterpret_cast<U32x4*>(&R32(x));
                 U32x4 v = *pr;
                 uint32_t mb[4], ma[4];
@@ -1265,10 +1264,8 @@ CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64
             }
         }
         if (sizeof(W) == 8) {
-            const int x0 = X0 > 32 ? (X0 & ~1) : 32;
-            const int s1 = x0 & (T::bits - 1);
-            W cvb = rvb << s1, cva = rva << s1;
-            for (int x = x0; x < X1; x += 2) {
+            W cvb = rvb << (32 & (T::bits - 1)), cva = rva << (32 & (T::bits - 1));  // rows from 32
+            for (int x = 32; x < X1; x += 2) {
                 U64x2* pr = reinterpret_cast<U64x2*>(&R64(x));
                 U64x2 v = *pr;
                 v.a ^= (uint64_t)((Pm & topmask(cvb)) ^ (Qm & topmask(cva)));
@@ -1282,8 +1279,9 @@ CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64
                 R64(sidx) ^= (uint64_t)((wget<W>(rb, sidx) ? vb : (W)0) ^ (wget<W>(ra, sidx) ? va : (W)0));
         }
     }
-    if (upd)  // the dimer's D update of the rows in Ep; D1 is zero at a and b, so only D2 changes
-        D2 ^= (db2 ? vb : (W)0) ^ (da2 ? va : (W)0) ^ (vb & va);  // (vb & rb) = (va & ra) cancel
+    // the dimer's D update of the rows in Ep: D1 is zero at a and b, so only D2 changes, and the
+    // full update's terms vb & rb and va & ra are both ra & rb & Ep, so they cancel
+    if (upd) D2 ^= (db2 ? vb : (W)0) ^ (da2 ? va : (W)0) ^ (vb & va);
     if (live) E = Ep;
     E64 = (uint64_t)E;
 }
