@@ -1211,7 +1211,7 @@ CSIM_HD_INLINE void md_exp_step(const PairMem& M, uint64_t& E64, uint64_t keep64
     const int KP = live ? 64 - hd_clz64((uint64_t)(E | keep | es)) : 0;
     const int a = live ? T::bits - 1 - T::clz(E) : 0;
     const W ra = live ? md_read_row<W>(M, a, KP) : (W)0;
-    const W K = ra & E & ~wbit<W>(a);
+    const W K = ra & E;  // J_aa = D1_a = 0: bit a of row a is clear
     const bool dimer = K != (W)0;
     const int b = dimer ? T::bits - 1 - T::clz(K) : 0;
     const W rb = dimer ? md_read_row<W>(M, b, KP) : (W)0;
@@ -1306,7 +1306,7 @@ CSIM_HD inline void md_exp_sum(PairRegs& s, const PairMem& M, uint64_t F, bool a
         const int a = upd ? T::ffs(Sm) - 1 : 0;
         const W U = Sm & ~wbit<W>(a);
         const W Ja = upd ? md_read_row<W>(M, a, KP) : (W)0;
-        const W C = Ja ^ (wget<W>(Ja, a) ? U : (W)0);
+        const W C = Ja ^ U;  // J_aa = D1_a = 1 at the substituted variable
         const int KX = uniform_max(upd ? KP : 0);
         if (upd && U != (W)0) md_rank2<W>(M, KX, Ja, U, C);
         if (upd) CSIM_COUNT_ROWS(U != (W)0 ? 1 + KP : 1);
@@ -1432,6 +1432,38 @@ CSIM_HD_INLINE uint32_t shl32_upto32(uint32_t x, int s) {
 #endif
 }
 
+// Four words' low bytes (kLanes 4: into one word, byte q from word q) or two
+// words' low 16-bit halves (kLanes 2: into two words), and back (lane q of
+// the packed words, zero-extended).  Byte permutes on the GPU.
+template <int kLanes>
+CSIM_HD_INLINE void pack_lanes(const uint32_t (&h)[4], uint32_t (&out)[2]) {
+#ifdef __CUDA_ARCH__
+    if (kLanes == 4) {
+        out[0] = __byte_perm(__byte_perm(h[0], h[1], 0x0040), __byte_perm(h[2], h[3], 0x0040), 0x5410);
+    } else {
+        out[0] = __byte_perm(h[0], h[1], 0x5410);
+        out[1] = __byte_perm(h[2], h[3], 0x5410);
+    }
+#else
+    if (kLanes == 4) {
+        out[0] = (h[0] & 0xFFu) | ((h[1] & 0xFFu) << 8) | ((h[2] & 0xFFu) << 16) | ((h[3] & 0xFFu) << 24);
+    } else {
+        out[0] = (h[0] & 0xFFFFu) | (h[1] << 16);
+        out[1] = (h[2] & 0xFFFFu) | (h[3] << 16);
+    }
+#endif
+}
+template <int kLanes>
+CSIM_HD_INLINE uint32_t unpack_lane(const uint32_t (&c)[2], int q) {
+#ifdef __CUDA_ARCH__
+    if (kLanes == 4) return __byte_perm(c[0], 0u, 0x4440u | (unsigned)q);
+    return __byte_perm(c[q >> 1], 0u, (q & 1) ? 0x4432u : 0x4410u);
+#else
+    if (kLanes == 4) return (c[0] >> (8 * q)) & 0xFFu;
+    return (c[q >> 1] >> (16 * (q & 1))) & 0xFFFFu;
+#endif
+}
+
 // How pair_direct compresses a pair's words, by the warp's live coordinates:
 // all below 32 (kCompactLow); some at or above 32 but at most 32 live
 // variables in every lane, so every compressed word fits 32 bits
@@ -1469,7 +1501,6 @@ CSIM_HD_INLINE void direct_compact(const Canon& cs, const uint64_t* Jc, const ui
     // rows share compresses, four bytes or two 16-bit halves to a word: the move masks repeated
     // in each lane move every lane's bits within it
     constexpr int kLanes = RHI == 3 ? 4 : (RHI == 4 ? 2 : 1);
-    constexpr int kLaneBits = 32 / kLanes;
     constexpr uint32_t kLaneMask = kLanes == 4 ? 0xFFu : 0xFFFFu;
     constexpr uint32_t kRepeat = kLanes == 4 ? 0x01010101u : 0x00010001u;
     const bool pack = MODE == kCompactSplit && kLanes > 1;
@@ -1481,7 +1512,7 @@ CSIM_HD_INLINE void direct_compact(const Canon& cs, const uint64_t* Jc, const ui
     }
     for (int u = 0; 4 * u < (fmax < 32 ? fmax : 32); u++) {
         uint32_t w[4];
-        uint32_t hb[4] = {0u, 0u, 0u, 0u};
+        uint32_t hi[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const bool inlo = MODE == kCompactLow || rl != 0u;
@@ -1491,18 +1522,18 @@ CSIM_HD_INLINE void direct_compact(const Canon& cs, const uint64_t* Jc, const ui
             const uint64_t row = Jc[c & 63];
             if (pack) {
                 w[q] = compress32<5>((uint32_t)row, nlo);
-                hb[q / kLanes] |= ((uint32_t)(row >> 32) & kLaneMask) << (kLaneBits * (q % kLanes));
+                hi[q] = (uint32_t)(row >> 32);
             } else {
                 w[q] = (uint32_t)compress_word<MODE, RHI>(row, nlo, nhi, plo);
             }
         }
         if (pack) {
-            uint32_t hc[4];
+            uint32_t hb[2], hc[2];
+            pack_lanes<kLanes>(hi, hb);
 #pragma unroll
             for (int g = 0; g < 4 / kLanes; g++) hc[g] = compress32<RHI>(hb[g], nrep);
 #pragma unroll
-            for (int q = 0; q < 4; q++)
-                w[q] |= shl32_upto32((hc[q / kLanes] >> (kLaneBits * (q % kLanes))) & kLaneMask, plo);
+            for (int q = 0; q < 4; q++) w[q] |= shl32_upto32(unpack_lane<kLanes>(hc, q), plo);
         }
         if (4 * u < f) {
             U32x4 v;
