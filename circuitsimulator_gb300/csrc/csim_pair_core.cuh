@@ -1395,6 +1395,7 @@ CSIM_HD inline void md_exp_sum(PairRegs& s, const PairMem& M, uint64_t F, bool a
 // bit by up to 2^R - 1, which is enough when m has no bit at or above 2^R.
 struct CompressNet {
     uint32_t m, mv[5];
+    uint32_t keep0;  // m & ~mv[0]: the bits of m that stay in round 0
 };
 template <int R>
 CSIM_HD_INLINE CompressNet compress_net(uint32_t m) {
@@ -1411,13 +1412,16 @@ CSIM_HD_INLINE CompressNet compress_net(uint32_t m) {
         m = (m ^ mv) | (mv >> (1 << i));
         mk &= ~mp;
     }
+    c.keep0 = R > 0 ? c.m & ~c.mv[0] : c.m;
     return c;
 }
 template <int R>
 CSIM_HD_INLINE uint32_t compress32(uint32_t x, const CompressNet& c) {
-    x &= c.m;
+    if (R == 0) return x & c.m;
+    // round 0 with the mask by m folded in (mv[0] lies within m)
+    x = (x & c.keep0) | ((x & c.mv[0]) >> 1);
 #pragma unroll
-    for (int i = 0; i < R; i++) {
+    for (int i = 1; i < R; i++) {
         const uint32_t t = x & c.mv[i];
         x = (x ^ t) | (t >> (1 << i));
     }
@@ -1509,6 +1513,7 @@ CSIM_HD_INLINE void direct_compact(const Canon& cs, const uint64_t* Jc, const ui
         nrep.m = (nhi.m & kLaneMask) * kRepeat;
 #pragma unroll
         for (int i = 0; i < RHI && i < 5; i++) nrep.mv[i] = (nhi.mv[i] & kLaneMask) * kRepeat;
+        nrep.keep0 = nrep.m & ~nrep.mv[0];
     }
     for (int u = 0; 4 * u < (fmax < 32 ? fmax : 32); u++) {
         uint32_t w[4];
