@@ -181,6 +181,31 @@ def test_runs_vs_oracle(tp, oracle, t, k, run_len):
             w += 1
 
 
+@pytest.mark.parametrize("t", [8, 24, 40, 64])
+def test_j_diagonal_is_d1(oracle, t):
+    """The direct kernel's exponential sum leaves out the J_aa, J_bb terms of its
+    dimer steps and the bit-a mask of its dimer search (csim_pair_core.cuh,
+    md_exp_step): it takes J's diagonal to be D1 (J_xx = D_x/2 mod 2), which is
+    zero on the variables it eliminates.  That holds for every state the
+    reference's own operations make: drawn (randomStabilizerState), projected
+    (measurePauli) and shrunk."""
+    rs = np.random.RandomState(4400 + t)
+    thetas = list(_projected_thetas(oracle, rs, t, count=6))
+    r = oracle.rng(t + 1)
+    thetas += [oracle.random_state(t, r)[0] for _ in range(6)]
+    checked = 0
+    for th in thetas:
+        one = np.array([th])
+        for step in range(4):
+            k = int(one["k"][0])
+            d1 = int(one["D1"][0])
+            for a in range(k):
+                assert (int(one["J"][0][a]) >> a) & 1 == (d1 >> a) & 1, (t, step, a)
+            checked += k
+            oracle.shrink(one, rand_word(rs, t), int(rs.randint(2)), 0)
+    assert checked > 0
+
+
 @pytest.mark.parametrize("t,k,nshrink", [(1, 1, 0), (3, 3, 0), (8, 4, 0), (12, 6, 4), (24, 8, 0), (33, 8, 0),
                                          (40, 10, 0), (40, 10, 20), (44, 9, 0), (48, 9, 6), (57, 8, 0), (64, 9, 0),
                                          (64, 8, 40)])
